@@ -1,0 +1,357 @@
+// Operator application on packed product states (warp per input state).
+//
+// apply_columns: H|b> for single product states b (upstream finite.applyOp with {b: 1},
+//   impurityModel/ed/finite.py:1301-1511).  Terms that map a state onto itself ("diagonal"
+//   terms, flag bit 0) are accumulated in term order by warp shuffles; the few off-diagonal
+//   emissions go to a per-warp shared-memory buffer where equal output states are merged in
+//   term order.  This reproduces upstream's sequential dict sums bit for bit.
+// apply_vector: raw emissions of an operator on a weighted multi-state psi, in (state, term)
+//   order, for a later stable sort + segmented sum.
+#include "common.cuh"
+
+namespace edgpu {
+
+struct ColParams {
+  const uint64_t* states;
+  int64_t n_states;
+  const uint64_t* ops;
+  const double2* coeff;
+  const uint32_t* flags;
+  int n_terms;
+  Restr restr;
+  double weight_min;
+  const uint64_t* basis;
+  int64_t n_basis;
+  int filter;
+  const int64_t* offsets;
+  int64_t* counts;
+  uint64_t* out_states;
+  int64_t* out_index;
+  double2* out_vals;
+  int conj_vals;
+  int cap;
+  int stage_terms;
+  int32_t* status;
+};
+
+template <int W>
+__device__ __forceinline__ bool filter_pass(const ColParams& p, const uint64_t (&s)[W], int64_t& idx) {
+  idx = -1;
+  if (p.filter == EDGPU_FILTER_NONE) return true;
+  idx = find_state<W>(p.basis, p.n_basis, s);
+  return p.filter == EDGPU_FILTER_IN_BASIS ? (idx >= 0) : (idx < 0);
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int T = p.n_terms;
+
+  const double2* scoeff = p.coeff;
+  const uint64_t* sops = p.ops;
+  const uint32_t* sflags = p.flags;
+  size_t off = 0;
+  if (p.stage_terms) {
+    double2* c = reinterpret_cast<double2*>(smem);
+    uint64_t* o = reinterpret_cast<uint64_t*>(smem + 16 * (size_t)T);
+    uint32_t* f = reinterpret_cast<uint32_t*>(smem + 24 * (size_t)T);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+      c[t] = p.coeff[t];
+      o[t] = p.ops[t];
+      f[t] = p.flags[t];
+    }
+    scoeff = c;
+    sops = o;
+    sflags = f;
+    off = (28 * (size_t)T + 15) & ~(size_t)15;
+    __syncthreads();
+  }
+  const int cap = p.cap;
+  const size_t per_warp = (size_t)cap * (16 + 8 * W + 4);
+  unsigned char* wbase = smem + off + per_warp * warp;
+  double2* wvals = reinterpret_cast<double2*>(wbase);
+  uint64_t* wkeys = reinterpret_cast<uint64_t*>(wbase + 16 * (size_t)cap);
+  int* wtidx = reinterpret_cast<int*>(wbase + (16 + 8 * W) * (size_t)cap);
+
+  const bool fill = p.offsets != nullptr;
+  for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += (int64_t)gridDim.x * wpb) {
+    uint64_t s0[W];
+    load_state<W>(p.states + j * W, s0);
+    double dre = 0.0, dim = 0.0;
+    int dfirst = -1;
+    int m = 0;
+    for (int base = 0; base < T; base += 32) {
+      const int t = base + lane;
+      bool valid = false, isdiag = false;
+      double vre = 0.0, vim = 0.0;
+      uint64_t s[W];
+#pragma unroll
+      for (int q = 0; q < W; ++q) s[q] = s0[q];
+      if (t < T) {
+        int par = 0;
+        valid = apply_term<W>(s, sops[t], par);
+        if (valid) {
+          double2 c = scoeff[t];
+          if (par & 1) {
+            c.x = -c.x;
+            c.y = -c.y;
+          }
+          vre = c.x;
+          vim = c.y;
+          isdiag = (sflags[t] & 1u) != 0;
+        }
+      }
+      unsigned bd = __ballot_sync(FULL, valid && isdiag);
+      const unsigned bo = __ballot_sync(FULL, valid && !isdiag);
+      while (bd) {
+        const int k = __ffs(bd) - 1;
+        bd &= bd - 1;
+        const double xr = __shfl_sync(FULL, vre, k);
+        const double xi = __shfl_sync(FULL, vim, k);
+        if (dfirst < 0) {
+          dre = xr;
+          dim = xi;
+          dfirst = base + k;
+        } else {
+          dre = __dadd_rn(dre, xr);
+          dim = __dadd_rn(dim, xi);
+        }
+      }
+      if (bo) {
+        const int pos = m + __popc(bo & ((1u << lane) - 1u));
+        if (valid && !isdiag && pos < cap) {
+#pragma unroll
+          for (int q = 0; q < W; ++q) wkeys[(size_t)pos * W + q] = s[q];
+          wvals[pos] = make_double2(vre, vim);
+          wtidx[pos] = t;
+        }
+        m += __popc(bo);
+      }
+    }
+    __syncwarp();
+    if (m > cap) {
+      if (lane == 0) {
+        atomicExch(p.status, (int32_t)EDGPU_ERR_OVERFLOW);
+        if (!fill) p.counts[j] = 0;
+      }
+      continue;
+    }
+    // Diagonal entry (output == input state).
+    bool dkeep = false;
+    int64_t didx = -1;
+    if (dfirst >= 0) {
+      dkeep = abs2_py(dre, dim) >= p.weight_min && restr_ok<W>(p.restr, s0);
+      if (dkeep) dkeep = filter_pass<W>(p, s0, didx);
+    }
+    int kept = 0;       // kept off-diagonal heads so far (warp uniform)
+    int dbefore = 0;    // kept heads with first term index < dfirst
+    const int64_t obase = fill ? p.offsets[j] : 0;
+    for (int c0 = 0; c0 < m; c0 += 32) {
+      const int k = c0 + lane;
+      bool keep = false;
+      double sre = 0.0, sim = 0.0;
+      int64_t idx = -1;
+      uint64_t key[W];
+      int tk = 0x7fffffff;
+      if (k < m) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)k * W + q];
+        bool head = true;
+        for (int e = 0; e < k; ++e) {
+          if (state_eq<W>(key, wkeys + (size_t)e * W)) {
+            head = false;
+            break;
+          }
+        }
+        if (head) {
+          double2 v = wvals[k];
+          sre = v.x;
+          sim = v.y;
+          for (int e = k + 1; e < m; ++e) {
+            if (state_eq<W>(key, wkeys + (size_t)e * W)) {
+              double2 u = wvals[e];
+              sre = __dadd_rn(sre, u.x);
+              sim = __dadd_rn(sim, u.y);
+            }
+          }
+          keep = abs2_py(sre, sim) >= p.weight_min && restr_ok<W>(p.restr, key);
+          if (keep) keep = filter_pass<W>(p, key, idx);
+          tk = wtidx[k];
+        }
+      }
+      const unsigned bk = __ballot_sync(FULL, keep);
+      const unsigned bb = __ballot_sync(FULL, keep && dkeep && tk < dfirst);
+      if (fill && keep) {
+        const int rank = kept + __popc(bk & ((1u << lane) - 1u)) + ((dkeep && dfirst < tk) ? 1 : 0);
+        const int64_t o = obase + rank;
+        if (p.out_states) store_state<W>(p.out_states + o * W, key);
+        if (p.out_index) p.out_index[o] = idx;
+        if (p.out_vals) p.out_vals[o] = make_double2(sre, p.conj_vals ? -sim : sim);
+      }
+      kept += __popc(bk);
+      dbefore += __popc(bb);
+    }
+    if (!fill) {
+      if (lane == 0) p.counts[j] = kept + (dkeep ? 1 : 0);
+    } else if (dkeep && lane == 0) {
+      const int64_t o = obase + dbefore;
+      if (p.out_states) store_state<W>(p.out_states + o * W, s0);
+      if (p.out_index) p.out_index[o] = didx;
+      if (p.out_vals) p.out_vals[o] = make_double2(dre, p.conj_vals ? -dim : dim);
+    }
+    __syncwarp();
+  }
+}
+
+struct VecParams {
+  const uint64_t* states;
+  const double2* amps;
+  int64_t n_states;
+  const uint64_t* ops;
+  const double2* coeff;
+  int n_terms;
+  Restr restr;
+  const int64_t* offsets;
+  int64_t* counts;
+  uint64_t* out_states;
+  double2* out_vals;
+};
+
+template <int W>
+__global__ void __launch_bounds__(256) apply_vector_kernel(VecParams p) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const bool fill = p.offsets != nullptr;
+  for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += (int64_t)gridDim.x * wpb) {
+    uint64_t s0[W];
+    load_state<W>(p.states + j * W, s0);
+    const double2 a = fill ? p.amps[j] : make_double2(0.0, 0.0);
+    int64_t run = fill ? p.offsets[j] : 0;
+    int cnt = 0;
+    for (int base = 0; base < p.n_terms; base += 32) {
+      const int t = base + lane;
+      uint64_t s[W];
+#pragma unroll
+      for (int q = 0; q < W; ++q) s[q] = s0[q];
+      bool valid = false;
+      int par = 0;
+      if (t < p.n_terms) {
+        valid = apply_term<W>(s, p.ops[t], par);
+        if (valid) valid = restr_ok<W>(p.restr, s);
+      }
+      const unsigned b = __ballot_sync(FULL, valid);
+      if (fill && valid) {
+        const double2 h = p.coeff[t];
+        // CPython complex product (no fused multiply-add), then the sign.
+        double re = __dsub_rn(__dmul_rn(a.x, h.x), __dmul_rn(a.y, h.y));
+        double im = __dadd_rn(__dmul_rn(a.x, h.y), __dmul_rn(a.y, h.x));
+        if (par & 1) {
+          re = -re;
+          im = -im;
+        }
+        const int64_t o = run + __popc(b & ((1u << lane) - 1u));
+        store_state<W>(p.out_states + o * W, s);
+        p.out_vals[o] = make_double2(re, im);
+      }
+      run += __popc(b);
+      cnt += __popc(b);
+    }
+    if (!fill && lane == 0) p.counts[j] = cnt;
+  }
+}
+
+}  // namespace edgpu
+
+using namespace edgpu;
+
+extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t n_states, const edgpu_terms* terms,
+                                   const edgpu_restrictions* restr, double weight_min, const uint64_t* basis,
+                                   int64_t n_basis, int filter, const int64_t* offsets, int64_t* counts,
+                                   uint64_t* out_states, int64_t* out_index, double* out_vals, int conj_vals,
+                                   int scratch_entries, int32_t* status_dev, void* stream) {
+  if (!terms || n_states < 0 || !status_dev) return EDGPU_ERR_ARG;
+  if (n_states == 0) return EDGPU_OK;
+  if (!states || (!offsets && !counts)) return EDGPU_ERR_ARG;
+  if (filter != EDGPU_FILTER_NONE && (!basis || n_basis < 0)) return EDGPU_ERR_ARG;
+  if (filter != EDGPU_FILTER_NONE && filter != EDGPU_FILTER_IN_BASIS && filter != EDGPU_FILTER_NOT_IN_BASIS)
+    return EDGPU_ERR_ARG;
+  if (restr && (restr->n < 0 || restr->n > EDGPU_MAX_RESTRICTIONS)) return EDGPU_ERR_ARG;
+  if (n_words < 1 || n_words > EDGPU_MAX_WORDS) return EDGPU_ERR_ARG;
+  ColParams p{};
+  p.states = states;
+  p.n_states = n_states;
+  p.ops = terms->ops;
+  p.coeff = reinterpret_cast<const double2*>(terms->coeff);
+  p.flags = terms->flags;
+  p.n_terms = terms->n_terms;
+  p.restr = make_restr(restr);
+  p.weight_min = weight_min;
+  p.basis = basis;
+  p.n_basis = n_basis;
+  p.filter = filter;
+  p.offsets = offsets;
+  p.counts = counts;
+  p.out_states = out_states;
+  p.out_index = out_index;
+  p.out_vals = reinterpret_cast<double2*>(out_vals);
+  p.conj_vals = conj_vals;
+  p.cap = scratch_entries > 0 ? scratch_entries : 256;
+  p.status = status_dev;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t term_bytes = (28 * (size_t)p.n_terms + 15) & ~(size_t)15;
+  const size_t per_warp = (size_t)p.cap * (16 + 8 * n_words + 4);
+  const size_t smem_max = 220 * 1024;
+  int warps = 8;
+  p.stage_terms = 1;
+  while (warps > 1 && term_bytes + per_warp * warps > smem_max) warps >>= 1;
+  if (term_bytes + per_warp * warps > smem_max) {
+    p.stage_terms = 0;
+    warps = 8;
+    while (warps > 1 && per_warp * warps > smem_max) warps >>= 1;
+    if (per_warp * warps > smem_max) return EDGPU_ERR_ARG;
+  }
+  const size_t smem = (p.stage_terms ? term_bytes : 0) + per_warp * warps;
+  const int threads = 32 * warps;
+  int64_t blocks = (n_states + warps - 1) / warps;
+  const int64_t cap_blocks = (int64_t)grid_cap() * 8;
+  if (blocks > cap_blocks) blocks = cap_blocks;
+  EDGPU_DISPATCH_W(n_words, {
+    cudaFuncSetAttribute(apply_columns_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    apply_columns_kernel<W><<<(unsigned)blocks, threads, smem, s>>>(p);
+  });
+  return check_launch();
+}
+
+extern "C" int edgpu_apply_vector(int n_words, const uint64_t* states, const double* amps, int64_t n_states,
+                                  const edgpu_terms* terms, const edgpu_restrictions* restr, const int64_t* offsets,
+                                  int64_t* counts, uint64_t* out_states, double* out_vals, void* stream) {
+  if (!terms || n_states < 0) return EDGPU_ERR_ARG;
+  if (n_states == 0) return EDGPU_OK;
+  if (!states || (!offsets && !counts)) return EDGPU_ERR_ARG;
+  if (offsets && (!amps || !out_states || !out_vals)) return EDGPU_ERR_ARG;
+  if (restr && (restr->n < 0 || restr->n > EDGPU_MAX_RESTRICTIONS)) return EDGPU_ERR_ARG;
+  VecParams p{};
+  p.states = states;
+  p.amps = reinterpret_cast<const double2*>(amps);
+  p.n_states = n_states;
+  p.ops = terms->ops;
+  p.coeff = reinterpret_cast<const double2*>(terms->coeff);
+  p.n_terms = terms->n_terms;
+  p.restr = make_restr(restr);
+  p.offsets = offsets;
+  p.counts = counts;
+  p.out_states = out_states;
+  p.out_vals = reinterpret_cast<double2*>(out_vals);
+  const int threads = 256;
+  int64_t blocks = (n_states + 7) / 8;
+  const int64_t cap_blocks = (int64_t)grid_cap() * 8;
+  if (blocks > cap_blocks) blocks = cap_blocks;
+  EDGPU_DISPATCH_W(n_words, { apply_vector_kernel<W><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p); });
+  return check_launch();
+}

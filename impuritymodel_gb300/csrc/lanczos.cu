@@ -1,0 +1,587 @@
+// Sparse H·v, batched Lanczos tridiagonalisation, Lanczos with full reorthogonalisation,
+// Ritz/shifted-solve vector assembly and continued fractions.
+//
+// Upstream counterparts: get_tridiagonal_krylov_vectors (impurityModel/ed/finite.py:1897-1995),
+// scipy eigsh in eigensystem (finite.py:105), BiCGSTAB in getRIXSmap (spectra.py:962,1080)
+// and the continued fraction of getGreen (spectra.py:678-680).
+//
+// Vectors of a batch are stored [n][R] (run index fastest) so that the R threads of one
+// row read the row's CSR entries once (broadcast) and gather x[col][0..R) contiguously.
+// All reductions are deterministic: per-block partials in fixed order, summed in fixed order.
+#include "common.cuh"
+
+namespace edgpu {
+
+template <typename T>
+struct Cx;
+template <>
+struct Cx<double> {
+  using V = double2;
+};
+template <>
+struct Cx<float> {
+  using V = float2;
+};
+
+__device__ __forceinline__ double2 ld(const double2* p) { return *p; }
+__device__ __forceinline__ float2 ld(const float2* p) { return *p; }
+
+struct RunTile {
+  int rt;   // runs per block (blockDim.x)
+  int rb;   // rows per block pass (blockDim.y)
+  int nrb;  // row blocks (gridDim.x)
+  int nrt;  // run tiles (gridDim.y)
+};
+
+inline RunTile make_tile(int64_t n, int R) {
+  RunTile t;
+  t.rt = R < 32 ? R : 32;
+  t.rb = 256 / t.rt;
+  if (t.rb < 1) t.rb = 1;
+  t.nrt = (R + t.rt - 1) / t.rt;
+  int64_t nrb = (n + t.rb - 1) / t.rb;
+  const int64_t cap = (int64_t)grid_cap() * 4;
+  if (nrb > cap) nrb = cap;
+  if (nrb < 1) nrb = 1;
+  t.nrb = (int)nrb;
+  return t;
+}
+
+// Y = H X and alpha partial Re<Y, X> per run.  T: vector/accumulation scalar, VALC: complex values.
+template <typename T, bool VALC>
+__global__ void spmm_alpha_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                  const T* __restrict__ vals, int R, const typename Cx<T>::V* __restrict__ X,
+                                  typename Cx<T>::V* __restrict__ Y, double* __restrict__ partial, int with_alpha) {
+  using V = typename Cx<T>::V;
+  extern __shared__ double red[];
+  const int tr = threadIdx.x, ti = threadIdx.y;
+  const int r = blockIdx.y * blockDim.x + tr;
+  double acc = 0.0;
+  if (r < R) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
+      T yr = 0, yi = 0;
+      const int64_t e1 = rp[i + 1];
+      for (int64_t e = rp[i]; e < e1; ++e) {
+        const int c = col[e];
+        const V x = ld(X + (int64_t)c * R + r);
+        if (VALC) {
+          const T hr = vals[2 * e], hi = vals[2 * e + 1];
+          yr += hr * x.x - hi * x.y;
+          yi += hr * x.y + hi * x.x;
+        } else {
+          const T h = vals[e];
+          yr += h * x.x;
+          yi += h * x.y;
+        }
+      }
+      V y;
+      y.x = yr;
+      y.y = yi;
+      Y[i * R + r] = y;
+      if (with_alpha) {
+        const V v = ld(X + i * R + r);
+        acc += (double)yr * (double)v.x + (double)yi * (double)v.y;
+      }
+    }
+  }
+  if (!with_alpha) return;
+  red[ti * blockDim.x + tr] = acc;
+  __syncthreads();
+  if (ti == 0 && r < R) {
+    double s = 0.0;
+    for (int k = 0; k < (int)blockDim.y; ++k) s += red[k * blockDim.x + tr];
+    partial[(int64_t)blockIdx.x * R + r] = s;
+  }
+}
+
+// alpha_r = sum of partials; W = Y - alpha Vc - beta_prev Vp; beta partial ||W||^2.
+template <typename T>
+__global__ void axpy_beta_kernel(int64_t n, int R, typename Cx<T>::V* __restrict__ Y,
+                                 const typename Cx<T>::V* __restrict__ Vc, const typename Cx<T>::V* __restrict__ Vp,
+                                 const double* __restrict__ palpha, int nrb, const double* __restrict__ beta_prev,
+                                 double* __restrict__ alpha_out, int K, int j, double* __restrict__ pbeta) {
+  using V = typename Cx<T>::V;
+  extern __shared__ double red[];
+  const int tr = threadIdx.x, ti = threadIdx.y;
+  const int r = blockIdx.y * blockDim.x + tr;
+  double acc = 0.0;
+  if (r < R) {
+    double a = 0.0;
+    for (int b = 0; b < nrb; ++b) a += palpha[(int64_t)b * R + r];
+    const double bp = beta_prev ? beta_prev[(int64_t)r * K + (j - 1)] : 0.0;
+    if (blockIdx.x == 0 && ti == 0) alpha_out[(int64_t)r * K + j] = a;
+    const T af = (T)a, bf = (T)bp;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
+      V y = Y[i * R + r];
+      const V c = ld(Vc + i * R + r);
+      y.x -= af * c.x;
+      y.y -= af * c.y;
+      if (Vp) {
+        const V p = ld(Vp + i * R + r);
+        y.x -= bf * p.x;
+        y.y -= bf * p.y;
+      }
+      Y[i * R + r] = y;
+      acc += (double)y.x * (double)y.x + (double)y.y * (double)y.y;
+    }
+  }
+  red[ti * blockDim.x + tr] = acc;
+  __syncthreads();
+  if (ti == 0 && r < R) {
+    double s = 0.0;
+    for (int k = 0; k < (int)blockDim.y; ++k) s += red[k * blockDim.x + tr];
+    pbeta[(int64_t)blockIdx.x * R + r] = s;
+  }
+}
+
+// beta_r = sqrt(sum partials); Vn = W / beta.
+template <typename T>
+__global__ void normalize_kernel(int64_t n, int R, const typename Cx<T>::V* __restrict__ Wv,
+                                 typename Cx<T>::V* __restrict__ Vn, const double* __restrict__ pbeta, int nrb,
+                                 double* __restrict__ beta_out, int K, int j, const int32_t* __restrict__ k_max,
+                                 int32_t* status) {
+  using V = typename Cx<T>::V;
+  const int tr = threadIdx.x, ti = threadIdx.y;
+  const int r = blockIdx.y * blockDim.x + tr;
+  if (r >= R) return;
+  double s = 0.0;
+  for (int b = 0; b < nrb; ++b) s += pbeta[(int64_t)b * R + r];
+  const double beta = sqrt(s);
+  const bool active = k_max[r] > j + 1;
+  if (blockIdx.x == 0 && ti == 0) {
+    beta_out[(int64_t)r * K + j] = beta;
+    if (active && !(beta > 0.0)) atomicExch(status, (int32_t)(beta == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+  }
+  const T inv = beta > 0.0 ? (T)(1.0 / beta) : (T)0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
+    V w = Wv[i * R + r];
+    V o;
+    if (sizeof(T) == 8) {
+      // upstream divides: v = w / beta
+      o.x = beta > 0.0 ? (T)((double)w.x / beta) : (T)0;
+      o.y = beta > 0.0 ? (T)((double)w.y / beta) : (T)0;
+    } else {
+      o.x = w.x * inv;
+      o.y = w.y * inv;
+    }
+    Vn[i * R + r] = o;
+  }
+}
+
+__global__ void to_c64_kernel(const double2* in, float2* out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = in[i];
+    out[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__global__ void copy_c128_kernel(const double2* in, double2* out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+// ---------------------------------------------------------------------------------------
+// Full reorthogonalisation: dots h[k] = <V_k, w>, k < m; then w -= sum_k h[k] V_k.
+// ---------------------------------------------------------------------------------------
+constexpr int kDotTile = 8;
+
+__global__ void multidot_kernel(const double2* __restrict__ V, int m, int64_t n, const double2* __restrict__ w,
+                                double2* __restrict__ partial) {
+  __shared__ double2 red[kDotTile][256 / 32];
+  const int k0 = blockIdx.y * kDotTile;
+  double2 acc[kDotTile];
+#pragma unroll
+  for (int k = 0; k < kDotTile; ++k) acc[k] = make_double2(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 x = w[i];
+#pragma unroll
+    for (int k = 0; k < kDotTile; ++k) {
+      if (k0 + k < m) {
+        const double2 v = V[(int64_t)(k0 + k) * n + i];
+        acc[k].x += v.x * x.x + v.y * x.y;
+        acc[k].y += v.x * x.y - v.y * x.x;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kDotTile; ++k) {
+    double a = acc[k].x, b = acc[k].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) red[k][warp] = make_double2(a, b);
+  }
+  __syncthreads();
+  if (threadIdx.x < kDotTile && k0 + threadIdx.x < m) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      a += red[threadIdx.x][q].x;
+      b += red[threadIdx.x][q].y;
+    }
+    partial[(int64_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = make_double2(a, b);
+  }
+}
+
+__global__ void sum_partials_kernel(const double2* partial, int m, int nb, double2* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  double a = 0.0, b = 0.0;
+  for (int q = 0; q < nb; ++q) {
+    a += partial[(int64_t)k * nb + q].x;
+    b += partial[(int64_t)k * nb + q].y;
+  }
+  out[k] = make_double2(a, b);
+}
+
+__global__ void subtract_proj_kernel(const double2* __restrict__ V, int m, int64_t n, const double2* __restrict__ h,
+                                     double2* __restrict__ w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double2 x = w[i];
+    for (int k = 0; k < m; ++k) {
+      const double2 c = h[k];
+      const double2 v = V[(int64_t)k * n + i];
+      x.x -= c.x * v.x - c.y * v.y;
+      x.y -= c.x * v.y + c.y * v.x;
+    }
+    w[i] = x;
+  }
+}
+
+// Single-run helpers for the reorthogonalised Lanczos (R == 1 specialisations).
+__global__ void reorth_alpha_update_kernel(int64_t n, double2* w, const double2* vj, const double2* vjm1,
+                                           const double* palpha, int nrb, double* alpha, const double* beta, int j,
+                                           double* pnorm) {
+  __shared__ double red[256];
+  double a = 0.0;
+  for (int b = 0; b < nrb; ++b) a += palpha[b];
+  if (blockIdx.x == 0 && threadIdx.x == 0) alpha[j] = a;
+  const double bp = (j > 0) ? beta[j - 1] : 0.0;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double2 y = w[i];
+    const double2 c = vj[i];
+    y.x -= a * c.x;
+    y.y -= a * c.y;
+    if (j > 0) {
+      const double2 p = vjm1[i];
+      y.x -= bp * p.x;
+      y.y -= bp * p.y;
+    }
+    w[i] = y;
+    acc += y.x * y.x + y.y * y.y;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)blockDim.x; ++k) s += red[k];
+    pnorm[blockIdx.x] = s;
+  }
+}
+
+__global__ void norm_partial_kernel(int64_t n, const double2* w, double* pnorm) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 y = w[i];
+    acc += y.x * y.x + y.y * y.y;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)blockDim.x; ++k) s += red[k];
+    pnorm[blockIdx.x] = s;
+  }
+}
+
+__global__ void reorth_normalize_kernel(int64_t n, const double2* w, double2* vnext, const double* pnorm, int nb,
+                                        double* beta, int j, int32_t* status) {
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += pnorm[b];
+  const double bt = sqrt(s);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    beta[j] = bt;
+    if (!(bt > 0.0)) atomicExch(status, (int32_t)(bt == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 y = w[i];
+    vnext[i] = bt > 0.0 ? make_double2(y.x / bt, y.y / bt) : make_double2(0.0, 0.0);
+  }
+}
+
+// X[m][i] = sum_k C[k][m] V[k][i]
+__global__ void combine_kernel(const double2* __restrict__ V, int K, int64_t n, const double2* __restrict__ C, int M,
+                               double2* __restrict__ X) {
+  const int m = blockIdx.y;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double xr = 0.0, xi = 0.0;
+    for (int k = 0; k < K; ++k) {
+      const double2 c = C[(int64_t)k * M + m];
+      const double2 v = V[(int64_t)k * n + i];
+      xr += c.x * v.x - c.y * v.y;
+      xi += c.x * v.y + c.y * v.x;
+    }
+    X[(int64_t)m * n + i] = make_double2(xr, xi);
+  }
+}
+
+// Continued fraction, thread per (run, omega).
+__global__ void cfrac_kernel(const double* __restrict__ alpha, const double* __restrict__ beta,
+                             const int32_t* __restrict__ k_len, int K, int R, const double* __restrict__ omega,
+                             int n_omega, double delta, const double* __restrict__ e, const double* __restrict__ scale,
+                             double2* __restrict__ g) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (int64_t)R * n_omega) return;
+  const int r = (int)(tid / n_omega);
+  const int w = (int)(tid % n_omega);
+  const int kl = k_len[r];
+  const double zr = omega[w] + e[r];
+  const double zi = delta;
+  double gr = 0.0, gi = 0.0;
+  const double* a = alpha + (int64_t)r * K;
+  const double* b = beta + (int64_t)r * K;
+  for (int i = kl - 1; i >= 0; --i) {
+    double dr = zr - a[i];
+    double di = zi;
+    if (i != kl - 1) {
+      const double b2 = b[i] * b[i];
+      dr -= b2 * gr;
+      di -= b2 * gi;
+    }
+    // g = 1 / (dr + i di), Smith's algorithm
+    if (fabs(dr) >= fabs(di)) {
+      const double q = di / dr;
+      const double den = dr + di * q;
+      gr = 1.0 / den;
+      gi = -q / den;
+    } else {
+      const double q = dr / di;
+      const double den = dr * q + di;
+      gr = q / den;
+      gi = -1.0 / den;
+    }
+  }
+  const double s = scale ? scale[r] : 1.0;
+  g[tid] = kl > 0 ? make_double2(s * gr, s * gi) : make_double2(0.0, 0.0);
+}
+
+inline unsigned grid_1d(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)grid_cap() * 8;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+template <typename T>
+int spmv_impl(const edgpu_csr* h, const typename Cx<T>::V* x, typename Cx<T>::V* y, int R, cudaStream_t s) {
+  RunTile t = make_tile(h->n, R);
+  dim3 grid(t.nrb, t.nrt), block(t.rt, t.rb);
+  if (sizeof(T) == 8) {
+    if (h->val_c)
+      spmm_alpha_kernel<T, true><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_c, R,
+                                                        x, y, nullptr, 0);
+    else
+      spmm_alpha_kernel<T, false><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_r, R,
+                                                         x, y, nullptr, 0);
+  } else {
+    if (h->val_cf)
+      spmm_alpha_kernel<T, true><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_cf, R,
+                                                        x, y, nullptr, 0);
+    else
+      spmm_alpha_kernel<T, false><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_rf, R,
+                                                         x, y, nullptr, 0);
+  }
+  return check_launch();
+}
+
+template <typename T>
+int lanczos_impl(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha, double* beta,
+                 int32_t* status, unsigned char* ws, size_t ws_bytes, cudaStream_t s) {
+  using V = typename Cx<T>::V;
+  const int64_t n = h->n;
+  const int64_t nv = n * (int64_t)R;
+  RunTile t = make_tile(n, R);
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    unsigned char* p = ws + off;
+    off += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  V* A = reinterpret_cast<V*>(carve(sizeof(V) * nv));
+  V* B = reinterpret_cast<V*>(carve(sizeof(V) * nv));
+  V* Wb = reinterpret_cast<V*>(carve(sizeof(V) * nv));
+  double* pa = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)t.nrb * R));
+  double* pb = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)t.nrb * R));
+  if (off > ws_bytes) return EDGPU_ERR_WORKSPACE;
+  if (sizeof(T) == 8)
+    copy_c128_kernel<<<grid_1d(nv, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0),
+                                                       reinterpret_cast<double2*>(A), nv);
+  else
+    to_c64_kernel<<<grid_1d(nv, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0),
+                                                    reinterpret_cast<float2*>(A), nv);
+  int rc = check_launch();
+  if (rc) return rc;
+  dim3 grid(t.nrb, t.nrt), block(t.rt, t.rb);
+  const size_t red = sizeof(double) * (size_t)t.rt * t.rb;
+  const T* vals = nullptr;
+  bool valc = false;
+  if (sizeof(T) == 8) {
+    valc = h->val_c != nullptr;
+    vals = (const T*)(valc ? (const void*)h->val_c : (const void*)h->val_r);
+  } else {
+    valc = h->val_cf != nullptr;
+    vals = (const T*)(valc ? (const void*)h->val_cf : (const void*)h->val_rf);
+  }
+  if (!vals) return EDGPU_ERR_ARG;
+  V* Vc = A;
+  V* Vp = B;
+  for (int j = 0; j < K; ++j) {
+    if (valc)
+      spmm_alpha_kernel<T, true><<<grid, block, red, s>>>(n, h->row_ptr, h->col, vals, R, Vc, Wb, pa, 1);
+    else
+      spmm_alpha_kernel<T, false><<<grid, block, red, s>>>(n, h->row_ptr, h->col, vals, R, Vc, Wb, pa, 1);
+    axpy_beta_kernel<T><<<grid, block, red, s>>>(n, R, Wb, Vc, j > 0 ? Vp : nullptr, pa, t.nrb,
+                                                 j > 0 ? beta : nullptr, alpha, K, j, pb);
+    if (j + 1 < K) normalize_kernel<T><<<grid, block, 0, s>>>(n, R, Wb, Vp, pb, t.nrb, beta, K, j, k_max, status);
+    if ((rc = check_launch())) return rc;
+    V* tmp = Vc;
+    Vc = Vp;
+    Vp = tmp;
+  }
+  return EDGPU_OK;
+}
+
+}  // namespace edgpu
+
+using namespace edgpu;
+
+extern "C" int edgpu_spmv(const edgpu_csr* h, const double* x, double* y, int R, void* stream) {
+  if (!h || !x || !y || R < 1 || h->n < 0) return EDGPU_ERR_ARG;
+  if (!h->val_c && !h->val_r) return EDGPU_ERR_ARG;
+  if (h->n == 0) return EDGPU_OK;
+  return spmv_impl<double>(h, reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), R,
+                           (cudaStream_t)stream);
+}
+
+extern "C" int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* stream) {
+  if (!h || !x || !y || R < 1 || h->n < 0) return EDGPU_ERR_ARG;
+  if (!h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
+  if (h->n == 0) return EDGPU_OK;
+  return spmv_impl<float>(h, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y), R,
+                          (cudaStream_t)stream);
+}
+
+extern "C" size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision) {
+  (void)K;
+  const size_t vs = precision ? sizeof(float2) : sizeof(double2);
+  RunTile t = make_tile(n > 0 ? n : 1, R > 0 ? R : 1);
+  size_t b = 0;
+  for (int k = 0; k < 3; ++k) b += ((vs * (size_t)n * R) + 255) & ~(size_t)255;
+  b += 2 * (((sizeof(double) * (size_t)t.nrb * R) + 255) & ~(size_t)255);
+  return b + 256;
+}
+
+extern "C" int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                             double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                             void* stream) {
+  if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
+  unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  if (precision == 0)
+    return lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes,
+                                (cudaStream_t)stream);
+  return lanczos_impl<float>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap) {
+  const int64_t nrb = grid_1d(n > 0 ? n : 1, 256);
+  size_t b = 0;
+  b += sizeof(double2) * (size_t)n;                        // y
+  b += sizeof(double) * (size_t)nrb * 2 + 512;             // alpha/norm partials
+  b += sizeof(double2) * (size_t)(K_cap + 1) * nrb + 256;  // dot partials
+  b += sizeof(double2) * (size_t)(K_cap + 1) + 256;        // h
+  return b + 1024;
+}
+
+extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* Vd,
+                                    double* wd, double* alpha, double* beta, int32_t* status_dev, void* workspace,
+                                    size_t workspace_bytes, void* stream) {
+  if (!h || !Vd || !wd || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  if (j0 < 0 || j1 > K_cap || j0 > j1) return EDGPU_ERR_ARG;
+  if (j0 == 0 && !v0) return EDGPU_ERR_ARG;
+  if (workspace_bytes < edgpu_lanczos_reorth_workspace(h->n, K_cap)) return EDGPU_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = h->n;
+  double2* V = reinterpret_cast<double2*>(Vd);
+  double2* w = reinterpret_cast<double2*>(wd);
+  const unsigned nrb = grid_1d(n, 256);
+  unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    unsigned char* p = ws + off;
+    off += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  double* pa = reinterpret_cast<double*>(carve(sizeof(double) * nrb));
+  double* pn = reinterpret_cast<double*>(carve(sizeof(double) * nrb));
+  double2* pd = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1) * nrb));
+  double2* hc = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1)));
+  (void)carve(sizeof(double2) * (size_t)n);
+  if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
+  if (j0 == 0) copy_c128_kernel<<<grid_1d(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0), V, n);
+  int rc = check_launch();
+  if (rc) return rc;
+  for (int j = j0; j < j1; ++j) {
+    const double2* vj = V + (int64_t)j * n;
+    // w = H v_j ; alpha partials
+    dim3 grid(nrb, 1), block(1, 256);
+    if (h->val_c)
+      spmm_alpha_kernel<double, true><<<grid, block, sizeof(double) * 256, s>>>(n, h->row_ptr, h->col, h->val_c, 1,
+                                                                                vj, w, pa, 1);
+    else
+      spmm_alpha_kernel<double, false><<<grid, block, sizeof(double) * 256, s>>>(n, h->row_ptr, h->col, h->val_r, 1,
+                                                                                 vj, w, pa, 1);
+    reorth_alpha_update_kernel<<<nrb, 256, 0, s>>>(n, w, vj, j > 0 ? V + (int64_t)(j - 1) * n : nullptr, pa, nrb,
+                                                   alpha, beta, j, pn);
+    if ((rc = check_launch())) return rc;
+    if (j + 1 >= K_cap) break;
+    // two passes of classical Gram-Schmidt against V[0..j]
+    const int m = j + 1;
+    for (int pass = 0; pass < 2; ++pass) {
+      dim3 g2(nrb, (m + kDotTile - 1) / kDotTile);
+      multidot_kernel<<<g2, 256, 0, s>>>(V, m, n, w, pd);
+      sum_partials_kernel<<<(m + 127) / 128, 128, 0, s>>>(pd, m, nrb, hc);
+      subtract_proj_kernel<<<nrb, 256, 0, s>>>(V, m, n, hc, w);
+    }
+    norm_partial_kernel<<<nrb, 256, 0, s>>>(n, w, pn);
+    reorth_normalize_kernel<<<nrb, 256, 0, s>>>(n, w, V + (int64_t)(j + 1) * n, pn, nrb, beta, j, status_dev);
+    if ((rc = check_launch())) return rc;
+  }
+  return EDGPU_OK;
+}
+
+extern "C" int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, double* X, void* stream) {
+  if (!V || !C || !X || K < 1 || M < 1 || n < 1) return EDGPU_ERR_ARG;
+  dim3 grid(grid_1d(n, 256) > 64 ? 64 : grid_1d(n, 256), M);
+  combine_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const double2*>(V), K, n,
+                                                        reinterpret_cast<const double2*>(C), M,
+                                                        reinterpret_cast<double2*>(X));
+  return check_launch();
+}
+
+extern "C" int edgpu_cfrac(const double* alpha, const double* beta, const int32_t* k_len, int K, int R,
+                           const double* omega, int n_omega, double delta, const double* e, const double* scale,
+                           double* g, void* stream) {
+  if (!alpha || !beta || !k_len || !omega || !e || !g || K < 1 || R < 0 || n_omega < 0) return EDGPU_ERR_ARG;
+  const int64_t tot = (int64_t)R * n_omega;
+  if (tot == 0) return EDGPU_OK;
+  const int threads = 256;
+  cfrac_kernel<<<(unsigned)((tot + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
+      alpha, beta, k_len, K, R, omega, n_omega, delta, e, scale, reinterpret_cast<double2*>(g));
+  return check_launch();
+}

@@ -1,0 +1,535 @@
+"""Device engine: compiled operators, sorted sector bases, CSR Hamiltonians and Lanczos.
+
+Host orchestration in Python over the C ABI of ``libedgpu.so`` (``include/edgpu.h``).  All
+device memory is owned by torch tensors; the library only receives pointers, sizes, a
+workspace and the current CUDA stream.  States live on the device as ``int64[N, W]``
+tensors holding the bit patterns of the packed ``uint64`` words.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .codec import n_words
+
+_U64 = np.uint64
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else C.c_void_p(0)
+
+
+class DeviceOp:
+    """Operator dict compiled to the device term table of ``edgpu_terms``.
+
+    Upstream format ``{((i, 'c'|'a'), ...): amplitude}`` (impurityModel/ed/finite.py:1301);
+    term order is the dict order, which fixes the summation order of equal outputs.
+    """
+
+    def __init__(self, op, device):
+        keys = list(op.keys())
+        t = len(keys)
+        ops = np.zeros(t, dtype=np.uint64)
+        flags = np.zeros(t, dtype=np.uint32)
+        coeff = np.zeros((t, 2), dtype=np.float64)
+        max_orb = -1
+        for k, key in enumerate(keys):
+            if len(key) > 4:
+                raise ValueError("terms with more than four operators are not supported")
+            packed = 0
+            cre, ann = [], []
+            for j, (i, a) in enumerate(key):
+                if a not in ("c", "a"):
+                    raise ValueError("Operator type unknown: {}".format(a))
+                i = int(i)
+                if not 0 <= i < 1024:
+                    raise ValueError("spin-orbital index out of range: %d" % i)
+                max_orb = max(max_orb, i)
+                packed |= (0x8000 | (0x4000 if a == "c" else 0) | i) << (16 * j)
+                (cre if a == "c" else ann).append(i)
+            ops[k] = packed
+            flags[k] = (1 if sorted(cre) == sorted(ann) else 0) | (len(key) << 8)
+            v = complex(op[key])
+            coeff[k] = (v.real, v.imag)
+        self.n_terms = t
+        self.max_orbital = max_orb
+        self.is_real = bool(np.all(coeff[:, 1] == 0.0))
+        self.ops = torch.from_numpy(ops.view(np.int64)).to(device)
+        self.coeff = torch.from_numpy(coeff).to(device)
+        self.flags = torch.from_numpy(flags.view(np.int32)).to(device)
+        self.terms = L.Terms(self.ops.data_ptr() if t else 0, self.coeff.data_ptr() if t else 0,
+                             self.flags.data_ptr() if t else 0, t)
+
+
+def make_restrictions(restrictions, n_spin_orbitals):
+    """``{frozenset(indices): (lo, hi)}`` -> ``edgpu_restrictions`` (None when absent)."""
+    if not restrictions:
+        return None
+    r = L.Restrictions()
+    items = list(restrictions.items())
+    if len(items) > L.MAX_RESTRICTIONS:
+        raise ValueError("at most %d restrictions are supported" % L.MAX_RESTRICTIONS)
+    r.n = len(items)
+    for k, (idx, (lo, hi)) in enumerate(items):
+        r.lo[k] = int(lo)
+        r.hi[k] = int(hi)
+        for q in range(L.MAX_WORDS):
+            r.mask[k][q] = 0
+        for i in idx:
+            i = int(i)
+            if not 0 <= i < 64 * L.MAX_WORDS:
+                raise ValueError("restriction index out of range: %d" % i)
+            r.mask[k][i // 64] |= 1 << (63 - i % 64)
+    return r
+
+
+class CsrMatrix:
+    """CSR Hamiltonian on the device (row j holds <j|H|k> for the sector basis)."""
+
+    def __init__(self, row_ptr, col, val_c=None, val_r=None, ncols=None):
+        self.row_ptr = row_ptr
+        self.col = col
+        self.val_c = val_c
+        self.val_r = val_r
+        self.val_cf = None
+        self.val_rf = None
+        self.n = row_ptr.numel() - 1
+        self.ncols = self.n if ncols is None else int(ncols)
+        self.nnz = col.numel()
+        self._struct = None
+
+    def mixed(self):
+        """Add the complex64/float32 value copy used by the mixed-precision form."""
+        if self.val_r is not None and self.val_rf is None:
+            self.val_rf = self.val_r.to(torch.float32)
+            self._struct = None
+        if self.val_c is not None and self.val_cf is None:
+            self.val_cf = self.val_c.to(torch.float32)
+            self._struct = None
+        return self
+
+    def struct(self):
+        if self._struct is None:
+            s = L.CSR()
+            s.n = self.n
+            s.nnz = self.nnz
+            s.row_ptr = self.row_ptr.data_ptr()
+            s.col = self.col.data_ptr() if self.nnz else self.row_ptr.data_ptr()
+            s.val_c = self.val_c.data_ptr() if self.val_c is not None and self.nnz else None
+            s.val_r = self.val_r.data_ptr() if self.val_r is not None and self.nnz else None
+            if self.nnz == 0:
+                s.val_r = self.row_ptr.data_ptr()
+            s.val_cf = self.val_cf.data_ptr() if self.val_cf is not None and self.nnz else None
+            s.val_rf = self.val_rf.data_ptr() if self.val_rf is not None and self.nnz else None
+            self._struct = s
+        return self._struct
+
+    def value_bytes(self):
+        return 16 if self.val_c is not None else 8
+
+
+class Engine:
+    """One engine per CUDA device.  Holds the library handle, a status word and a workspace."""
+
+    def __init__(self, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("impuritymodel_gb300 needs a CUDA device (there is no CPU fallback)")
+        self.lib = L.load()
+        self.device = torch.device(device if device is not None else "cuda")
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._ws = torch.empty(1 << 20, dtype=torch.uint8, device=self.device)
+        self.scratch_entries = 256
+
+    # -- plumbing -------------------------------------------------------------------------
+    @property
+    def stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def workspace(self, nbytes):
+        nbytes = int(nbytes)
+        if self._ws.numel() < nbytes:
+            self._ws = torch.empty(max(nbytes, 2 * self._ws.numel()), dtype=torch.uint8, device=self.device)
+        return C.c_void_p(self._ws.data_ptr()), C.c_size_t(self._ws.numel())
+
+    def reset_status(self):
+        self.status.zero_()
+
+    def read_status(self, where):
+        st = int(self.status.item())
+        if st != L.EDGPU_OK:
+            raise L.EdgpuError(st, where)
+
+    def upload_states(self, words):
+        words = np.ascontiguousarray(words, dtype=np.uint64)
+        return torch.from_numpy(words.view(np.int64)).to(self.device)
+
+    @staticmethod
+    def download_states(t):
+        return t.cpu().numpy().view(np.uint64)
+
+    # -- primitives -----------------------------------------------------------------------
+    def scan(self, counts):
+        n = counts.numel()
+        out = torch.empty(n + 1, dtype=torch.int64, device=self.device)
+        ws, wsn = self.workspace(self.lib.edgpu_scan_workspace(n))
+        L.check(self.lib.edgpu_scan_i64(_ptr(counts), _ptr(out), n, ws, wsn, self.stream), "scan")
+        return out
+
+    def sort_states(self, keys, payload):
+        """In-place stable sort of ``keys`` [M, W] with ``payload`` int32 [M]."""
+        m, w = keys.shape
+        if m <= 1:
+            return keys, payload
+        vary = torch.empty(w, dtype=torch.int64, device=self.device)
+        L.check(self.lib.edgpu_vary_mask(w, _ptr(keys), m, _ptr(vary), self.stream), "vary_mask")
+        vm = vary.cpu().numpy().view(np.uint64).copy()
+        arr = (C.c_uint64 * w)(*[int(x) for x in vm])
+        ws, wsn = self.workspace(self.lib.edgpu_sort_states_workspace(w, m))
+        L.check(self.lib.edgpu_sort_states(w, _ptr(keys), _ptr(payload), m, arr, ws, wsn, self.stream), "sort")
+        return keys, payload
+
+    def unique_sorted(self, keys, payload=None, vals=None):
+        """Unique rows of sorted keys.  Returns (keys, first_payload, summed vals or None)."""
+        m, w = keys.shape
+        if m == 0:
+            return keys, payload, vals
+        head = torch.empty(m, dtype=torch.int64, device=self.device)
+        L.check(self.lib.edgpu_segment_heads(w, _ptr(keys), m, _ptr(head), self.stream), "segment_heads")
+        hs = self.scan(head)
+        nu = int(hs[-1].item())
+        out_keys = torch.empty((nu, w), dtype=torch.int64, device=self.device)
+        if payload is None:
+            payload = torch.arange(m, dtype=torch.int32, device=self.device)
+        out_first = torch.empty(nu, dtype=torch.int32, device=self.device)
+        out_vals = torch.empty((nu, 2), dtype=torch.float64, device=self.device) if vals is not None else None
+        L.check(
+            self.lib.edgpu_segment_reduce(w, _ptr(keys), _ptr(payload), m, _ptr(hs), _ptr(vals), _ptr(out_keys),
+                                          _ptr(out_first), _ptr(out_vals), self.stream),
+            "segment_reduce",
+        )
+        return out_keys, out_first, out_vals
+
+    def merge(self, a, b):
+        na, w = a.shape
+        nb = b.shape[0]
+        out = torch.empty((na + nb, w), dtype=torch.int64, device=self.device)
+        L.check(self.lib.edgpu_merge_states(w, _ptr(a), na, _ptr(b), nb, _ptr(out), self.stream), "merge")
+        return out
+
+    def lookup(self, basis, query):
+        nq, w = query.shape
+        out = torch.empty(nq, dtype=torch.int64, device=self.device)
+        L.check(self.lib.edgpu_lookup_states(w, _ptr(basis), basis.shape[0], _ptr(query), nq, _ptr(out), self.stream),
+                "lookup")
+        return out
+
+    def sort_unique(self, keys):
+        """Sorted unique rows of ``keys`` (copy)."""
+        k = keys.clone()
+        p = torch.arange(k.shape[0], dtype=torch.int32, device=self.device)
+        self.sort_states(k, p)
+        u, _, _ = self.unique_sorted(k, p)
+        return u
+
+    # -- operator application -------------------------------------------------------------
+    def apply_columns(self, states, dop, restr, weight_min, basis=None, filt=L.FILTER_NONE, want_states=False,
+                      want_index=False, want_vals=False, conj=False):
+        """Per-state H|b> (see edgpu_apply_columns). Returns (offsets, states, index, vals)."""
+        n, w = states.shape
+        offsets = torch.zeros(n + 1, dtype=torch.int64, device=self.device)
+        empty = torch.empty((0, w), dtype=torch.int64, device=self.device)
+        if n == 0 or dop.n_terms == 0:
+            return offsets, empty, torch.empty(0, dtype=torch.int64, device=self.device), torch.empty(
+                (0, 2), dtype=torch.float64, device=self.device)
+        counts = torch.empty(n, dtype=torch.int64, device=self.device)
+        rp = C.byref(restr) if restr is not None else None
+        bptr = _ptr(basis) if basis is not None else C.c_void_p(0)
+        nb = basis.shape[0] if basis is not None else 0
+        while True:
+            self.reset_status()
+            L.check(
+                self.lib.edgpu_apply_columns(w, _ptr(states), n, C.byref(dop.terms), rp, weight_min, bptr, nb, filt,
+                                             None, _ptr(counts), None, None, None, 0, self.scratch_entries,
+                                             _ptr(self.status), self.stream),
+                "apply_columns(count)",
+            )
+            st = int(self.status.item())
+            if st == L.EDGPU_ERR_OVERFLOW and self.scratch_entries < 8192:
+                self.scratch_entries *= 4
+                continue
+            if st != L.EDGPU_OK:
+                raise L.EdgpuError(st, "apply_columns(count)")
+            break
+        offsets = self.scan(counts)
+        total = int(offsets[-1].item())
+        out_s = torch.empty((total, w), dtype=torch.int64, device=self.device) if want_states else None
+        out_i = torch.empty(total, dtype=torch.int64, device=self.device) if want_index else None
+        out_v = torch.empty((total, 2), dtype=torch.float64, device=self.device) if want_vals else None
+        if total:
+            self.reset_status()
+            L.check(
+                self.lib.edgpu_apply_columns(w, _ptr(states), n, C.byref(dop.terms), rp, weight_min, bptr, nb, filt,
+                                             _ptr(offsets), None, _ptr(out_s), _ptr(out_i), _ptr(out_v), int(conj),
+                                             self.scratch_entries, _ptr(self.status), self.stream),
+                "apply_columns(fill)",
+            )
+            self.read_status("apply_columns(fill)")
+        return offsets, out_s, out_i, out_v
+
+    def apply_vector_raw(self, states, amps, dop, restr):
+        """Raw emissions (state, term) ordered.  Returns (offsets, out_states, out_vals)."""
+        n, w = states.shape
+        if n == 0 or dop.n_terms == 0:
+            return (torch.zeros(n + 1, dtype=torch.int64, device=self.device),
+                    torch.empty((0, w), dtype=torch.int64, device=self.device),
+                    torch.empty((0, 2), dtype=torch.float64, device=self.device))
+        counts = torch.empty(n, dtype=torch.int64, device=self.device)
+        rp = C.byref(restr) if restr is not None else None
+        L.check(self.lib.edgpu_apply_vector(w, _ptr(states), None, n, C.byref(dop.terms), rp, None, _ptr(counts), None,
+                                            None, self.stream), "apply_vector(count)")
+        offsets = self.scan(counts)
+        total = int(offsets[-1].item())
+        out_s = torch.empty((total, w), dtype=torch.int64, device=self.device)
+        out_v = torch.empty((total, 2), dtype=torch.float64, device=self.device)
+        if total:
+            L.check(self.lib.edgpu_apply_vector(w, _ptr(states), _ptr(amps), n, C.byref(dop.terms), rp,
+                                                _ptr(offsets), None, _ptr(out_s), _ptr(out_v), self.stream),
+                    "apply_vector(fill)")
+        return offsets, out_s, out_v
+
+    def apply_vectors(self, run_states, run_amps, dop, restr, weight_min):
+        """psi'_r = Op psi_r for several runs r (upstream applyOp per run, finite.py:1301-1511).
+
+        ``run_states``/``run_amps``: lists of [n_r, W] int64 and [n_r, 2] float64 device
+        tensors.  Returns per-run (states [m_r, W], amps [m_r, 2]) with outputs merged in
+        upstream order (psi order, then term order), pruned at |a|^2 < weight_min, and listed
+        in first-occurrence (dict insertion) order.
+        """
+        runs = len(run_states)
+        w = run_states[0].shape[1] if runs else 1
+        sizes = [int(s.shape[0]) for s in run_states]
+        if sum(sizes) == 0 or dop.n_terms == 0:
+            z = [(torch.empty((0, w), dtype=torch.int64, device=self.device),
+                  torch.empty((0, 2), dtype=torch.float64, device=self.device)) for _ in range(runs)]
+            return z
+        states = torch.cat(run_states, 0)
+        amps = torch.cat(run_amps, 0)
+        offsets, out_s, out_v = self.apply_vector_raw(states, amps, dop, restr)
+        total = out_s.shape[0]
+        if total == 0:
+            return [(out_s[:0], out_v[:0]) for _ in range(runs)]
+        run_of_input = torch.repeat_interleave(torch.arange(runs, device=self.device),
+                                               torch.tensor(sizes, device=self.device))
+        counts = offsets[1:] - offsets[:-1]
+        run_of_emit = torch.repeat_interleave(run_of_input, counts)
+        keys = torch.cat([run_of_emit.view(-1, 1), out_s], 1).contiguous()
+        payload = torch.arange(total, dtype=torch.int32, device=self.device)
+        self.sort_states(keys, payload)
+        ukeys, first, sums = self.unique_sorted(keys, payload, out_v)
+        a2 = torch.hypot(sums[:, 0], sums[:, 1]) ** 2
+        keep = a2 >= weight_min
+        ukeys, first, sums = ukeys[keep], first[keep], sums[keep]
+        # dict insertion order: by first emission index within each run
+        order = torch.argsort(first.to(torch.int64))
+        ukeys, sums = ukeys[order], sums[order]
+        run_id = ukeys[:, 0]
+        out = []
+        bounds = torch.searchsorted(torch.sort(run_id).values, torch.arange(runs + 1, device=self.device))
+        # runs are interleaved after the first-occurrence ordering only if emissions of
+        # run r all precede run r+1, which holds since inputs are concatenated by run.
+        b = bounds.cpu().tolist()
+        for r in range(runs):
+            out.append((ukeys[b[r]:b[r + 1], 1:].contiguous(), sums[b[r]:b[r + 1]].contiguous()))
+        return out
+
+    # -- sectors --------------------------------------------------------------------------
+    def expand(self, basis0, dop, restr, weight_min=1e-12):
+        """Closure of ``basis0`` under the operator (upstream expand_basis, finite.py:1696-1803).
+
+        Returns (sorted basis [N, W], layered order [N, W]); the layered order is upstream's
+        basis order: ``basis0`` as given, then each breadth-first layer sorted.
+        """
+        s_sorted = self.sort_unique(basis0)
+        layers = [basis0]
+        frontier = basis0
+        while frontier.shape[0] > 0:
+            _, cand, _, _ = self.apply_columns(frontier, dop, restr, weight_min, basis=s_sorted,
+                                               filt=L.FILTER_NOT_IN_BASIS, want_states=True)
+            if cand.shape[0] == 0:
+                break
+            new = self.sort_unique(cand)
+            s_sorted = self.merge(s_sorted, new)
+            layers.append(new)
+            frontier = new
+        return s_sorted, torch.cat(layers, 0)
+
+    def build_csr(self, basis_sorted, dop, restr, weight_min=1e-12):
+        """Sector Hamiltonian on a sorted basis (upstream get_hamiltonian_matrix_from_h_dict).
+
+        Column j of H (= H|b_j>) becomes row j with conjugated values, which for the
+        Hermitian H is row j of H.  Real operators store float64 values.
+        """
+        offsets, _, idx, vals = self.apply_columns(basis_sorted, dop, restr, weight_min, basis=basis_sorted,
+                                                   filt=L.FILTER_IN_BASIS, want_index=True, want_vals=True, conj=True)
+        col = idx.to(torch.int32)
+        if dop.is_real:
+            return CsrMatrix(offsets, col, val_r=vals[:, 0].contiguous())
+        return CsrMatrix(offsets, col, val_c=vals.contiguous())
+
+    def components(self, csr):
+        """Connected-component label (smallest member index) of every sector state."""
+        n = csr.n
+        labels = torch.arange(n, dtype=torch.int64, device=self.device)
+        if csr.nnz == 0:
+            return labels
+        rows = torch.repeat_interleave(torch.arange(n, device=self.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
+        cols = csr.col.to(torch.int64)
+        for _ in range(10 * n + 10):
+            m = torch.minimum(labels[rows], labels[cols])
+            new = labels.clone()
+            new.scatter_reduce_(0, rows, m, reduce="amin")
+            new.scatter_reduce_(0, cols, m, reduce="amin")
+            new = new[new]
+            if torch.equal(new, labels):
+                break
+            labels = new
+        return labels
+
+    def run_dims(self, csr, v0_nonzero_rows, run_of_row, runs):
+        """Dimension of the closure of each run's support (upstream len(basis_index))."""
+        labels = self.components(csr)
+        uniq, inv = torch.unique(labels, return_inverse=True)
+        sizes = torch.bincount(inv, minlength=uniq.numel())
+        comp = inv[v0_nonzero_rows]
+        pair = torch.unique(run_of_row * uniq.numel() + comp)
+        dims = torch.zeros(runs, dtype=torch.int64, device=self.device)
+        dims.index_add_(0, pair // uniq.numel(), sizes[pair % uniq.numel()])
+        return dims
+
+    # -- Krylov ---------------------------------------------------------------------------
+    def lanczos(self, csr, v0, k_max, precision=0):
+        """Batched Lanczos on R start vectors v0 [N, R] complex128 (normalised)."""
+        n, r = v0.shape
+        if n != csr.n or csr.ncols != csr.n:
+            raise ValueError("lanczos: square matrix of size %d required for vectors of size %d" % (csr.n, n))
+        kmax = torch.as_tensor(k_max, dtype=torch.int32).to(self.device)
+        K = int(kmax.max().item())
+        alpha = torch.zeros((r, K), dtype=torch.float64, device=self.device)
+        beta = torch.zeros((r, K), dtype=torch.float64, device=self.device)
+        if precision:
+            csr.mixed()
+        v0r = torch.view_as_real(v0.contiguous()) if v0.is_complex() else v0
+        ws, wsn = self.workspace(self.lib.edgpu_lanczos_workspace(n, r, K, precision))
+        self.reset_status()
+        L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision, _ptr(alpha),
+                                       _ptr(beta), _ptr(self.status), ws, wsn, self.stream), "lanczos")
+        self.read_status("lanczos")
+        return alpha, beta
+
+    def spmv(self, csr, x, precision=0):
+        """y [csr.n, R] = csr @ x for x [csr.ncols, R]."""
+        nx, r = x.shape
+        if nx != csr.ncols:
+            raise ValueError("spmv: x has %d rows, matrix has %d columns" % (nx, csr.ncols))
+        n = csr.n
+        if precision:
+            csr.mixed()
+            xr = torch.view_as_real(x.to(torch.complex64).contiguous())
+            y = torch.empty((n, r), dtype=torch.complex64, device=self.device)
+            L.check(self.lib.edgpu_spmv_c64(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r,
+                                            self.stream), "spmv_c64")
+            return y
+        xr = torch.view_as_real(x.contiguous())
+        y = torch.empty((n, r), dtype=torch.complex128, device=self.device)
+        L.check(self.lib.edgpu_spmv(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r, self.stream),
+                "spmv")
+        return y
+
+    def cfrac(self, alpha, beta, k_len, omega, delta, e, scale):
+        r, K = alpha.shape
+        om = torch.as_tensor(np.asarray(omega, dtype=np.float64)).to(self.device)
+        e_t = torch.as_tensor(np.asarray(e, dtype=np.float64)).to(self.device)
+        sc = torch.as_tensor(np.asarray(scale, dtype=np.float64)).to(self.device)
+        kl = torch.as_tensor(k_len, dtype=torch.int32).to(self.device)
+        g = torch.empty((r, om.numel()), dtype=torch.complex128, device=self.device)
+        L.check(self.lib.edgpu_cfrac(_ptr(alpha), _ptr(beta), _ptr(kl), K, r, _ptr(om), om.numel(), float(delta),
+                                     _ptr(e_t), _ptr(sc), _ptr(torch.view_as_real(g)), self.stream), "cfrac")
+        return g
+
+    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16):
+        """Lanczos with full reorthogonalisation from v0 (normalised, [N] complex128).
+
+        ``stop(alpha, beta, j)`` (host arrays of length j) returns True when converged.
+        Returns (V [K, N], alpha [K], beta [K]) with K the number of steps taken;
+        ``beta[:K-1]`` is the tridiagonal's off-diagonal and ``beta[K-1]`` the coupling to
+        the next Krylov vector (0 when the space is exhausted).
+        """
+        n = csr.n
+        if csr.ncols != n or v0.numel() != n:
+            raise ValueError("krylov_reorth: square matrix and start vector of matching size required")
+        k_cap = int(min(k_cap, n))
+        V = torch.zeros((k_cap, n), dtype=torch.complex128, device=self.device)
+        w = torch.zeros(n, dtype=torch.complex128, device=self.device)
+        alpha = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
+        beta = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
+        ws, wsn = self.workspace(self.lib.edgpu_lanczos_reorth_workspace(n, k_cap))
+        v0r = torch.view_as_real(v0.contiguous())
+        j = 0
+        while j < k_cap:
+            j1 = min(k_cap, j + chunk)
+            self.reset_status()
+            L.check(self.lib.edgpu_lanczos_reorth(C.byref(csr.struct()), _ptr(v0r), j, j1, k_cap,
+                                                  _ptr(torch.view_as_real(V)), _ptr(torch.view_as_real(w)),
+                                                  _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
+                    "lanczos_reorth")
+            st = int(self.status.item())
+            if st == L.EDGPU_ERR_BREAKDOWN:
+                # invariant subspace: the Krylov space is exact at the first zero beta
+                bh = beta[:j1].cpu().numpy()
+                kb = int(np.argmax(bh == 0.0)) + 1
+                return V[:kb], alpha[:kb].cpu().numpy(), bh[:kb]
+            if st != L.EDGPU_OK:
+                raise L.EdgpuError(st, "lanczos_reorth")
+            j = j1
+            if stop is not None and stop(alpha[:j].cpu().numpy(), beta[:j].cpu().numpy(), j):
+                break
+        return V[:j], alpha[:j].cpu().numpy(), beta[:j].cpu().numpy()
+
+    def combine(self, V, coeffs):
+        """X[m] = sum_k coeffs[k, m] V[k] (complex128)."""
+        k, n = V.shape
+        cm = torch.as_tensor(np.ascontiguousarray(coeffs, dtype=np.complex128)).to(self.device)
+        m = cm.shape[1]
+        X = torch.empty((m, n), dtype=torch.complex128, device=self.device)
+        L.check(self.lib.edgpu_combine(_ptr(torch.view_as_real(V)), k, n, _ptr(torch.view_as_real(cm)), m,
+                                       _ptr(torch.view_as_real(X)), self.stream), "combine")
+        return X
+
+
+_ENGINES = {}
+
+
+def get_engine(device=None):
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    key = str(dev)
+    if key not in _ENGINES:
+        _ENGINES[key] = Engine(dev)
+    return _ENGINES[key]
+
+
+def words_for(n_spin_orbitals):
+    w = n_words(n_spin_orbitals)
+    if w > L.MAX_WORDS:
+        raise ValueError("at most %d spin-orbitals are supported" % (64 * L.MAX_WORDS))
+    return w
+
+
+def sqrt_norm2(amps):
+    return math.sqrt(float((amps[:, 0] ** 2 + amps[:, 1] ** 2).sum().item())) if amps.numel() else 0.0

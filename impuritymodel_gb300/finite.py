@@ -1,0 +1,550 @@
+"""Drop-in replacement of upstream ``impurityModel.ed.finite`` for the ED hot path.
+
+Same function names, argument meanings, return types and error behaviour as
+``impurityModel/ed/finite.py``; the work runs in the sm_103a kernels of ``libedgpu.so``
+through :mod:`impuritymodel_gb300.engine`.  Product states are upstream ``bytes``;
+operators are upstream dicts; matrices returned to the caller are SciPy CSR.
+
+MPI ``parallelization_mode``/``mode`` arguments are accepted for signature compatibility
+and run on the single GPU of the process.
+"""
+
+from __future__ import annotations
+
+import itertools
+import math
+
+import numpy as np
+import scipy.linalg
+import scipy.sparse
+import torch
+
+from . import _lib as L
+from . import codec
+from .engine import CsrMatrix, DeviceOp, get_engine, make_restrictions, words_for
+from .models import (  # noqa: F401  (upstream names re-exported)
+    add_ops as addOps,
+    c2i,
+    dagger_op as daggerOp,
+    dc_mlft as dc_MLFT,
+    gaunt_c as gauntC,
+    get_u as getU,
+    get_uop as getUop,
+    hfield_op as gethHfieldop,
+    slater_condon_2p3d_uop as get2p3dSlaterCondonUop,
+    soc_op as getSOCop,
+)
+
+
+def get_spherical_2_cubic_matrix(spinpol=False, l=2):
+    """Spherical -> cubic harmonics unitary (upstream finite.py:216-268)."""
+    from .models import spherical_to_cubic
+
+    u = spherical_to_cubic(l)
+    if spinpol:
+        n, m = u.shape
+        big = np.zeros((2 * n, 2 * m), dtype=complex)
+        big[:n, :m] = u
+        big[n:, m:] = u
+        u = big
+    return u
+
+
+def assert_hermitian(op):
+    assert daggerOp(op) == op
+
+
+def get_job_tasks(rank, ranks, tasks_tot):
+    """Split task indices over ranks (upstream finite.py:27-55)."""
+    n_tot = len(tasks_tot)
+    nj = n_tot // ranks
+    rest = n_tot % ranks
+    tasks = [tasks_tot[i] for i in range(nj * rank, nj * rank + nj)]
+    if rank < rest:
+        tasks.append(tasks_tot[n_tot - rest + rank])
+    return tuple(tasks)
+
+
+# ---------------------------------------------------------------------------------------
+# Operator cache: compiling an operator dict to a device term table once per dict object
+# ---------------------------------------------------------------------------------------
+
+_OP_CACHE = {}
+
+
+def _device_op(op, eng):
+    key = (id(op), len(op), str(eng.device))
+    hit = _OP_CACHE.get(key)
+    if hit is not None and hit[0] is op:
+        return hit[1]
+    d = DeviceOp(op, eng.device)
+    if len(_OP_CACHE) > 64:
+        _OP_CACHE.clear()
+    _OP_CACHE[key] = (op, d)
+    return d
+
+
+def _n_from_psi(psi, n_spin_orbitals):
+    return n_spin_orbitals
+
+
+# ---------------------------------------------------------------------------------------
+# Operator application (upstream finite.py:1301-1511)
+# ---------------------------------------------------------------------------------------
+
+
+def applyOp(n_spin_orbitals, op, psi, slaterWeightMin=1e-12, restrictions=None, opResult=None):
+    r"""Return :math:`|psi'\rangle = op |psi\rangle` (upstream ``finite.applyOp``).
+
+    Without ``opResult`` the outputs are accumulated in upstream order (psi order, then
+    term order) and pruned at ``|amp|^2 < slaterWeightMin``; ``restrictions`` filter the
+    output states.  With ``opResult`` (in/out memo) the action on each product state is
+    computed once on the GPU, stored in ``opResult`` pruned at ``slaterWeightMin`` like
+    upstream, and reused (including a wrong result a caller stored there) for states
+    already present.
+    """
+    if not psi:
+        return {}
+    eng = get_engine()
+    n = int(n_spin_orbitals)
+    w = words_for(n)
+    dop = _device_op(op, eng)
+    restr = make_restrictions(restrictions, n)
+    if opResult is None:
+        words, amps = codec.psi_to_arrays(psi, n)
+        s_t = eng.upload_states(words)
+        a_t = torch.from_numpy(amps).to(eng.device)
+        (out_s, out_a), = eng.apply_vectors([s_t], [a_t], dop, restr, slaterWeightMin)
+        return codec.arrays_to_psi(eng.download_states(out_s), out_a.cpu().numpy(), n)
+    # memo path: compute per-state results for unseen states, then combine
+    states = list(psi.keys())
+    fresh = [s for s in states if s not in opResult]
+    if fresh:
+        f_t = eng.upload_states(codec.bytes_to_words(fresh, n))
+        offsets, out_s, _, out_v = eng.apply_columns(f_t, dop, restr, 0.0, want_states=True, want_vals=True)
+        off = offsets.cpu().numpy()
+        ob = codec.words_to_bytes(eng.download_states(out_s), n) if out_s.shape[0] else []
+        ov = out_v.cpu().numpy()
+        fresh_res = {}
+        for k, s in enumerate(fresh):
+            a, b = off[k], off[k + 1]
+            fresh_res[s] = [(ob[e], complex(ov[e, 0], ov[e, 1])) for e in range(a, b)]
+    psi_new = {}
+    for s in states:
+        amp = psi[s]
+        if s in opResult:
+            for s2, a2 in opResult[s].items():
+                psi_new[s2] = psi_new[s2] + a2 * amp if s2 in psi_new else a2 * amp
+            continue
+        memo = {}
+        for s2, h in fresh_res[s]:
+            memo[s2] = h
+            psi_new[s2] = psi_new[s2] + amp * h if s2 in psi_new else amp * h
+        opResult[s] = {s2: h for s2, h in memo.items() if abs(h) ** 2 >= slaterWeightMin}
+    return {s: a for s, a in psi_new.items() if abs(a) ** 2 >= slaterWeightMin}
+
+
+def c(n_spin_orbitals, i, psi):
+    r"""Return :math:`c_i^\dagger |psi\rangle` (upstream finite.py:449-473)."""
+    return applyOp(n_spin_orbitals, {((i, "c"),): 1.0}, psi, slaterWeightMin=0.0)
+
+
+def a(n_spin_orbitals, i, psi):
+    r"""Return :math:`c_i |psi\rangle` (upstream finite.py:424-446)."""
+    return applyOp(n_spin_orbitals, {((i, "a"),): 1.0}, psi, slaterWeightMin=0.0)
+
+
+def inner(a, b):
+    r"""Return :math:`\langle a|b\rangle` of two dict states (upstream finite.py:377-395)."""
+    acc = 0
+    for state, amp in b.items():
+        if state in a:
+            acc += np.conj(a[state]) * amp
+    return acc
+
+
+def addToFirst(psi1, psi2, mul=1):
+    """``psi1 += mul * psi2`` in place (upstream finite.py:398-421)."""
+    for s, amp in psi2.items():
+        if s in psi1:
+            psi1[s] += amp * mul
+        else:
+            psi1[s] = amp * mul
+
+
+def add(psi1, psi2, mul=1):
+    """Return ``psi1 + mul * psi2`` (upstream finite.py:1998-2017)."""
+    psi = psi1.copy()
+    for s, amp in psi2.items():
+        if s in psi:
+            psi[s] += mul * amp
+        else:
+            psi[s] = mul * amp
+    return psi
+
+
+def norm2(psi):
+    """Return <psi|psi> (upstream finite.py:2020-2033)."""
+    return sum(abs(x) ** 2 for x in psi.values())
+
+
+# ---------------------------------------------------------------------------------------
+# Basis construction (upstream finite.py:294-374)
+# ---------------------------------------------------------------------------------------
+
+
+def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
+    """Restricted basis of product states, in upstream's itertools order."""
+    for l in nBaths.keys():
+        assert valBaths[l] <= nBaths[l]
+    basis_l = {}
+    for l in nBaths.keys():
+        basis_l[l] = []
+        for dn_val in range(dnValBaths[l] + 1):
+            for dn_con in range(dnConBaths[l] + 1):
+                dn_imp = dn_val - dn_con
+                if abs(dn_imp) <= dnTol[l]:
+                    n_imp = n0imp[l] + dn_imp
+                    n_val = valBaths[l] - dn_val
+                    n_con = dn_con
+                    assert n_val <= valBaths[l]
+                    assert n_con <= nBaths[l] - valBaths[l]
+                    assert n_imp <= 2 * (2 * l + 1)
+                    idx = [c2i(nBaths, (l, s, m)) for s in range(2) for m in range(-l, l + 1)]
+                    b_imp = tuple(itertools.combinations(idx, n_imp))
+                    if valBaths[l] == 0:
+                        b_val = ((),)
+                    else:
+                        idx = [c2i(nBaths, (l, b)) for b in range(valBaths[l])]
+                        b_val = tuple(itertools.combinations(idx, n_val))
+                    if nBaths[l] - valBaths[l] == 0:
+                        b_con = ((),)
+                    else:
+                        idx = [c2i(nBaths, (l, b)) for b in range(valBaths[l], nBaths[l])]
+                        b_con = tuple(itertools.combinations(idx, n_con))
+                    for bi in b_imp:
+                        for bv in b_val:
+                            for bc in b_con:
+                                basis_l[l].append(bi + bv + bc)
+    n = sum(2 * (2 * ang + 1) + nb for ang, nb in nBaths.items())
+    basis = []
+    for conf in itertools.product(*basis_l.values()):
+        basis.append(codec.tuple_to_bytes(tuple(sorted(itertools.chain.from_iterable(conf))), n))
+    return tuple(basis)
+
+
+# ---------------------------------------------------------------------------------------
+# Hamiltonian matrices
+# ---------------------------------------------------------------------------------------
+
+
+class _SortedBasis:
+    """A basis given in caller order, held sorted on the device with the permutation."""
+
+    def __init__(self, eng, basis, n):
+        self.words = codec.bytes_to_words(basis, n)
+        given = eng.upload_states(self.words)
+        keys = given.clone()
+        payload = torch.arange(keys.shape[0], dtype=torch.int32, device=eng.device)
+        eng.sort_states(keys, payload)
+        self.sorted = keys
+        self.perm = payload.to(torch.int64)  # sorted position -> given position
+        if keys.shape[0] > 1:
+            u, _, _ = eng.unique_sorted(keys, payload)
+            if u.shape[0] != keys.shape[0]:
+                raise ValueError("basis contains duplicate product states")
+
+
+def _device_hamiltonian(eng, dop, sb, weight_min=1e-12, restr=None):
+    """H on a fixed basis in sorted order (columns kept only for rows inside the basis)."""
+    return eng.build_csr(sb.sorted, dop, restr, weight_min)
+
+
+def _csr_to_scipy_given_order(csr, perm, conj_back=True):
+    """Device CSR (sorted order, row j = conj column j) -> SciPy CSR H in caller order."""
+    rp = csr.row_ptr.cpu().numpy()
+    col = csr.col.cpu().numpy().astype(np.int64)
+    if csr.val_c is not None:
+        v = csr.val_c.cpu().numpy()
+        val = v[:, 0] + 1j * v[:, 1]
+    else:
+        val = csr.val_r.cpu().numpy().astype(np.complex128)
+    n = csr.n
+    p = perm.cpu().numpy()
+    rows_sorted = np.repeat(np.arange(n), np.diff(rp))
+    # device row j holds conj(H[k, j]) at column k: H[k, j] = conj(val)
+    h_row = p[col]
+    h_col = p[rows_sorted]
+    data = np.conj(val) if conj_back else val
+    return scipy.sparse.csr_matrix((data, (h_row, h_col)), shape=(n, n))
+
+
+def get_hamiltonian_matrix(n_spin_orbitals, hOp, basis, mode="sparse_MPI"):
+    """Hamiltonian in the given basis (upstream finite.py:1514-1610); SciPy CSR or dense."""
+    eng = get_engine()
+    n = int(n_spin_orbitals)
+    words_for(n)
+    sb = _SortedBasis(eng, list(basis), n)
+    csr = _device_hamiltonian(eng, _device_op(hOp, eng), sb)
+    h = _csr_to_scipy_given_order(csr, sb.perm)
+    if mode in ("dense_serial", "dense_MPI"):
+        return h.toarray()
+    return h
+
+
+def get_hamiltonian_matrix_from_h_dict(h_dict, basis, parallelization_mode="serial", return_h_local=False,
+                                       mode="sparse"):
+    """Matrix from an ``h_dict`` memo (upstream finite.py:1613-1693).
+
+    ``h_dict`` is the caller's ``{state: {state: amplitude}}`` dict; this is a pure format
+    conversion at the API boundary.
+    """
+    if parallelization_mode == "serial":
+        assert return_h_local is False
+    n = len(basis)
+    basis_index = {basis[i]: i for i in range(n)}
+    if mode == "dense":
+        h = np.zeros((n, n), dtype=complex)
+        for j in range(n):
+            for k, v in h_dict[basis[j]].items():
+                h[basis_index[k], j] = v
+        return h, basis_index
+    if mode != "sparse":
+        raise Exception("Wrong input parameters")
+    data, row, col = [], [], []
+    for j in range(n):
+        if basis[j] not in h_dict and parallelization_mode == "H_build":
+            continue
+        for k, v in h_dict[basis[j]].items():
+            data.append(v)
+            col.append(j)
+            row.append(basis_index[k])
+    h = scipy.sparse.csr_matrix((np.array(data, dtype=complex), (row, col)), shape=(n, n))
+    return h, basis_index
+
+
+def _expand_device(eng, n, dop, restr, basis0_words, h_dict=None):
+    """Closure on the device; returns (sorted basis tensor, layered order words)."""
+    b0 = eng.upload_states(basis0_words)
+    if h_dict:
+        # states already memoised in h_dict contribute their stored outputs (upstream
+        # reuses h_dict[b] as is); the rest are expanded on the device
+        return _expand_with_memo(eng, n, dop, restr, b0, h_dict)
+    s_sorted, order = eng.expand(b0, dop, restr)
+    return s_sorted, order
+
+
+def _expand_with_memo(eng, n, dop, restr, b0, h_dict):
+    s_sorted = eng.sort_unique(b0)
+    layers = [b0]
+    frontier = b0
+    while frontier.shape[0] > 0:
+        fw = eng.download_states(frontier)
+        fb = codec.words_to_bytes(fw, n)
+        cached = [k for k, s in enumerate(fb) if s in h_dict]
+        todo = [k for k, s in enumerate(fb) if s not in h_dict]
+        cands = []
+        if todo:
+            sub = frontier[torch.tensor(todo, device=eng.device)]
+            _, cand, _, _ = eng.apply_columns(sub, dop, restr, 1e-12, basis=s_sorted, filt=L.FILTER_NOT_IN_BASIS,
+                                              want_states=True)
+            cands.append(cand)
+        if cached:
+            outs = [o for k in cached for o in h_dict[fb[k]].keys()]
+            if outs:
+                ot = eng.upload_states(codec.bytes_to_words(outs, n))
+                hit = eng.lookup(s_sorted, ot)
+                cands.append(ot[hit < 0])
+        cand = torch.cat(cands, 0) if cands else frontier[:0]
+        if cand.shape[0] == 0:
+            break
+        new = eng.sort_unique(cand)
+        s_sorted = eng.merge(s_sorted, new)
+        layers.append(new)
+        frontier = new
+    return s_sorted, torch.cat(layers, 0)
+
+
+def _fill_h_dict(eng, n, dop, restr, states_t, h_dict):
+    """Store H|b> for the given states into the caller's h_dict (upstream memo contents)."""
+    if states_t.shape[0] == 0:
+        return
+    offsets, out_s, _, out_v = eng.apply_columns(states_t, dop, restr, 1e-12, want_states=True, want_vals=True)
+    sb = codec.words_to_bytes(eng.download_states(states_t), n)
+    off = offsets.cpu().numpy()
+    ob = codec.words_to_bytes(eng.download_states(out_s), n) if out_s.shape[0] else []
+    ov = out_v.cpu().numpy()
+    for k, s in enumerate(sb):
+        if s in h_dict:
+            continue
+        h_dict[s] = {ob[e]: complex(ov[e, 0], ov[e, 1]) for e in range(off[k], off[k + 1])}
+
+
+def expand_basis(n_spin_orbitals, h_dict, hOp, basis0, restrictions, parallelization_mode="serial"):
+    """Closure of ``basis0`` under ``hOp`` with restrictions (upstream finite.py:1696-1803).
+
+    Returns the basis in upstream order (``basis0``, then each new layer sorted) and adds
+    ``H|b>`` of every basis state to ``h_dict`` (when ``h_dict`` is not None).
+    """
+    if parallelization_mode not in ("serial", "H_build"):
+        raise Exception("Wrong parallelization parameter.")
+    eng = get_engine()
+    n = int(n_spin_orbitals)
+    words_for(n)
+    dop = _device_op(hOp, eng)
+    restr = make_restrictions(restrictions, n)
+    basis0 = list(basis0)
+    if not basis0:
+        return ()
+    _, order = _expand_device(eng, n, dop, restr, codec.bytes_to_words(basis0, n), h_dict)
+    if h_dict is not None:
+        _fill_h_dict(eng, n, dop, restr, order, h_dict)
+    return tuple(codec.words_to_bytes(eng.download_states(order), n))
+
+
+def expand_basis_and_hamiltonian(n_spin_orbitals, h_dict, hOp, basis0, restrictions, parallelization_mode="serial",
+                                 return_h_local=False):
+    """Expanded basis and its Hamiltonian (upstream finite.py:1806-1894).
+
+    Returns ``(h, basis_index)``: SciPy CSR in upstream basis order and the
+    ``{state: index}`` dict.
+    """
+    eng = get_engine()
+    n = int(n_spin_orbitals)
+    words_for(n)
+    dop = _device_op(hOp, eng)
+    restr = make_restrictions(restrictions, n)
+    basis0 = list(basis0)
+    s_sorted, order = _expand_device(eng, n, dop, restr, codec.bytes_to_words(basis0, n), h_dict)
+    if h_dict is not None:
+        _fill_h_dict(eng, n, dop, restr, order, h_dict)
+    csr = eng.build_csr(s_sorted, dop, restr)
+    # permutation sorted position -> upstream (layered) position
+    pos = eng.lookup(s_sorted, order)  # layered index -> sorted index
+    perm = torch.empty_like(pos)
+    perm[pos] = torch.arange(pos.numel(), device=eng.device)
+    h = _csr_to_scipy_given_order(csr, perm)
+    basis = codec.words_to_bytes(eng.download_states(order), n)
+    return h, {b: i for i, b in enumerate(basis)}
+
+
+# ---------------------------------------------------------------------------------------
+# Lanczos (upstream finite.py:1897-1995) and the eigensystem (finite.py:58-118)
+# ---------------------------------------------------------------------------------------
+
+
+def _scipy_to_device_csr(eng, h):
+    """Upload a SciPy matrix as a device CSR (values as stored; h.dot semantics)."""
+    hc = scipy.sparse.csr_matrix(h)
+    hc.sum_duplicates()
+    rp = torch.from_numpy(hc.indptr.astype(np.int64)).to(eng.device)
+    col = torch.from_numpy(hc.indices.astype(np.int32)).to(eng.device)
+    data = np.asarray(hc.data, dtype=np.complex128)
+    if np.all(data.imag == 0):
+        return CsrMatrix(rp, col, val_r=torch.from_numpy(np.ascontiguousarray(data.real)).to(eng.device))
+    return CsrMatrix(rp, col, val_c=torch.from_numpy(np.ascontiguousarray(data).view(np.float64).reshape(-1, 2))
+                     .to(eng.device))
+
+
+def get_tridiagonal_krylov_vectors(h, psi0, krylovSize, h_local=False, mode="sparse"):
+    """Lanczos alpha/beta without reorthogonalisation (upstream finite.py:1897-1995).
+
+    ``h``: SciPy sparse/dense matrix or a device :class:`CsrMatrix`; ``psi0``: start vector.
+    Raises ValueError on beta == 0 like upstream.
+    """
+    eng = get_engine()
+    csr = h if isinstance(h, CsrMatrix) else _scipy_to_device_csr(eng, scipy.sparse.csr_matrix(h))
+    n = len(psi0)
+    k = min(int(krylovSize), n)
+    v0 = torch.as_tensor(np.asarray(psi0, dtype=np.complex128)).to(eng.device).view(n, 1)
+    try:
+        alpha, beta = eng.lanczos(csr, v0, [k])
+    except L.EdgpuError as exc:
+        if exc.status == L.EDGPU_ERR_BREAKDOWN:
+            raise ValueError("Warning: beta==0, implementation absent!") from exc
+        raise
+    return alpha[0, :k].cpu().numpy(), beta[0, : k - 1].cpu().numpy()
+
+
+def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
+    """Lowest ``k`` eigenpairs by Lanczos with full reorthogonalisation (FP64 on the GPU).
+
+    Ritz values come from the Krylov tridiagonal matrix on the host each chunk; iteration
+    stops when every wanted residual ``beta_j |s_{j,i}|`` is below
+    ``tol_rel * max(1, |theta_i|)`` or the Krylov space spans the basis.
+    Returns (energies [k] ascending, eigenvectors [k, N] complex128 device tensor).
+    """
+    n = csr.n
+    k = min(k, n)
+    k_cap = int(min(n, k_cap or max(300, 4 * k + 100)))
+    g = torch.Generator(device=eng.device)
+    g.manual_seed(seed)
+    v0 = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
+    v0 = v0 / torch.linalg.vector_norm(v0)
+
+    def ritz(a, bfull):
+        if len(a) == 1:
+            return np.array(a, dtype=float), np.ones((1, 1))
+        return scipy.linalg.eigh_tridiagonal(a, bfull[: len(a) - 1])
+
+    def residuals(a, bfull, j):
+        th, s = ritz(a, bfull)
+        if j >= n:
+            return th, s, np.zeros(min(k, j))
+        return th, s, np.abs(bfull[j - 1] * s[-1, : min(k, j)])
+
+    def stop(a, bfull, j):
+        if j < k:
+            return False
+        th, _, res = residuals(a, bfull, j)
+        return bool(np.all(res <= tol_rel * np.maximum(1.0, np.abs(th[:k]))))
+
+    while True:
+        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop)
+        kk = len(a)
+        th, s, res = residuals(a, bfull, kk)
+        exact = kk >= n or (kk < k_cap and bfull[kk - 1] == 0.0)
+        if exact or stop(a, bfull, kk) or k_cap >= n:
+            break
+        k_cap = min(n, 2 * k_cap)
+    kk = len(a)
+    kw = min(k, kk)
+    coeffs = np.ascontiguousarray(s[:, :kw]).astype(np.complex128)
+    X = eng.combine(V, coeffs)
+    X = X / torch.linalg.vector_norm(X, dim=1, keepdim=True)
+    return th[:kw], X
+
+
+def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", eigenValueTol=1e-9,
+                slaterWeightMin=1e-7):
+    """Lowest eigenpairs and eigenstates as dicts (upstream finite.py:58-118).
+
+    ``groundDiagMode='Lanczos'`` runs Lanczos with full reorthogonalisation on the GPU;
+    ``'full'`` diagonalises the dense matrix (upstream ``np.linalg.eigh``).  Eigenvectors
+    keep product states with ``|amp|^2 >= slaterWeightMin``.
+    """
+    eng = get_engine()
+    n = int(n_spin_orbitals)
+    words_for(n)
+    basis = list(basis)
+    sb = _SortedBasis(eng, basis, n)
+    csr = _device_hamiltonian(eng, _device_op(hOp, eng), sb)
+    if groundDiagMode == "full":
+        h = _csr_to_scipy_given_order(csr, sb.perm).toarray()
+        es, vecs = np.linalg.eigh(h)
+        es = es[:nPsiMax]
+        vecs = vecs[:, :nPsiMax]
+    elif groundDiagMode == "Lanczos":
+        es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3))
+        # sorted position -> caller position
+        vec_sorted = X.t().contiguous()
+        vecs_t = torch.empty_like(vec_sorted)
+        vecs_t[sb.perm] = vec_sorted
+        vecs = vecs_t.cpu().numpy()
+    else:
+        raise ValueError("Wrong diagonalization mode")
+    psis = [
+        {basis[i]: vecs[i, vi] for i in np.nonzero(np.abs(vecs[:, vi]) ** 2 >= slaterWeightMin)[0]}
+        for vi in range(len(es))
+    ]
+    return np.asarray(es), psis

@@ -1,0 +1,225 @@
+/*
+ * edgpu — C ABI of the GB300 exact-diagonalization engine (libedgpu.so).
+ *
+ * Every entry point takes plain device pointers and sizes, never allocates device memory
+ * (scratch comes from a caller-provided workspace sized by the matching *_workspace query),
+ * runs on the caller's CUDA stream and returns an edgpu_status.  Device-side conditions
+ * (buffer overflow, Lanczos breakdown, NaN) are written to a caller-provided int32 device
+ * status word, which the caller reads after synchronising the stream.
+ *
+ * Product states: n_words = ceil(n_spin_orbitals / 64) uint64 words per state, stored
+ * contiguously (array of structures).  Orbital i is bit 63 - (i % 64) of word i / 64, so
+ * lexicographic word order equals the order of the upstream big-endian ``bytes`` states.
+ * n_words must be 1..8 (up to 512 spin-orbitals).
+ *
+ * Complex numbers are interleaved (re, im) doubles or floats.
+ *
+ * Each declaration names the upstream (impurityModel) interface it replaces.
+ */
+#ifndef EDGPU_H
+#define EDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum edgpu_status {
+  EDGPU_OK = 0,
+  EDGPU_ERR_ARG = 1,        /* bad argument (upstream: ValueError / Exception on bad input) */
+  EDGPU_ERR_OVERFLOW = 2,   /* a per-state scratch buffer or output capacity was exceeded */
+  EDGPU_ERR_BREAKDOWN = 3,  /* Lanczos beta == 0 (upstream: ValueError, finite.py:1963,1988) */
+  EDGPU_ERR_NAN = 4,        /* non-finite value produced */
+  EDGPU_ERR_NOCONV = 5,     /* iteration cap reached before convergence */
+  EDGPU_ERR_CUDA = 6,       /* a CUDA launch or runtime call failed */
+  EDGPU_ERR_WORKSPACE = 7   /* workspace smaller than the matching *_workspace query */
+} edgpu_status;
+
+/* Filters of edgpu_apply_columns. */
+enum { EDGPU_FILTER_NONE = 0, EDGPU_FILTER_IN_BASIS = 1, EDGPU_FILTER_NOT_IN_BASIS = 2 };
+
+/*
+ * Compiled operator (term table), device arrays of n_terms entries.
+ *   ops[t]   : up to 4 elementary operators, 16 bits each, slot k = k-th operator of the
+ *              upstream process tuple (left to right).  Slot bits: 15 present, 14 creation
+ *              (0 = annihilation), 0..9 spin-orbital index.  Applied right to left.
+ *   coeff[t] : complex128 amplitude (re, im).
+ *   flags[t] : bit 0 set when the creation and annihilation index multisets are equal
+ *              (the term maps a product state onto itself); bits 8..10 operator count.
+ */
+typedef struct edgpu_terms {
+  const uint64_t* ops;
+  const double* coeff;
+  const uint32_t* flags;
+  int32_t n_terms;
+} edgpu_terms;
+
+/*
+ * Occupation restrictions ``{frozenset(indices): (lo, hi)}`` (upstream finite.applyOp
+ * ``restrictions``): a state passes when lo <= popcount(state & mask[r]) <= hi for all r.
+ * Host memory; copied into the kernel parameters.
+ */
+#define EDGPU_MAX_RESTRICTIONS 8
+#define EDGPU_MAX_WORDS 8
+typedef struct edgpu_restrictions {
+  int32_t n;
+  int32_t lo[EDGPU_MAX_RESTRICTIONS];
+  int32_t hi[EDGPU_MAX_RESTRICTIONS];
+  uint64_t mask[EDGPU_MAX_RESTRICTIONS][EDGPU_MAX_WORDS];
+} edgpu_restrictions;
+
+/* CSR matrix on the device: row_ptr[n+1], col[nnz], values complex (val_c) or real (val_r). */
+typedef struct edgpu_csr {
+  int64_t n;
+  int64_t nnz;
+  const int64_t* row_ptr;
+  const int32_t* col;
+  const double* val_c;  /* complex128 values, or NULL */
+  const double* val_r;  /* real float64 values (used when val_c is NULL) */
+  const float* val_cf;  /* complex64 copy for the mixed-precision form, or NULL */
+  const float* val_rf;  /* float32 copy for the mixed-precision form, or NULL */
+} edgpu_csr;
+
+int edgpu_abi_version(void);
+const char* edgpu_status_string(int status);
+
+/*
+ * H|b> for each single product state b of ``states`` (n_states x n_words).
+ * Replaces upstream ``applyOp(n, hOp, {b: 1}, weight_min, restrictions)``
+ * (impurityModel/ed/finite.py:1301-1511) as called per basis column by
+ * ``get_hamiltonian_matrix`` (finite.py:1514-1610) and ``expand_basis`` (finite.py:1696-1803).
+ * Per state: values of equal output states are summed in term order, entries with
+ * |v|^2 < weight_min are dropped, outputs failing ``restr`` are dropped, and ``filter``
+ * keeps only outputs present in / absent from the sorted ``basis``.  Entries are emitted
+ * in upstream dict order (first occurrence in term order).
+ *
+ * Count pass: offsets == NULL; writes counts[n_states].
+ * Fill pass : offsets[n_states] (exclusive scan of counts); writes any of out_states
+ *             (n_words each), out_index (position in basis, FILTER_IN_BASIS) and out_vals
+ *             (complex128; conjugated when conj_vals != 0).
+ * scratch_entries: per-warp capacity for off-diagonal emissions (0 = default 256); on
+ * overflow *status_dev receives EDGPU_ERR_OVERFLOW and the caller retries larger.
+ */
+int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t n_states, const edgpu_terms* terms,
+                        const edgpu_restrictions* restr, double weight_min, const uint64_t* basis,
+                        int64_t n_basis, int filter, const int64_t* offsets, int64_t* counts,
+                        uint64_t* out_states, int64_t* out_index, double* out_vals, int conj_vals,
+                        int scratch_entries, int32_t* status_dev, void* stream);
+
+/*
+ * Raw emissions of an operator on a multi-configurational state psi = sum_k amps[k] |states[k]>.
+ * Replaces the inner loops of upstream ``applyOp`` (finite.py:1355-1388): for every
+ * (state k, term t) in that order the valid result amps[k] * h_t * sign is emitted; outputs
+ * failing ``restr`` are skipped (upstream checks restrictions on first insertion, which is
+ * the same filter).  Count pass (offsets == NULL) writes counts[n_states]; the fill pass
+ * writes out_states (n_words each) and out_vals (complex128, product without fused
+ * multiply-add, as CPython computes it) at offsets[k] + rank in term order.
+ */
+int edgpu_apply_vector(int n_words, const uint64_t* states, const double* amps, int64_t n_states,
+                       const edgpu_terms* terms, const edgpu_restrictions* restr, const int64_t* offsets,
+                       int64_t* counts, uint64_t* out_states, double* out_vals, void* stream);
+
+/*
+ * Stable LSD radix sort of n keys (n_words each) carrying a uint32 payload.  Replaces the
+ * ``sorted(...)`` of upstream ``expand_basis`` (finite.py:1793) and the dict merging of
+ * ``applyOp``.  keys/payload are sorted in place (results written back to the inputs).
+ * vary_mask: OR over keys of (key XOR first key), n_words host words (NULL = all bits);
+ * digits where it is zero are skipped.
+ */
+size_t edgpu_sort_states_workspace(int n_words, int64_t n);
+int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload, int64_t n, const uint64_t* vary_mask,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* OR over rows of (row XOR row 0) into vary_out[n_words] (device). */
+int edgpu_vary_mask(int n_words, const uint64_t* keys, int64_t n, uint64_t* vary_out, void* stream);
+
+/*
+ * Exclusive prefix sum of int64 ``in`` (n entries) into ``out`` (n + 1 entries; out[n] = total).
+ */
+size_t edgpu_scan_workspace(int64_t n);
+int edgpu_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/*
+ * Segment heads of sorted keys: head[i] = 1 if i == 0 or keys[i] != keys[i-1] (int64 0/1).
+ */
+int edgpu_segment_heads(int n_words, const uint64_t* keys, int64_t n, int64_t* head, void* stream);
+
+/*
+ * Compact sorted keys by segment: for every head i (head_scan[i+1] != head_scan[i]) write
+ * keys[i] to out_keys[head_scan[i]], the first payload to out_first[head_scan[i]] and, when
+ * vals != NULL, the sequential sum (in sorted order) of vals[payload[j]] over the segment
+ * into out_vals.  Replaces upstream dict accumulation ``psiNew[s] += amp * h * sign``.
+ */
+int edgpu_segment_reduce(int n_words, const uint64_t* keys, const uint32_t* payload, int64_t n,
+                         const int64_t* head_scan, const double* vals, uint64_t* out_keys, uint32_t* out_first,
+                         double* out_vals, void* stream);
+
+/*
+ * Merge two sorted, disjoint state arrays a (na) and b (nb) into out (na + nb).
+ * Replaces ``basis += sorted(basis_new)`` bookkeeping of upstream expand_basis, kept sorted.
+ */
+int edgpu_merge_states(int n_words, const uint64_t* a, int64_t na, const uint64_t* b, int64_t nb, uint64_t* out,
+                       void* stream);
+
+/* Position of each query state in the sorted basis, or -1 (upstream ``basis_index`` dict). */
+int edgpu_lookup_states(int n_words, const uint64_t* basis, int64_t n_basis, const uint64_t* query, int64_t nq,
+                        int64_t* out_index, void* stream);
+
+/*
+ * y = H x for R vectors (row-major, complex128): x is [ncols][R] where ncols exceeds every
+ * column index of H, y is [n][R].  Replaces ``h.dot(v)`` of upstream
+ * get_tridiagonal_krylov_vectors (finite.py:1946-1989).
+ */
+int edgpu_spmv(const edgpu_csr* h, const double* x, double* y, int R, void* stream);
+
+/* Same with complex64 vectors and float32 accumulation (mixed-precision form). */
+int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* stream);
+
+/*
+ * Batched Lanczos tridiagonalisation without reorthogonalisation, R independent runs on one
+ * CSR matrix.  Replaces upstream ``get_tridiagonal_krylov_vectors`` (finite.py:1897-1995):
+ * same recurrence (alpha_j = Re<H v_j, v_j>, w = H v_j - alpha_j v_j - beta_{j-1} v_{j-1},
+ * beta_j = ||w||).  v0: [n][R] normalised start vectors (complex128, read only).
+ * k_max[R]: per-run Krylov size (upstream min(krylovSize, dim of the run's basis)).
+ * K = max over k_max.  Outputs alpha[R][K], beta[R][K] (beta[r][j] for j < k_max[r]-1).
+ * precision: 0 = complex128 vectors and values; 1 = complex64 vectors, float32 SpMV
+ * accumulation, float64 alpha/beta reductions.  Breakdown (beta == 0 before k_max) sets
+ * *status_dev = EDGPU_ERR_BREAKDOWN.
+ */
+size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision);
+int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                  double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
+/*
+ * Lanczos with full (twice classical Gram-Schmidt) reorthogonalisation, one run, complex128,
+ * storing the Krylov basis V[K_cap][n].  Runs steps j0 .. j1-1 (resumable: the caller keeps
+ * V, alpha, beta and the work vector between calls).  Step j0 == 0 copies v0 into V[0].
+ * Replaces upstream ``scipy.sparse.linalg.eigsh(which="SA")`` in ``eigensystem``
+ * (finite.py:105) and the BiCGSTAB solves of ``getRIXSmap`` (spectra.py:962,1080) through
+ * Ritz pairs and shifted tridiagonal solves on the host.
+ * w: work vector [n] complex128 (carries H v_{j} - ... between calls).
+ */
+size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap);
+int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
+                         double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                         void* stream);
+
+/* X[m][n] = sum_k C[k][m] V[k][n] (complex128): Ritz vectors / shifted-solve solutions. */
+int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, double* X, void* stream);
+
+/*
+ * Continued fractions (upstream spectra.py:678-680) for R runs on n_omega points:
+ * g[r][w] = scale[r] / (z - a0 - b0^2 / (z - a1 - ...)), z = omega[w] + i*delta + e[r],
+ * depth k_len[r] (alpha[r][0..k_len), beta[r][0..k_len-1), row stride K).
+ */
+int edgpu_cfrac(const double* alpha, const double* beta, const int32_t* k_len, int K, int R, const double* omega,
+                int n_omega, double delta, const double* e, const double* scale, double* g, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EDGPU_H */

@@ -1,0 +1,731 @@
+"""NumPy/SciPy restatement of impurityModel's ED hot path (oracle; test infrastructure).
+
+Every public function names the upstream function it restates (paths relative to the
+upstream project root).  Two implementations of operator application exist:
+
+* :func:`apply_op` — a direct dict restatement of ``finite.applyOp``
+  (``impurityModel/ed/finite.py:1301-1511``) including the ``opResult`` memo and the
+  restriction check on first insertion.  Pure Python; used for small inputs.
+* :func:`h_columns` — a vectorised (NumPy) evaluation of ``applyOp(n, hOp, {b: 1},
+  restrictions=...)`` for many single product states ``b`` at once.  Values are summed
+  per output state sequentially in operator-term order, which reproduces the upstream
+  sums bit for bit (``psiNew[stateB] += amp * h * signTot`` with ``amp == 1``).
+
+Product states are ``bytes`` at the API (upstream format: orbital ``i`` is bit
+``7 - i % 8`` of byte ``i // 8``) and ``uint64`` words internally (orbital ``i`` is bit
+``63 - i % 64`` of word ``i // 64``), so lexicographic word order equals ``bytes`` order.
+"""
+
+from __future__ import annotations
+
+import itertools
+import math
+from math import sqrt
+
+import numpy as np
+import scipy.sparse
+import scipy.sparse.linalg
+
+K_B = 8.617333262e-05  # eV/K, scipy.constants "Boltzmann constant in eV/K"
+
+__all__ = [
+    "n_words",
+    "bytes_to_words",
+    "words_to_bytes",
+    "tuple_to_bytes",
+    "bytes_to_tuple",
+    "create_sign",
+    "remove_sign",
+    "TermTable",
+    "restriction_masks",
+    "apply_op",
+    "h_columns",
+    "get_basis",
+    "expand_basis",
+    "get_hamiltonian_matrix",
+    "hamiltonian_from_columns",
+    "expand_basis_and_hamiltonian",
+    "get_tridiagonal_krylov_vectors",
+    "continued_fraction",
+    "eigensystem",
+    "get_green",
+    "get_spectra",
+    "get_rixs_map",
+    "exact_green",
+    "thermal_average",
+    "norm2",
+    "K_B",
+]
+
+# ---------------------------------------------------------------------------------------
+# Product-state codecs (impurityModel/ed/product_state_representation.py:131-161, 246-273)
+# ---------------------------------------------------------------------------------------
+
+
+def n_words(n_spin_orbitals):
+    return (n_spin_orbitals + 63) // 64
+
+
+def bytes_to_words(states, n_spin_orbitals):
+    """list of upstream ``bytes`` states -> ``uint64[N, W]`` (big-endian words)."""
+    w = n_words(n_spin_orbitals)
+    nb = 8 * w
+    buf = b"".join(s + b"\x00" * (nb - len(s)) for s in states)
+    if not states:
+        return np.zeros((0, w), dtype=np.uint64)
+    return np.frombuffer(buf, dtype=">u8").astype(np.uint64).reshape(len(states), w)
+
+
+def words_to_bytes(words, n_spin_orbitals):
+    nbytes = (n_spin_orbitals + 7) // 8
+    arr = np.ascontiguousarray(np.asarray(words, dtype=np.uint64).astype(">u8"))
+    raw = arr.tobytes()
+    stride = arr.shape[1] * 8 if arr.ndim == 2 else 8
+    return [raw[k * stride : k * stride + nbytes] for k in range(arr.shape[0])]
+
+
+def tuple_to_bytes(t, n_spin_orbitals):
+    """``psr.tuple2bytes`` (product_state_representation.py:262-273)."""
+    nbytes = (n_spin_orbitals + 7) // 8
+    v = 0
+    for i in t:
+        v |= 1 << (8 * nbytes - 1 - i)
+    return v.to_bytes(nbytes, "big")
+
+
+def bytes_to_tuple(b, n_spin_orbitals):
+    nbytes = len(b)
+    v = int.from_bytes(b, "big")
+    return tuple(i for i in range(n_spin_orbitals) if (v >> (8 * nbytes - 1 - i)) & 1)
+
+
+def create_sign(v, i, nbits):
+    """``create.ubitarray`` (impurityModel/ed/create.py:124-151) on an int state.
+
+    ``nbits`` is the padded bit width; orbital ``i`` is bit ``nbits-1-i``.  Returns
+    ``(new_state, sign)`` with sign 0 when the orbital is occupied.
+    """
+    pos = nbits - 1 - i
+    if (v >> pos) & 1:
+        return v, 0
+    sign = -1 if bin(v >> (pos + 1)).count("1") & 1 else 1
+    return v | (1 << pos), sign
+
+
+def remove_sign(v, i, nbits):
+    """``remove.ubitarray`` (impurityModel/ed/remove.py:124-150) on an int state."""
+    pos = nbits - 1 - i
+    if not (v >> pos) & 1:
+        return v, 0
+    sign = -1 if bin(v >> (pos + 1)).count("1") & 1 else 1
+    return v & ~(1 << pos), sign
+
+
+# ---------------------------------------------------------------------------------------
+# Operator application
+# ---------------------------------------------------------------------------------------
+
+
+def apply_op(n_spin_orbitals, op, psi, slaterWeightMin=1e-12, restrictions=None, opResult=None):
+    """Restatement of ``finite.applyOp`` (impurityModel/ed/finite.py:1301-1511).
+
+    All four branches (with/without ``restrictions``, with/without ``opResult``) follow
+    upstream, including the restriction check only on first insertion into the result
+    (``:1379-1388``), the per-state memo pruning (``:1459-1464``, ``:1499-1504``) and the
+    final pruning of ``|amp|^2 < slaterWeightMin`` (``:1508-1510``).
+    """
+    if not psi:
+        return {}
+    nbytes = len(next(iter(psi)))
+    nbits = 8 * nbytes
+    items = list(op.items())
+    restr = None
+    if restrictions is not None:
+        restr = []
+        for idx, (lo, hi) in restrictions.items():
+            mask = 0
+            for i in idx:
+                mask |= 1 << (nbits - 1 - i)
+            restr.append((mask, lo, hi))
+
+    def allowed(v):
+        for mask, lo, hi in restr:
+            n = bin(v & mask).count("1")
+            if n < lo or hi < n:
+                return False
+        return True
+
+    def act(v, process):
+        sign_tot = 1
+        for i, action in process[::-1]:
+            if action == "a":
+                v, s = remove_sign(v, i, nbits)
+            elif action == "c":
+                v, s = create_sign(v, i, nbits)
+            else:
+                raise ValueError("unknown action %r" % action)
+            if s == 0:
+                return None, 0
+            sign_tot *= s
+        return v, sign_tot
+
+    psi_new = {}
+    if opResult is None:
+        for state, amp in psi.items():
+            v0 = int.from_bytes(state, "big")
+            for process, h in items:
+                v, s = act(v0, process)
+                if s == 0:
+                    continue
+                sb = v.to_bytes(nbytes, "big")
+                if sb in psi_new:
+                    psi_new[sb] += amp * h * s
+                elif restr is None or allowed(v):
+                    psi_new[sb] = amp * h * s
+    else:
+        for state, amp in psi.items():
+            if state in opResult:
+                for s2, a2 in opResult[state].items():
+                    if s2 in psi_new:
+                        psi_new[s2] += a2 * amp
+                    else:
+                        psi_new[s2] = a2 * amp
+                continue
+            v0 = int.from_bytes(state, "big")
+            memo = {}
+            opResult[state] = memo
+            for process, h in items:
+                v, s = act(v0, process)
+                if s == 0:
+                    continue
+                sb = v.to_bytes(nbytes, "big")
+                if restr is None:
+                    if sb in memo:
+                        memo[sb] += h * s
+                    else:
+                        memo[sb] = h * s
+                    if sb in psi_new:
+                        psi_new[sb] += amp * h * s
+                    else:
+                        psi_new[sb] = amp * h * s
+                else:
+                    if sb in psi_new:
+                        psi_new[sb] += amp * h * s
+                        if sb in memo:
+                            memo[sb] += h * s
+                        else:
+                            memo[sb] = h * s
+                    elif allowed(v):
+                        psi_new[sb] = amp * h * s
+                        memo[sb] = h * s
+            for sb, a in list(memo.items()):
+                if abs(a) ** 2 < slaterWeightMin:
+                    memo.pop(sb)
+    for sb, a in list(psi_new.items()):
+        if abs(a) ** 2 < slaterWeightMin:
+            psi_new.pop(sb)
+    return psi_new
+
+
+class TermTable:
+    """Operator dict -> arrays: ``n_ops[T]``, ``orb[T, 4]``, ``cre[T, 4]``, ``coeff[T]``.
+
+    ``orb[t, k]``/``cre[t, k]`` list the term's elementary operators left to right as
+    written in the dict key; application runs right to left (``finite.py:1365``).
+    """
+
+    def __init__(self, op):
+        keys = list(op.keys())
+        t = len(keys)
+        self.n_ops = np.zeros(t, dtype=np.int32)
+        self.orb = np.zeros((t, 4), dtype=np.int32)
+        self.cre = np.zeros((t, 4), dtype=bool)
+        self.coeff = np.zeros(t, dtype=np.complex128)
+        for k, key in enumerate(keys):
+            if len(key) > 4:
+                raise ValueError("terms with more than 4 operators are not supported")
+            self.n_ops[k] = len(key)
+            for j, (i, a) in enumerate(key):
+                self.orb[k, j] = i
+                self.cre[k, j] = a == "c"
+            self.coeff[k] = complex(op[key])
+
+    def __len__(self):
+        return len(self.n_ops)
+
+
+def restriction_masks(restrictions, n_spin_orbitals):
+    """``{frozenset(idx): (lo, hi)}`` -> list of ``(mask uint64[W], lo, hi)``."""
+    w = n_words(n_spin_orbitals)
+    out = []
+    if not restrictions:
+        return out
+    for idx, (lo, hi) in restrictions.items():
+        m = np.zeros(w, dtype=np.uint64)
+        for i in idx:
+            m[i // 64] |= np.uint64(1) << np.uint64(63 - i % 64)
+        out.append((m, int(lo), int(hi)))
+    return out
+
+
+_ONE = np.uint64(1)
+_ALL = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _apply_terms(words, table):
+    """Apply every term to every state. Returns (col, term, out_words, value) arrays."""
+    n, w = words.shape
+    cols, terms, outs, vals = [], [], [], []
+    for t in range(len(table)):
+        cur = words.copy()
+        valid = np.ones(n, dtype=bool)
+        parity = np.zeros(n, dtype=np.int64)
+        for k in range(table.n_ops[t] - 1, -1, -1):
+            i = int(table.orb[t, k])
+            wi, bi = i // 64, i % 64
+            m = _ONE << np.uint64(63 - bi)
+            occ = (cur[:, wi] & m) != 0
+            if table.cre[t, k]:
+                valid &= ~occ
+            else:
+                valid &= occ
+            # orbitals with index < i: all earlier words and bits above bi in word wi
+            above = np.uint64(0) if bi == 0 else (_ALL << np.uint64(64 - bi))
+            cnt = np.bitwise_count(cur[:, wi] & above).astype(np.int64)
+            if wi > 0:
+                cnt += np.bitwise_count(cur[:, :wi]).sum(axis=1).astype(np.int64)
+            parity += cnt
+            cur[:, wi] ^= m
+        idx = np.nonzero(valid)[0]
+        if idx.size == 0:
+            continue
+        sign = np.where(parity[idx] & 1, -1.0, 1.0)
+        cols.append(idx)
+        terms.append(np.full(idx.size, t, dtype=np.int64))
+        outs.append(cur[idx])
+        vals.append(table.coeff[t] * sign)
+    if not cols:
+        return (np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros((0, w), np.uint64), np.zeros(0, complex))
+    return np.concatenate(cols), np.concatenate(terms), np.concatenate(outs), np.concatenate(vals)
+
+
+def h_columns(words, table, restrictions=None, weight_min=1e-12, chunk=4096):
+    """``applyOp(n, op, {b: 1}, weight_min, restrictions)`` for every row ``b`` of ``words``.
+
+    Restates ``finite.py:1301-1388`` + ``:1508-1510`` for single product states with unit
+    amplitude.  Returns ``(colptr[N+1], out_words[M, W], values[M])`` where the entries
+    of column ``j`` are ``colptr[j]:colptr[j+1]`` in upstream dict order (first occurrence
+    in term order) and values are summed sequentially in term order.
+    """
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    n, w = words.shape
+    masks = restrictions if isinstance(restrictions, list) else None
+    counts = np.zeros(n, dtype=np.int64)
+    all_out, all_val, all_col = [], [], []
+    for c0 in range(0, n, chunk):
+        sub = words[c0 : c0 + chunk]
+        col, term, out, val = _apply_terms(sub, table)
+        if col.size == 0:
+            continue
+        keys = [term] + [out[:, k] for k in range(w - 1, -1, -1)] + [col]
+        order = np.lexsort(keys)
+        col, term, out, val = col[order], term[order], out[order], val[order]
+        newseg = np.ones(col.size, dtype=bool)
+        newseg[1:] = (col[1:] != col[:-1]) | np.any(out[1:] != out[:-1], axis=1)
+        starts = np.nonzero(newseg)[0]
+        lens = np.diff(np.append(starts, col.size))
+        acc = val[starts].copy()
+        for k in range(1, int(lens.max())):
+            m = lens > k
+            acc[m] = acc[m] + val[starts[m] + k]
+        scol = col[starts]
+        sout = out[starts]
+        sfirst = term[starts]
+        keep = np.abs(acc) ** 2 >= weight_min
+        if masks:
+            for mw, lo, hi in masks:
+                cnt = np.bitwise_count(sout & mw[None, :]).sum(axis=1)
+                keep &= (cnt >= lo) & (cnt <= hi)
+        scol, sout, acc, sfirst = scol[keep], sout[keep], acc[keep], sfirst[keep]
+        order = np.lexsort((sfirst, scol))
+        scol, sout, acc = scol[order], sout[order], acc[order]
+        np.add.at(counts, scol + c0, 1)
+        all_out.append(sout)
+        all_val.append(acc)
+        all_col.append(scol + c0)
+    colptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=colptr[1:])
+    if all_out:
+        out = np.concatenate(all_out)
+        val = np.concatenate(all_val)
+    else:
+        out = np.zeros((0, w), np.uint64)
+        val = np.zeros(0, complex)
+    return colptr, out, val
+
+
+def _lex_key(words):
+    """View rows of uint64[N, W] as sortable void keys (big-endian bytes)."""
+    be = np.ascontiguousarray(words.astype(">u8"))
+    return be.view(np.dtype((np.void, be.shape[1] * 8))).ravel()
+
+
+def _index_in(sorted_words, query):
+    """Row index of each query row in lexicographically sorted rows, -1 if absent."""
+    if sorted_words.shape[0] == 0:
+        return np.full(query.shape[0], -1, dtype=np.int64)
+    sk = _lex_key(sorted_words)
+    qk = _lex_key(query)
+    pos = np.searchsorted(sk, qk)
+    pos_c = np.minimum(pos, sk.size - 1)
+    hit = sk[pos_c] == qk
+    return np.where(hit, pos_c, -1)
+
+
+def _sort_rows(words):
+    keys = [words[:, k] for k in range(words.shape[1] - 1, -1, -1)]
+    return np.lexsort(keys) if words.shape[0] else np.zeros(0, np.int64)
+
+
+# ---------------------------------------------------------------------------------------
+# Basis construction
+# ---------------------------------------------------------------------------------------
+
+
+def _c2i(nBaths, spin_orb):
+    i = 0
+    for lp in nBaths.keys():
+        for sp in range(2):
+            for mp in range(-lp, lp + 1):
+                if (lp, sp, mp) == spin_orb:
+                    return i
+                i += 1
+    for lp, nb in nBaths.items():
+        for b in range(nb):
+            if (lp, b) == spin_orb:
+                return i
+            i += 1
+    raise KeyError(spin_orb)
+
+
+def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
+    """Restatement of ``finite.get_basis`` (impurityModel/ed/finite.py:294-374)."""
+    basis_l = {}
+    for l in nBaths.keys():
+        basis_l[l] = []
+        for dn_val in range(dnValBaths[l] + 1):
+            for dn_con in range(dnConBaths[l] + 1):
+                dn_imp = dn_val - dn_con
+                if abs(dn_imp) <= dnTol[l]:
+                    n_imp = n0imp[l] + dn_imp
+                    n_val = valBaths[l] - dn_val
+                    n_con = dn_con
+                    idx = [_c2i(nBaths, (l, s, m)) for s in range(2) for m in range(-l, l + 1)]
+                    b_imp = tuple(itertools.combinations(idx, n_imp))
+                    if valBaths[l] == 0:
+                        b_val = ((),)
+                    else:
+                        idx = [_c2i(nBaths, (l, b)) for b in range(valBaths[l])]
+                        b_val = tuple(itertools.combinations(idx, n_val))
+                    if nBaths[l] - valBaths[l] == 0:
+                        b_con = ((),)
+                    else:
+                        idx = [_c2i(nBaths, (l, b)) for b in range(valBaths[l], nBaths[l])]
+                        b_con = tuple(itertools.combinations(idx, n_con))
+                    for bi in b_imp:
+                        for bv in b_val:
+                            for bc in b_con:
+                                basis_l[l].append(bi + bv + bc)
+    n = sum(2 * (2 * ang + 1) + nb for ang, nb in nBaths.items())
+    basis = []
+    for conf in itertools.product(*basis_l.values()):
+        basis.append(tuple_to_bytes(tuple(sorted(itertools.chain.from_iterable(conf))), n))
+    return tuple(basis)
+
+
+class _ColumnMemo:
+    """The ``h_dict`` memo of upstream, held as arrays: state bytes -> column entries."""
+
+    def __init__(self, n_spin_orbitals, hOp, restrictions, weight_min=1e-12):
+        self.n = n_spin_orbitals
+        self.table = TermTable(hOp)
+        self.masks = restriction_masks(restrictions, n_spin_orbitals) if restrictions is not None else None
+        self.weight_min = weight_min
+        self.cols = {}
+
+    def ensure(self, states_bytes):
+        todo = [s for s in states_bytes if s not in self.cols]
+        if not todo:
+            return
+        words = bytes_to_words(todo, self.n)
+        colptr, out, val = h_columns(words, self.table, self.masks, self.weight_min)
+        out_b = words_to_bytes(out, self.n) if out.shape[0] else []
+        for j, s in enumerate(todo):
+            a, b = colptr[j], colptr[j + 1]
+            self.cols[s] = (out_b[a:b], val[a:b])
+
+
+def expand_basis(n_spin_orbitals, h_dict, hOp, basis0, restrictions, parallelization_mode="serial", memo=None):
+    """Restatement of ``finite.expand_basis`` (impurityModel/ed/finite.py:1696-1803).
+
+    Breadth-first closure of ``basis0`` under ``hOp`` with ``restrictions``; each new layer
+    is appended in sorted (``bytes``) order.  ``memo`` plays the role of ``h_dict``.
+    """
+    if memo is None:
+        memo = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    basis = list(basis0)
+    i, n = 0, len(basis)
+    while i < n:
+        basis_set = set(basis)
+        memo.ensure(basis[i:n])
+        new = set()
+        for b in basis[i:n]:
+            for s in memo.cols[b][0]:
+                if s not in basis_set:
+                    new.add(s)
+        i = n
+        basis += sorted(new)
+        n = len(basis)
+    return tuple(basis)
+
+
+def hamiltonian_from_columns(memo, basis):
+    """``finite.get_hamiltonian_matrix_from_h_dict`` sparse/serial (finite.py:1613-1693)."""
+    index = {b: k for k, b in enumerate(basis)}
+    data, row, col = [], [], []
+    for j, b in enumerate(basis):
+        outs, vals = memo.cols[b]
+        for s, v in zip(outs, vals):
+            data.append(v)
+            col.append(j)
+            row.append(index[s])
+    n = len(basis)
+    h = scipy.sparse.csr_matrix((np.array(data, dtype=complex), (row, col)), shape=(n, n))
+    return h, index
+
+
+def expand_basis_and_hamiltonian(n_spin_orbitals, h_dict, hOp, basis0, restrictions, memo=None):
+    """``finite.expand_basis_and_hamiltonian`` (finite.py:1806-1894)."""
+    if memo is None:
+        memo = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    basis = expand_basis(n_spin_orbitals, None, hOp, basis0, restrictions, memo=memo)
+    return hamiltonian_from_columns(memo, basis)
+
+
+def get_hamiltonian_matrix(n_spin_orbitals, hOp, basis, weight_min=1e-12):
+    """``finite.get_hamiltonian_matrix`` sparse modes (finite.py:1514-1610).
+
+    ``applyOp`` without restrictions per column; only rows present in ``basis`` are kept.
+    """
+    words = bytes_to_words(list(basis), n_spin_orbitals)
+    colptr, out, val = h_columns(words, TermTable(hOp), None, weight_min)
+    order = _sort_rows(words)
+    srt = words[order]
+    pos = _index_in(srt, out)
+    rows = np.where(pos >= 0, order[np.maximum(pos, 0)], -1)
+    cols = np.repeat(np.arange(len(basis)), np.diff(colptr))
+    keep = rows >= 0
+    n = len(basis)
+    return scipy.sparse.csr_matrix((val[keep], (rows[keep], cols[keep])), shape=(n, n))
+
+
+# ---------------------------------------------------------------------------------------
+# Lanczos, continued fraction, eigensystem
+# ---------------------------------------------------------------------------------------
+
+
+def get_tridiagonal_krylov_vectors(h, psi0, krylovSize):
+    """``finite.get_tridiagonal_krylov_vectors`` (finite.py:1897-1995), serial branch."""
+    n = len(psi0)
+    krylovSize = min(krylovSize, n)
+    alpha = np.zeros(krylovSize, dtype=float)
+    beta = np.zeros(krylovSize - 1, dtype=float)
+    v = np.zeros((2, n), dtype=complex)
+    v[0, :] = psi0
+    wp = h.dot(v[0, :])
+    alpha[0] = np.dot(np.conj(wp), v[0, :]).real
+    w = wp - alpha[0] * v[0, :]
+    for j in range(1, krylovSize):
+        beta[j - 1] = sqrt(np.sum(np.abs(w) ** 2))
+        if beta[j - 1] != 0:
+            v[1, :] = w / beta[j - 1]
+        else:
+            raise ValueError("Warning: beta==0, implementation absent!")
+        wp = h.dot(v[1, :])
+        alpha[j] = np.dot(np.conj(wp), v[1, :]).real
+        w = wp - alpha[j] * v[1, :] - beta[j - 1] * v[0, :]
+        v[0, :] = v[1, :]
+    return alpha, beta
+
+
+def continued_fraction(alpha, beta, omega, delta, e):
+    """Bottom-up continued fraction of ``spectra.getGreen`` (spectra.py:678-680)."""
+    omega_p = np.asarray(omega) + 1j * delta + e
+    k = len(alpha)
+    g = None
+    for i in range(k - 1, -1, -1):
+        g = 1.0 / (omega_p - alpha[i]) if i == k - 1 else 1.0 / (omega_p - alpha[i] - beta[i] ** 2 * g)
+    return g
+
+
+def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", eigenValueTol=1e-9,
+                slaterWeightMin=1e-7):
+    """``finite.eigensystem`` (finite.py:58-118): ARPACK ``eigsh`` or dense ``eigh``."""
+    h = get_hamiltonian_matrix(n_spin_orbitals, hOp, basis)
+    if groundDiagMode == "full":
+        es, vecs = np.linalg.eigh(h.toarray())
+        es = es[:nPsiMax]
+        vecs = vecs[:, :nPsiMax]
+    else:
+        es, vecs = scipy.sparse.linalg.eigsh(h, k=nPsiMax, which="SA", tol=eigenValueTol)
+        idx = np.argsort(es)
+        es = np.array([es[i] for i in idx])
+        vecs = np.array([vecs[:, i] for i in idx]).T
+    psis = [
+        {basis[i]: vecs[i, vi] for i in range(len(basis)) if slaterWeightMin <= abs(vecs[i, vi]) ** 2}
+        for vi in range(len(es))
+    ]
+    return es, psis
+
+
+def norm2(psi):
+    """``finite.norm2`` (finite.py:2020-2033)."""
+    return sum(abs(a) ** 2 for a in psi.values())
+
+
+def thermal_average(energies, observable, T=300):
+    """``average.thermal_average`` (impurityModel/ed/average.py:11-45)."""
+    energies = np.asarray(energies)
+    if len(energies) != np.shape(observable)[0]:
+        raise ValueError("Passed array is not of the right shape")
+    z = 0
+    o_average = 0
+    shift = np.min(energies)
+    for e, o in zip(energies, observable):
+        weight = np.exp(-(e - shift) / (K_B * T))
+        z += weight
+        o_average = o_average + weight * o
+    return o_average / z
+
+
+# ---------------------------------------------------------------------------------------
+# Green's functions and spectra (impurityModel/ed/spectra.py)
+# ---------------------------------------------------------------------------------------
+
+
+def exact_green(h, psi0, omega, delta, e):
+    """Exact resolvent ``<psi0|((omega + i delta + e) - H)^{-1}|psi0>`` by dense diagonalisation.
+
+    Not an upstream function: the limit the Lanczos continued fraction approximates,
+    used to judge the accuracy of Krylov results whose size is below the sector dimension.
+    """
+    ev, u = np.linalg.eigh(h.toarray() if hasattr(h, "toarray") else np.asarray(h))
+    c2 = np.abs(u.conj().T @ psi0) ** 2
+    z = np.asarray(omega) + 1j * delta + e
+    return (c2[None, :] / (z[:, None] - ev[None, :])).sum(axis=1)
+
+
+def get_green(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeightMin, restrictions=None,
+              memo=None, return_coeffs=False, exact=False):
+    """``spectra.getGreen`` sparse mode (spectra.py:551-681); ``exact=True`` returns the
+    exact resolvent of the same sector instead of the Krylov continued fraction."""
+    g = np.zeros(len(omega), dtype=complex)
+    if len(psi) == 0:
+        return (g, None, None, 0) if return_coeffs else g
+    if memo is None:
+        memo = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    h, index = expand_basis_and_hamiltonian(n_spin_orbitals, None, hOp, list(psi.keys()), restrictions, memo=memo)
+    n = len(index)
+    psi0 = np.zeros(n, dtype=complex)
+    for ps, amp in psi.items():
+        psi0[index[ps]] = amp
+    k = min(krylovSize, n)
+    if exact:
+        g = exact_green(h, psi0, omega, delta, e)
+        return (g, None, None, n) if return_coeffs else g
+    alpha, beta = get_tridiagonal_krylov_vectors(h, psi0, k)
+    g = continued_fraction(alpha, beta, omega, delta, e)
+    if return_coeffs:
+        return g, alpha, beta, n
+    return g
+
+
+def get_spectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=None, krylovSize=150,
+                slaterWeightMin=1e-7, return_coeffs=False, exact=False):
+    """``spectra.getSpectra`` in its default ``H_build`` mode (spectra.py:684-806)."""
+    n = len(es)
+    gs = np.zeros((n, len(tOps), len(w)), dtype=complex)
+    memo = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    coeffs = {}
+    for t, top in enumerate(tOps):
+        t_big = {}
+        for i in range(n):
+            psi_r = apply_op(n_spin_orbitals, top, psis[i], slaterWeightMin, restrictions, t_big)
+            normalization = sqrt(norm2(psi_r))
+            for state in psi_r.keys():
+                psi_r[state] /= normalization
+            g, a, b, dim = get_green(n_spin_orbitals, es[i], psi_r, hOp, w, delta, krylovSize, slaterWeightMin,
+                                     restrictions, memo=memo, return_coeffs=True, exact=exact)
+            gs[i, t, :] = normalization**2 * g
+            coeffs[(i, t)] = (a, b, dim, normalization)
+    if return_coeffs:
+        return gs, coeffs
+    return gs
+
+
+def get_rixs_map(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, delta1, delta2, restrictions=None,
+                 krylovSize=150, slaterWeightMin=1e-7, solver="bicgstab", rtol=1e-5, share_out_memo=True,
+                 exact=False):
+    """``spectra.getRIXSmap`` (spectra.py:809-1130), ``wIn``/``H_build_wIn`` branch.
+
+    ``solver='bicgstab'`` calls SciPy's BiCGSTAB with the given ``rtol`` as upstream does
+    (upstream uses the default 1e-5); ``solver='direct'`` solves each shifted system with
+    a sparse LU factorisation, the tight reference used to pin the GPU's shifted solves.
+    ``exact=True`` replaces the final Krylov continued fractions by exact resolvents.
+    ``share_out_memo=True`` keeps upstream's single ``opResult`` dict shared by every
+    outgoing operator (``tOut_big = [{}] * len(tOpsOut)``, spectra.py:910): each product
+    state's outgoing action is computed once, with the first outgoing operator, and reused
+    for the other channels.
+    """
+    n_e = len(es)
+    gs = np.zeros((n_e, len(tOpsIn), len(tOpsOut), len(wIns), len(wLoss)), dtype=complex)
+    memo_exc = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    memo_gnd = _ColumnMemo(n_spin_orbitals, hOp, restrictions)
+    if share_out_memo:
+        shared = {}
+        t_out_big = [shared] * len(tOpsOut)
+    else:
+        t_out_big = [{} for _ in tOpsOut]
+    for t_in, top_in in enumerate(tOpsIn):
+        t_in_big = {}
+        for ie in range(n_e):
+            psi = psis[ie]
+            e = es[ie]
+            psi1 = apply_op(n_spin_orbitals, top_in, psi, slaterWeightMin, restrictions, t_in_big)
+            h, index = expand_basis_and_hamiltonian(n_spin_orbitals, None, hOp, list(psi1.keys()), restrictions,
+                                                    memo=memo_exc)
+            n = len(index)
+            y = np.zeros(n, dtype=complex)
+            for ps, amp in psi1.items():
+                y[index[ps]] = amp
+            basis_state = {k: ps for ps, k in index.items()}
+            for iw, w_in in enumerate(wIns):
+                a = scipy.sparse.csr_matrix(([w_in + 1j * delta1 + e] * n, (range(n), range(n))), shape=(n, n))
+                a = a - h
+                if solver == "bicgstab":
+                    x, info = scipy.sparse.linalg.bicgstab(a, y, rtol=rtol)
+                else:
+                    x = scipy.sparse.linalg.spsolve(a.tocsc(), y)
+                psi2 = {basis_state[i]: amp for i, amp in enumerate(x) if amp != 0}
+                for t_out, top_out in enumerate(tOpsOut):
+                    psi3 = apply_op(n_spin_orbitals, top_out, psi2, slaterWeightMin, restrictions, t_out_big[t_out])
+                    normalization = sqrt(norm2(psi3))
+                    for state in psi3.keys():
+                        psi3[state] /= normalization
+                    for state, amp in list(psi3.items()):
+                        if abs(amp) ** 2 < slaterWeightMin:
+                            psi3.pop(state)
+                    gs[ie, t_in, t_out, iw, :] = normalization**2 * get_green(
+                        n_spin_orbitals, e, psi3, hOp, wLoss, delta2, krylovSize, slaterWeightMin, restrictions,
+                        memo=memo_gnd, exact=exact)
+    return gs

@@ -1,0 +1,209 @@
+"""Generate golden fixtures by running the upstream impurityModel implementation.
+
+Run in a container that has the upstream checkout (read-only) at
+``$IMPURITYMODEL_REFERENCE`` (default ``/root/reference``)::
+
+    python tests/golden/make_golden.py
+
+Writes small ``.npz`` files next to this script.  Upstream runs behind the stand-ins of
+``_standins/`` (see ``refenv.py``).  Inputs are the seeded synthetic models of
+``impuritymodel_gb300.models`` plus upstream's own shipped NiO 50-bath inputs
+(``impurityModel/test/referenceOutput/Ni_NiO_50bath/data.npz``, read with a restricted
+unpickler) and its shipped thermal spectra (``XAS.dat``).
+"""
+
+import io
+import os
+import pickle
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import refenv  # noqa: E402
+
+from impuritymodel_gb300 import models as M  # noqa: E402
+from tests.golden.fixtures import encode_op, encode_psi, encode_restrictions, encode_states  # noqa: E402
+
+
+class _SafeUnpickler(pickle.Unpickler):
+    """Only containers, complex numbers and NumPy scalar/array reconstruction."""
+
+    _ALLOWED = {
+        ("collections", "OrderedDict"),
+        ("builtins", "complex"),
+        ("builtins", "frozenset"),
+        ("builtins", "set"),
+        ("builtins", "dict"),
+        ("builtins", "tuple"),
+        ("builtins", "list"),
+    }
+
+    def find_class(self, module, name):
+        if (module, name) in self._ALLOWED:
+            import builtins
+            import collections
+
+            return getattr(collections if module == "collections" else builtins, name)
+        if module in ("numpy.core.multiarray", "numpy._core.multiarray") and name in ("scalar", "_reconstruct"):
+            from numpy._core import multiarray
+
+            return getattr(multiarray, name)
+        if module == "numpy" and name in ("dtype", "ndarray"):
+            return getattr(np, name)
+        raise pickle.UnpicklingError("blocked %s.%s" % (module, name))
+
+
+def _load_npz_object(npz, key):
+    arr = npz[key]
+    return arr.item() if arr.dtype == object and arr.shape == () else arr
+
+
+def load_nio_data(ref_root):
+    path = os.path.join(ref_root, "impurityModel/test/referenceOutput/Ni_NiO_50bath/data.npz")
+    import zipfile
+
+    out = {}
+    with zipfile.ZipFile(path) as z:
+        for name in z.namelist():
+            with z.open(name) as fh:
+                raw = fh.read()
+            key = name[:-4]
+            try:
+                arr = np.load(io.BytesIO(raw), allow_pickle=False)
+            except ValueError:
+                # object array: parse the .npy header, then unpickle the payload safely
+                buf = io.BytesIO(raw)
+                version = np.lib.format.read_magic(buf)
+                if version == (1, 0):
+                    np.lib.format.read_array_header_1_0(buf)
+                else:
+                    np.lib.format.read_array_header_2_0(buf)
+                arr = _SafeUnpickler(buf).load()
+            out[key] = arr
+    return out
+
+
+def main():
+    finite, spectra, psr, create, remove = refenv.load()
+    import contextlib
+
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    t0 = time.time()
+
+    # ---------------- config1: full small pipeline -------------------------------------
+    mod = M.make_model("config1")
+    n = mod.n_spin_orbitals
+    with quiet:
+        basis = finite.get_basis(*mod.basis_args())
+        h = finite.get_hamiltonian_matrix(n, mod.hOp, basis)
+        es, psis = finite.eigensystem(n, mod.hOp, basis, 3)
+    tops = mod.xas_ops()
+    w = np.linspace(-25, 25, 2000)
+    with quiet:
+        gs_xas = spectra.getSpectra(n, mod.hOp, tops, psis, es, w, 0.1, mod.restrictions)
+    psi1 = finite.applyOp(n, tops[0], psis[0], 1e-7, mod.restrictions)
+    with quiet:
+        exp_basis = finite.expand_basis(n, {}, mod.hOp, tuple(psi1.keys()), mod.restrictions)
+        hx, bidx = finite.get_hamiltonian_matrix_from_h_dict(
+            {b: finite.applyOp(n, mod.hOp, {b: 1}, restrictions=mod.restrictions) for b in exp_basis}, exp_basis)
+    # Lanczos coefficients for the normalised psi1
+    nrm = np.sqrt(finite.norm2(psi1))
+    psi0 = np.zeros(len(exp_basis), dtype=complex)
+    for s, a in psi1.items():
+        psi0[bidx[s]] = a / nrm
+    with quiet:
+        alpha, beta = finite.get_tridiagonal_krylov_vectors(hx, psi0, 150)
+    # PS / IPS single-operator spectra for state 0..2
+    with quiet:
+        gs_ps = spectra.getSpectra(n, mod.hOp, mod.ps_ops()[:3], psis, es, -w, -0.1, mod.restrictions)
+        gs_ips = spectra.getSpectra(n, mod.hOp, mod.ips_ops()[:3], psis, es, w, 0.1, mod.restrictions)
+    # small RIXS map with upstream's BiCGSTAB
+    w_in = np.linspace(-5, 10, 4)
+    w_loss = np.linspace(-2, 12, 300)
+    with quiet:
+        gs_rixs = spectra.getRIXSmap(n, mod.hOp, tops, mod.rixs_out_ops(), psis[:1], es[:1], w_in, w_loss,
+                                     0.2, 0.05, mod.restrictions)
+    hcoo = h.tocoo()
+    np.savez_compressed(
+        os.path.join(HERE, "config1.npz"),
+        n_spin_orbitals=n,
+        **encode_op("hop", mod.hOp),
+        **encode_restrictions("restr", mod.restrictions),
+        basis=encode_states(basis, n),
+        h_row=hcoo.row, h_col=hcoo.col, h_val=hcoo.data,
+        es=es,
+        **{k: v for i, p in enumerate(psis) for k, v in encode_psi("eig%d" % i, p, n).items()},
+        w=w, gs_xas=gs_xas,
+        **encode_psi("psi1", psi1, n),
+        exp_basis=encode_states(exp_basis, n),
+        alpha=alpha, beta=beta,
+        gs_ps=gs_ps, gs_ips=gs_ips,
+        w_in=w_in, w_loss=w_loss, gs_rixs=gs_rixs,
+    )
+    print("config1 done %.1fs basis=%d exp=%d" % (time.time() - t0, len(basis), len(exp_basis)))
+
+    # ---------------- applyOp semantics on config1 inputs (memo + restrictions) ----------
+    cases = {}
+    t_big = {}
+    rng = np.random.default_rng(7)
+    for k, i in enumerate([0, 1, 2, 0]):
+        psi = {s: complex(a) for s, a in psis[i].items()}
+        out = finite.applyOp(n, tops[k % 3], psi, 1e-7, mod.restrictions, t_big)
+        cases.update(encode_psi("memo%d" % k, out, n))
+    big = {b: complex(rng.normal(), rng.normal()) for b in basis}
+    out = finite.applyOp(n, mod.hOp, big, 1e-12, None, None)
+    cases.update(encode_psi("hpsi_in", big, n))
+    cases.update(encode_psi("hpsi_out", out, n))
+    out = finite.applyOp(n, mod.hOp, big, 1e-12, mod.restrictions, None)
+    cases.update(encode_psi("hpsi_restr_out", out, n))
+    np.savez_compressed(os.path.join(HERE, "applyop_config1.npz"), **cases)
+    print("applyop done %.1fs" % (time.time() - t0))
+
+    # ---------------- config2: 50-bath ground state + XAS --------------------------------
+    mod2 = M.make_model("config2")
+    n2 = mod2.n_spin_orbitals
+    with quiet:
+        basis2 = finite.get_basis(*mod2.basis_args())
+        es2, psis2 = finite.eigensystem(n2, mod2.hOp, basis2, 5)
+    cut = 10 * M.K_B * 300
+    keep = [i for i in range(len(es2)) if es2[i] - es2[0] < cut]
+    w2 = np.linspace(-25, 25, 3000)
+    with quiet:
+        gs2 = spectra.getSpectra(n2, mod2.hOp, mod2.xas_ops(), psis2[: len(keep)], es2[: len(keep)], w2, 0.2,
+                                 mod2.restrictions)
+    np.savez_compressed(
+        os.path.join(HERE, "config2.npz"),
+        n_spin_orbitals=n2,
+        es=es2,
+        n_basis=len(basis2),
+        n_keep=len(keep),
+        w=w2,
+        xas_thermal=spectra.thermal_average(es2[: len(keep)], -gs2.imag, T=300),
+        **{k: v for i, p in enumerate(psis2[: len(keep)]) for k, v in encode_psi("eig%d" % i, p, n2).items()},
+    )
+    print("config2 done %.1fs basis=%d keep=%d" % (time.time() - t0, len(basis2), len(keep)))
+
+    # ---------------- upstream's NiO 50-bath inputs ---------------------------------------
+    data = load_nio_data(refenv.REFERENCE_ROOT)
+    hop = data["hOp"].item() if isinstance(data["hOp"], np.ndarray) else data["hOp"]
+    restr = data["restrictions"].item() if isinstance(data["restrictions"], np.ndarray) else data["restrictions"]
+    xas_dat = np.loadtxt(os.path.join(refenv.REFERENCE_ROOT,
+                                      "impurityModel/test/referenceOutput/Ni_NiO_50bath/XAS.dat"))
+    np.savez_compressed(
+        os.path.join(HERE, "nio50.npz"),
+        n_spin_orbitals=int(data["n_spin_orbitals"]),
+        **encode_op("hop", hop),
+        **encode_restrictions("restr", restr),
+        xas_dat=xas_dat,
+        es_log=np.array([-903.8237]),
+    )
+    print("nio done %.1fs" % (time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()
