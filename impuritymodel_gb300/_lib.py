@@ -83,8 +83,12 @@ SIGNATURES = {
     "edgpu_spmv_c64": (_I, [C.POINTER(CSR), _P, _P, _I, _P]),
     "edgpu_lanczos_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_lanczos": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
+    "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),
+    "edgpu_launch_count": (C.c_longlong, []),
     "edgpu_lanczos_reorth_workspace": (_SZ, [_I64, _I]),
     "edgpu_lanczos_reorth": (_I, [C.POINTER(CSR), _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "edgpu_shifted_solve_workspace": (_SZ, [_I64, _I, _I, _I]),
+    "edgpu_shifted_solve": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_combine": (_I, [_P, _I, _I64, _P, _I, _P, _P]),
     "edgpu_cfrac": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P]),
 }

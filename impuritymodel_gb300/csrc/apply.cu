@@ -323,7 +323,7 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
   if (blocks > cap_blocks) blocks = cap_blocks;
   EDGPU_DISPATCH_W(n_words, {
     cudaFuncSetAttribute(apply_columns_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    apply_columns_kernel<W><<<(unsigned)blocks, threads, smem, s>>>(p);
+    apply_columns_kernel<W><<<(unsigned)blocks, threads, smem, s>>>(p); note_launch();
   });
   return check_launch();
 }
@@ -352,6 +352,6 @@ extern "C" int edgpu_apply_vector(int n_words, const uint64_t* states, const dou
   int64_t blocks = (n_states + 7) / 8;
   const int64_t cap_blocks = (int64_t)grid_cap() * 8;
   if (blocks > cap_blocks) blocks = cap_blocks;
-  EDGPU_DISPATCH_W(n_words, { apply_vector_kernel<W><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p); });
+  EDGPU_DISPATCH_W(n_words, { apply_vector_kernel<W><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p); note_launch(); });
   return check_launch();
 }

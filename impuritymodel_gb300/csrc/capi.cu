@@ -1,5 +1,14 @@
 // Version and status strings of the edgpu C ABI.
+#include <atomic>
+
 #include "common.cuh"
+
+namespace edgpu {
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace edgpu
+
+extern "C" long long edgpu_launch_count(void) { return edgpu::g_launches.load(std::memory_order_relaxed); }
 
 extern "C" int edgpu_abi_version(void) { return 1; }
 

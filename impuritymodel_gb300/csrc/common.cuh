@@ -36,6 +36,9 @@ inline int grid_cap() {
   return sms;
 }
 
+// Running count of kernels this library launched (edgpu_launch_count).
+void note_launch();
+
 inline int check_launch() {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDGPU_OK : EDGPU_ERR_CUDA;

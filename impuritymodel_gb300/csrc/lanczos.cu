@@ -8,6 +8,8 @@
 // Vectors of a batch are stored [n][R] (run index fastest) so that the R threads of one
 // row read the row's CSR entries once (broadcast) and gather x[col][0..R) contiguously.
 // All reductions are deterministic: per-block partials in fixed order, summed in fixed order.
+#include <vector>
+
 #include "common.cuh"
 
 namespace edgpu {
@@ -40,7 +42,9 @@ inline RunTile make_tile(int64_t n, int R) {
   if (t.rb < 1) t.rb = 1;
   t.nrt = (R + t.rt - 1) / t.rt;
   int64_t nrb = (n + t.rb - 1) / t.rb;
-  const int64_t cap = (int64_t)grid_cap() * 4;
+  // about 4 blocks per SM in total over the (row block, run tile) grid
+  int64_t cap = ((int64_t)grid_cap() * 4 + t.nrt - 1) / t.nrt;
+  if (cap < 1) cap = 1;
   if (nrb > cap) nrb = cap;
   if (nrb < 1) nrb = 1;
   t.nrb = (int)nrb;
@@ -102,14 +106,20 @@ __global__ void axpy_beta_kernel(int64_t n, int R, typename Cx<T>::V* __restrict
                                  double* __restrict__ alpha_out, int K, int j, double* __restrict__ pbeta) {
   using V = typename Cx<T>::V;
   extern __shared__ double red[];
+  __shared__ double alpha_s[32];
   const int tr = threadIdx.x, ti = threadIdx.y;
   const int r = blockIdx.y * blockDim.x + tr;
-  double acc = 0.0;
-  if (r < R) {
+  if (ti == 0 && r < R) {
     double a = 0.0;
     for (int b = 0; b < nrb; ++b) a += palpha[(int64_t)b * R + r];
+    alpha_s[tr] = a;
+    if (blockIdx.x == 0) alpha_out[(int64_t)r * K + j] = a;
+  }
+  __syncthreads();
+  double acc = 0.0;
+  if (r < R) {
+    const double a = alpha_s[tr];
     const double bp = beta_prev ? beta_prev[(int64_t)r * K + (j - 1)] : 0.0;
-    if (blockIdx.x == 0 && ti == 0) alpha_out[(int64_t)r * K + j] = a;
     const T af = (T)a, bf = (T)bp;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
       V y = Y[i * R + r];
@@ -141,17 +151,23 @@ __global__ void normalize_kernel(int64_t n, int R, const typename Cx<T>::V* __re
                                  double* __restrict__ beta_out, int K, int j, const int32_t* __restrict__ k_max,
                                  int32_t* status) {
   using V = typename Cx<T>::V;
+  __shared__ double beta_s[32];
   const int tr = threadIdx.x, ti = threadIdx.y;
   const int r = blockIdx.y * blockDim.x + tr;
-  if (r >= R) return;
-  double s = 0.0;
-  for (int b = 0; b < nrb; ++b) s += pbeta[(int64_t)b * R + r];
-  const double beta = sqrt(s);
-  const bool active = k_max[r] > j + 1;
-  if (blockIdx.x == 0 && ti == 0) {
-    beta_out[(int64_t)r * K + j] = beta;
-    if (active && !(beta > 0.0)) atomicExch(status, (int32_t)(beta == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+  if (ti == 0 && r < R) {
+    double s = 0.0;
+    for (int b = 0; b < nrb; ++b) s += pbeta[(int64_t)b * R + r];
+    const double bt = sqrt(s);
+    beta_s[tr] = bt;
+    if (blockIdx.x == 0) {
+      beta_out[(int64_t)r * K + j] = bt;
+      if (k_max[r] > j + 1 && !(bt > 0.0))
+        atomicExch(status, (int32_t)(bt == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+    }
   }
+  __syncthreads();
+  if (r >= R) return;
+  const double beta = beta_s[tr];
   const T inv = beta > 0.0 ? (T)(1.0 / beta) : (T)0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
     V w = Wv[i * R + r];
@@ -369,6 +385,10 @@ __global__ void cfrac_kernel(const double* __restrict__ alpha, const double* __r
   g[tid] = kl > 0 ? make_double2(s * gr, s * gi) : make_double2(0.0, 0.0);
 }
 
+bool small_fits(int64_t n, int precision);
+int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                  double* alpha, double* beta, int32_t* status, cudaStream_t s);
+
 inline unsigned grid_1d(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   const int64_t cap = (int64_t)grid_cap() * 8;
@@ -387,21 +407,54 @@ int spmv_impl(const edgpu_csr* h, const typename Cx<T>::V* x, typename Cx<T>::V*
                                                         x, y, nullptr, 0);
     else
       spmm_alpha_kernel<T, false><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_r, R,
-                                                         x, y, nullptr, 0);
+                                                         x, y, nullptr, 0); note_launch();
   } else {
     if (h->val_cf)
       spmm_alpha_kernel<T, true><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_cf, R,
                                                         x, y, nullptr, 0);
     else
       spmm_alpha_kernel<T, false><<<grid, block, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_rf, R,
-                                                         x, y, nullptr, 0);
+                                                         x, y, nullptr, 0); note_launch();
   }
   return check_launch();
 }
 
+// Optional per-kernel timing with CUDA events on the launching stream: kernel_ms[0..2] receive
+// the summed durations of the SpMM, axpy/beta and normalise launches (host array).
+struct KernelTimer {
+  double* out;
+  std::vector<cudaEvent_t> ev[3];
+  cudaStream_t s;
+  KernelTimer(double* o, int K, cudaStream_t st) : out(o), s(st) {
+    if (!out) return;
+    for (int k = 0; k < 3; ++k) {
+      ev[k].resize(2 * (size_t)K);
+      for (auto& e : ev[k]) cudaEventCreate(&e);
+    }
+  }
+  void mark(int kind, int j, int phase) {
+    if (out) cudaEventRecord(ev[kind][2 * (size_t)j + phase], s);
+  }
+  void finish(int K) {
+    if (!out) return;
+    for (int k = 0; k < 3; ++k) {
+      double tot = 0.0;
+      for (int j = 0; j < K; ++j) {
+        if (k == 2 && j == K - 1) continue;
+        float ms = 0.f;
+        cudaEventSynchronize(ev[k][2 * (size_t)j + 1]);
+        if (cudaEventElapsedTime(&ms, ev[k][2 * (size_t)j], ev[k][2 * (size_t)j + 1]) == cudaSuccess) tot += ms;
+      }
+      out[k] = tot;
+    }
+    for (int k = 0; k < 3; ++k)
+      for (auto& e : ev[k]) cudaEventDestroy(e);
+  }
+};
+
 template <typename T>
 int lanczos_impl(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha, double* beta,
-                 int32_t* status, unsigned char* ws, size_t ws_bytes, cudaStream_t s) {
+                 int32_t* status, unsigned char* ws, size_t ws_bytes, cudaStream_t s, double* kernel_ms = nullptr) {
   using V = typename Cx<T>::V;
   const int64_t n = h->n;
   const int64_t nv = n * (int64_t)R;
@@ -423,7 +476,7 @@ int lanczos_impl(const edgpu_csr* h, const double* v0, int R, const int32_t* k_m
                                                        reinterpret_cast<double2*>(A), nv);
   else
     to_c64_kernel<<<grid_1d(nv, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0),
-                                                    reinterpret_cast<float2*>(A), nv);
+                                                    reinterpret_cast<float2*>(A), nv); note_launch();
   int rc = check_launch();
   if (rc) return rc;
   dim3 grid(t.nrb, t.nrt), block(t.rt, t.rb);
@@ -440,19 +493,30 @@ int lanczos_impl(const edgpu_csr* h, const double* v0, int R, const int32_t* k_m
   if (!vals) return EDGPU_ERR_ARG;
   V* Vc = A;
   V* Vp = B;
+  KernelTimer timer(kernel_ms, K, s);
   for (int j = 0; j < K; ++j) {
+    timer.mark(0, j, 0);
     if (valc)
       spmm_alpha_kernel<T, true><<<grid, block, red, s>>>(n, h->row_ptr, h->col, vals, R, Vc, Wb, pa, 1);
     else
-      spmm_alpha_kernel<T, false><<<grid, block, red, s>>>(n, h->row_ptr, h->col, vals, R, Vc, Wb, pa, 1);
+      spmm_alpha_kernel<T, false><<<grid, block, red, s>>>(n, h->row_ptr, h->col, vals, R, Vc, Wb, pa, 1); note_launch();
+    timer.mark(0, j, 1);
+    timer.mark(1, j, 0);
     axpy_beta_kernel<T><<<grid, block, red, s>>>(n, R, Wb, Vc, j > 0 ? Vp : nullptr, pa, t.nrb,
-                                                 j > 0 ? beta : nullptr, alpha, K, j, pb);
-    if (j + 1 < K) normalize_kernel<T><<<grid, block, 0, s>>>(n, R, Wb, Vp, pb, t.nrb, beta, K, j, k_max, status);
+                                                 j > 0 ? beta : nullptr, alpha, K, j, pb); note_launch();
+    timer.mark(1, j, 1);
+    if (j + 1 < K) {
+      timer.mark(2, j, 0);
+      normalize_kernel<T><<<grid, block, 0, s>>>(n, R, Wb, Vp, pb, t.nrb, beta, K, j, k_max, status);
+      note_launch();
+      timer.mark(2, j, 1);
+    }
     if ((rc = check_launch())) return rc;
     V* tmp = Vc;
     Vc = Vp;
     Vp = tmp;
   }
+  timer.finish(K);
   return EDGPU_OK;
 }
 
@@ -492,10 +556,44 @@ extern "C" int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const 
   if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
   if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  if (small_fits(h->n, precision))
+    return lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, (cudaStream_t)stream);
   if (precision == 0)
     return lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes,
                                 (cudaStream_t)stream);
   return lanczos_impl<float>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K,
+                                   int precision, double* alpha, double* beta, int32_t* status_dev, void* workspace,
+                                   size_t workspace_bytes, void* stream, double* kernel_ms) {
+  if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1 || !kernel_ms)
+    return EDGPU_ERR_ARG;
+  if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
+  unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  if (small_fits(h->n, precision)) {
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    int rc = lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    kernel_ms[0] = ms;  // whole fused Krylov loop (SpMV, reductions, axpy) in one launch
+    kernel_ms[1] = 0.0;
+    kernel_ms[2] = 0.0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  if (precision == 0)
+    return lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes,
+                                (cudaStream_t)stream, kernel_ms);
+  return lanczos_impl<float>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes, (cudaStream_t)stream,
+                             kernel_ms);
 }
 
 extern "C" size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap) {
@@ -533,7 +631,10 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
   double2* hc = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1)));
   (void)carve(sizeof(double2) * (size_t)n);
   if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
-  if (j0 == 0) copy_c128_kernel<<<grid_1d(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0), V, n);
+  if (j0 == 0) {
+    copy_c128_kernel<<<grid_1d(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0), V, n);
+    note_launch();
+  }
   int rc = check_launch();
   if (rc) return rc;
   for (int j = j0; j < j1; ++j) {
@@ -545,21 +646,21 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
                                                                                 vj, w, pa, 1);
     else
       spmm_alpha_kernel<double, false><<<grid, block, sizeof(double) * 256, s>>>(n, h->row_ptr, h->col, h->val_r, 1,
-                                                                                 vj, w, pa, 1);
+                                                                                 vj, w, pa, 1); note_launch();
     reorth_alpha_update_kernel<<<nrb, 256, 0, s>>>(n, w, vj, j > 0 ? V + (int64_t)(j - 1) * n : nullptr, pa, nrb,
-                                                   alpha, beta, j, pn);
+                                                   alpha, beta, j, pn); note_launch();
     if ((rc = check_launch())) return rc;
     if (j + 1 >= K_cap) break;
     // two passes of classical Gram-Schmidt against V[0..j]
     const int m = j + 1;
     for (int pass = 0; pass < 2; ++pass) {
       dim3 g2(nrb, (m + kDotTile - 1) / kDotTile);
-      multidot_kernel<<<g2, 256, 0, s>>>(V, m, n, w, pd);
-      sum_partials_kernel<<<(m + 127) / 128, 128, 0, s>>>(pd, m, nrb, hc);
-      subtract_proj_kernel<<<nrb, 256, 0, s>>>(V, m, n, hc, w);
+      multidot_kernel<<<g2, 256, 0, s>>>(V, m, n, w, pd); note_launch();
+      sum_partials_kernel<<<(m + 127) / 128, 128, 0, s>>>(pd, m, nrb, hc); note_launch();
+      subtract_proj_kernel<<<nrb, 256, 0, s>>>(V, m, n, hc, w); note_launch();
     }
-    norm_partial_kernel<<<nrb, 256, 0, s>>>(n, w, pn);
-    reorth_normalize_kernel<<<nrb, 256, 0, s>>>(n, w, V + (int64_t)(j + 1) * n, pn, nrb, beta, j, status_dev);
+    norm_partial_kernel<<<nrb, 256, 0, s>>>(n, w, pn); note_launch();
+    reorth_normalize_kernel<<<nrb, 256, 0, s>>>(n, w, V + (int64_t)(j + 1) * n, pn, nrb, beta, j, status_dev); note_launch();
     if ((rc = check_launch())) return rc;
   }
   return EDGPU_OK;
@@ -570,7 +671,7 @@ extern "C" int edgpu_combine(const double* V, int K, int64_t n, const double* C,
   dim3 grid(grid_1d(n, 256) > 64 ? 64 : grid_1d(n, 256), M);
   combine_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const double2*>(V), K, n,
                                                         reinterpret_cast<const double2*>(C), M,
-                                                        reinterpret_cast<double2*>(X));
+                                                        reinterpret_cast<double2*>(X)); note_launch();
   return check_launch();
 }
 
@@ -582,6 +683,434 @@ extern "C" int edgpu_cfrac(const double* alpha, const double* beta, const int32_
   if (tot == 0) return EDGPU_OK;
   const int threads = 256;
   cfrac_kernel<<<(unsigned)((tot + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
-      alpha, beta, k_len, K, R, omega, n_omega, delta, e, scale, reinterpret_cast<double2*>(g));
+      alpha, beta, k_len, K, R, omega, n_omega, delta, e, scale, reinterpret_cast<double2*>(g)); note_launch();
+  return check_launch();
+}
+
+// =======================================================================================
+// Small sectors: one CTA per run, the whole Krylov loop in one persistent launch.
+// =======================================================================================
+namespace edgpu {
+
+constexpr int kSmallThreads = 512;
+
+// Deterministic block sum (fixed thread -> partial mapping and fixed tree).
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    double t = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+__device__ __forceinline__ double2 to_v(double2 a, double) { return a; }
+__device__ __forceinline__ float2 to_v(double2 a, float) { return make_float2((float)a.x, (float)a.y); }
+
+// Upstream's Lanczos recurrence (finite.py:1974-1992) for run r entirely in shared memory:
+// x = v_j, p = v_{j-1}, y = H v_j then w.  One CTA per run, persistent over runs.
+template <typename T, bool VALC>
+__global__ void __launch_bounds__(kSmallThreads) lanczos_small_kernel(
+    int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const T* __restrict__ vals, int R,
+    const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
+    double* __restrict__ beta, int32_t* status) {
+  using V = typename Cx<T>::V;
+  extern __shared__ __align__(16) unsigned char sm[];
+  V* A = reinterpret_cast<V*>(sm);
+  V* B = A + n;
+  V* Cv = B + n;
+  double* red = reinterpret_cast<double*>(Cv + n);
+  const int tid = threadIdx.x, bs = blockDim.x;
+  for (int r = blockIdx.x; r < R; r += gridDim.x) {
+    const int km = k_max[r];
+    if (km <= 0) continue;
+    for (int64_t i = tid; i < n; i += bs) {
+      A[i] = to_v(v0[i * R + r], T(0));
+      B[i] = to_v(make_double2(0.0, 0.0), T(0));
+    }
+    __syncthreads();
+    V* x = A;
+    V* p = B;
+    V* y = Cv;
+    double bprev = 0.0;
+    for (int j = 0; j < km; ++j) {
+      double acc = 0.0;
+      for (int64_t i = tid; i < n; i += bs) {
+        T yr = 0, yi = 0;
+        const int64_t e1 = rp[i + 1];
+        for (int64_t e = rp[i]; e < e1; ++e) {
+          const V xv = x[col[e]];
+          if (VALC) {
+            const T hr = vals[2 * e], hi = vals[2 * e + 1];
+            yr += hr * xv.x - hi * xv.y;
+            yi += hr * xv.y + hi * xv.x;
+          } else {
+            const T h = vals[e];
+            yr += h * xv.x;
+            yi += h * xv.y;
+          }
+        }
+        V yv;
+        yv.x = yr;
+        yv.y = yi;
+        y[i] = yv;
+        const V xi = x[i];
+        acc += (double)yr * (double)xi.x + (double)yi * (double)xi.y;
+      }
+      const double a = block_sum(acc, red);
+      if (tid == 0) alpha[(int64_t)r * K + j] = a;
+      if (j + 1 == km) break;
+      acc = 0.0;
+      const T af = (T)a, bf = (T)bprev;
+      for (int64_t i = tid; i < n; i += bs) {
+        V w = y[i];
+        const V xi = x[i];
+        const V pi = p[i];
+        w.x = (w.x - af * xi.x) - bf * pi.x;
+        w.y = (w.y - af * xi.y) - bf * pi.y;
+        y[i] = w;
+        acc += (double)w.x * (double)w.x + (double)w.y * (double)w.y;
+      }
+      const double b = sqrt(block_sum(acc, red));
+      if (tid == 0) {
+        beta[(int64_t)r * K + j] = b;
+        if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+      }
+      for (int64_t i = tid; i < n; i += bs) {
+        const V w = y[i];
+        V o;
+        if (sizeof(T) == 8) {
+          o.x = b > 0.0 ? (T)((double)w.x / b) : (T)0;
+          o.y = b > 0.0 ? (T)((double)w.y / b) : (T)0;
+        } else {
+          const T inv = b > 0.0 ? (T)(1.0 / b) : (T)0;
+          o.x = w.x * inv;
+          o.y = w.y * inv;
+        }
+        p[i] = o;  // overwrite v_{j-1} with v_{j+1}
+      }
+      __syncthreads();
+      V* t = p;
+      p = x;
+      x = t;
+      bprev = b;
+    }
+    __syncthreads();
+  }
+}
+
+size_t small_smem_bytes(int64_t n, int precision) {
+  const size_t v = precision ? sizeof(float2) : sizeof(double2);
+  return 3 * v * (size_t)n + 34 * sizeof(double) + 16;
+}
+
+bool small_fits(int64_t n, int precision) { return small_smem_bytes(n, precision) <= 200 * 1024; }
+
+template <typename T, bool VALC>
+int launch_small(const edgpu_csr* h, const T* vals, const double* v0, int R, const int32_t* k_max, int K,
+                 double* alpha, double* beta, int32_t* status, int precision, cudaStream_t s) {
+  const size_t smem = small_smem_bytes(h->n, precision);
+  auto kern = lanczos_small_kernel<T, VALC>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSmallThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  int grid = grid_cap() * per_sm;
+  if (grid > R) grid = R;
+  kern<<<grid, kSmallThreads, smem, s>>>(h->n, h->row_ptr, h->col, vals, R, reinterpret_cast<const double2*>(v0), k_max,
+                                         K, alpha, beta, status);
+  note_launch();
+  return check_launch();
+}
+
+int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                  double* alpha, double* beta, int32_t* status, cudaStream_t s) {
+  if (precision == 0) {
+    if (h->val_c) return launch_small<double, true>(h, h->val_c, v0, R, k_max, K, alpha, beta, status, 0, s);
+    return launch_small<double, false>(h, h->val_r, v0, R, k_max, K, alpha, beta, status, 0, s);
+  }
+  if (h->val_cf) return launch_small<float, true>(h, h->val_cf, v0, R, k_max, K, alpha, beta, status, 1, s);
+  if (!h->val_rf) return EDGPU_ERR_ARG;
+  return launch_small<float, false>(h, h->val_rf, v0, R, k_max, K, alpha, beta, status, 1, s);
+}
+
+// ---------------------------------------------------------------------------------------
+// Shifted solves (z - H) x = y for many z from one Krylov space, CTA per right-hand side.
+// Full reorthogonalisation (two classical Gram-Schmidt passes) in FP64; the Krylov basis
+// lives in global memory V[rhs][k_cap][n] (L2-resident for small sectors).  Thread t < nz
+// tracks shift z_t: LU pivots d_k = (z - a_k) - b_{k-1}^2 / d_{k-1} and the last component
+// q_m of (z - T_m)^{-1} e_1, so the residual estimate b_{m-1} |q_m| costs O(1) per step.
+// Replaces upstream's per-energy BiCGSTAB (spectra.py:962,1080).
+// ---------------------------------------------------------------------------------------
+template <bool VALC>
+__global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
+    int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const double* __restrict__ vals,
+    int n_rhs, const double2* __restrict__ Y, const double2* __restrict__ zs, int nz, int k_cap, double tol,
+    double2* __restrict__ V, double* __restrict__ alpha, double* __restrict__ beta, int32_t* __restrict__ m_out,
+    double* __restrict__ ynorm_out, int32_t* status) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  double2* w = reinterpret_cast<double2*>(sm);
+  double2* hc = w + n;  // k_cap reorthogonalisation coefficients
+  double* red = reinterpret_cast<double*>(hc + k_cap);
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = bs >> 5;
+  for (int r = blockIdx.x; r < n_rhs; r += gridDim.x) {
+    double2* Vr = V + (size_t)r * k_cap * n;
+    const double2* y = Y + (size_t)r * n;
+    double acc = 0.0;
+    for (int64_t i = tid; i < n; i += bs) acc += y[i].x * y[i].x + y[i].y * y[i].y;
+    const double yn = sqrt(block_sum(acc, red));
+    if (tid == 0) ynorm_out[r] = yn;
+    if (!(yn > 0.0)) {
+      if (tid == 0) m_out[r] = 0;
+      continue;
+    }
+    for (int64_t i = tid; i < n; i += bs) Vr[i] = make_double2(y[i].x / yn, y[i].y / yn);
+    __syncthreads();
+    double2 z = make_double2(0.0, 0.0), d = make_double2(1.0, 0.0), q = make_double2(1.0, 0.0);
+    if (tid < nz) z = zs[(size_t)r * nz + tid];
+    double bprev = 0.0;
+    int m = k_cap;
+    for (int j = 0; j < k_cap; ++j) {
+      const double2* vj = Vr + (size_t)j * n;
+      acc = 0.0;
+      for (int64_t i = tid; i < n; i += bs) {
+        double yr = 0.0, yi = 0.0;
+        const int64_t e1 = rp[i + 1];
+        for (int64_t e = rp[i]; e < e1; ++e) {
+          const double2 xv = vj[col[e]];
+          if (VALC) {
+            const double hr = vals[2 * e], hi = vals[2 * e + 1];
+            yr += hr * xv.x - hi * xv.y;
+            yi += hr * xv.y + hi * xv.x;
+          } else {
+            const double h = vals[e];
+            yr += h * xv.x;
+            yi += h * xv.y;
+          }
+        }
+        w[i] = make_double2(yr, yi);
+        acc += yr * vj[i].x + yi * vj[i].y;
+      }
+      const double a = block_sum(acc, red);
+      if (tid == 0) alpha[(size_t)r * k_cap + j] = a;
+      for (int64_t i = tid; i < n; i += bs) {
+        double2 t = w[i];
+        const double2 c = vj[i];
+        t.x -= a * c.x;
+        t.y -= a * c.y;
+        if (j > 0) {
+          const double2 pv = Vr[(size_t)(j - 1) * n + i];
+          t.x -= bprev * pv.x;
+          t.y -= bprev * pv.y;
+        }
+        w[i] = t;
+      }
+      __syncthreads();
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int k = warp; k <= j; k += nwarps) {
+          const double2* vk = Vr + (size_t)k * n;
+          double hr = 0.0, hi = 0.0;
+          for (int64_t i = lane; i < n; i += 32) {
+            const double2 v = vk[i], x = w[i];
+            hr += v.x * x.x + v.y * x.y;
+            hi += v.x * x.y - v.y * x.x;
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            hr += __shfl_down_sync(0xffffffffu, hr, o);
+            hi += __shfl_down_sync(0xffffffffu, hi, o);
+          }
+          if (lane == 0) hc[k] = make_double2(hr, hi);
+        }
+        __syncthreads();
+        for (int64_t i = tid; i < n; i += bs) {
+          double2 x = w[i];
+          for (int k = 0; k <= j; ++k) {
+            const double2 c = hc[k];
+            const double2 v = Vr[(size_t)k * n + i];
+            x.x -= c.x * v.x - c.y * v.y;
+            x.y -= c.x * v.y + c.y * v.x;
+          }
+          w[i] = x;
+        }
+        __syncthreads();
+      }
+      acc = 0.0;
+      for (int64_t i = tid; i < n; i += bs) acc += w[i].x * w[i].x + w[i].y * w[i].y;
+      const double b = sqrt(block_sum(acc, red));
+      if (tid == 0) beta[(size_t)r * k_cap + j] = b;
+      // shift-wise LU pivot and residual estimate for T_{j+1}
+      bool ok = true;
+      if (tid < nz) {
+        double2 dn = make_double2(z.x - a, z.y);
+        if (j > 0) {
+          const double b2 = bprev * bprev;
+          const double den = d.x * d.x + d.y * d.y;
+          dn.x -= b2 * d.x / den;
+          dn.y += b2 * d.y / den;
+        }
+        // q_{j+1} = q_j * (j > 0 ? bprev : 1) / dn
+        const double2 qn = make_double2(j > 0 ? q.x * bprev : 1.0, j > 0 ? q.y * bprev : 0.0);
+        const double den = dn.x * dn.x + dn.y * dn.y;
+        q = make_double2((qn.x * dn.x + qn.y * dn.y) / den, (qn.y * dn.x - qn.x * dn.y) / den);
+        d = dn;
+        ok = b * sqrt(q.x * q.x + q.y * q.y) <= tol;
+      }
+      const bool done = __syncthreads_and(ok) || !(b > 0.0) || j + 1 == k_cap;
+      if (done) {
+        m = j + 1;
+        if (!(b >= 0.0) && tid == 0) atomicExch(status, (int32_t)EDGPU_ERR_NAN);
+        break;
+      }
+      for (int64_t i = tid; i < n; i += bs) Vr[(size_t)(j + 1) * n + i] = make_double2(w[i].x / b, w[i].y / b);
+      __syncthreads();
+      bprev = b;
+    }
+    if (tid == 0) m_out[r] = m;
+    __syncthreads();
+  }
+}
+
+// coef[r][z][k] = ynorm_r * ((z - T_m)^{-1} e_1)_k by the Thomas algorithm; thread per (r, z).
+// (z - T) has diagonal z - a_k and off-diagonals -b_k.  scratch holds the forward-sweep ratios.
+__global__ void shifted_coef_kernel(const double* alpha, const double* beta, const int32_t* m_arr,
+                                    const double* ynorm, const double2* zs, int n_rhs, int nz, int k_cap,
+                                    double2* coef, double2* scratch) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_rhs * nz) return;
+  const int r = t / nz;
+  const int m = m_arr[r];
+  double2* x = coef + (size_t)t * k_cap;
+  double2* cp = scratch + (size_t)t * k_cap;
+  if (m <= 0) {
+    for (int k = 0; k < k_cap; ++k) x[k] = make_double2(0.0, 0.0);
+    return;
+  }
+  const double2 z = zs[t];
+  const double* a = alpha + (size_t)r * k_cap;
+  const double* b = beta + (size_t)r * k_cap;
+  double2 cprev = make_double2(0.0, 0.0), dprev = make_double2(0.0, 0.0);
+  for (int k = 0; k < m; ++k) {
+    double2 den = make_double2(z.x - a[k], z.y);
+    double2 rk = make_double2(1.0, 0.0);
+    if (k > 0) {
+      den.x += b[k - 1] * cprev.x;
+      den.y += b[k - 1] * cprev.y;
+      rk = make_double2(b[k - 1] * dprev.x, b[k - 1] * dprev.y);
+    }
+    const double dd = den.x * den.x + den.y * den.y;
+    const double2 inv = make_double2(den.x / dd, -den.y / dd);
+    const double bk = (k + 1 < m) ? b[k] : 0.0;
+    cprev = make_double2(-bk * inv.x, -bk * inv.y);
+    dprev = make_double2(rk.x * inv.x - rk.y * inv.y, rk.x * inv.y + rk.y * inv.x);
+    cp[k] = cprev;
+    x[k] = dprev;
+  }
+  for (int k = m - 2; k >= 0; --k) {
+    const double2 c = cp[k], xn = x[k + 1];
+    x[k] = make_double2(x[k].x - (c.x * xn.x - c.y * xn.y), x[k].y - (c.x * xn.y + c.y * xn.x));
+  }
+  const double yn = ynorm[r];
+  for (int k = 0; k < m; ++k) x[k] = make_double2(yn * x[k].x, yn * x[k].y);
+  for (int k = m; k < k_cap; ++k) x[k] = make_double2(0.0, 0.0);
+}
+
+// X[r][z][i] = sum_k coef[r][z][k] V[r][k][i]
+__global__ void combine_batched_kernel(const double2* __restrict__ V, const double2* __restrict__ coef,
+                                       const int32_t* __restrict__ m_arr, int64_t n, int nz, int k_cap,
+                                       double2* __restrict__ X) {
+  const int r = blockIdx.z;
+  const int zi = blockIdx.y;
+  const int m = m_arr[r];
+  const double2* c = coef + ((size_t)r * nz + zi) * k_cap;
+  const double2* Vr = V + (size_t)r * k_cap * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double xr = 0.0, xi = 0.0;
+    for (int k = 0; k < m; ++k) {
+      const double2 ck = c[k];
+      const double2 v = Vr[(size_t)k * n + i];
+      xr += ck.x * v.x - ck.y * v.y;
+      xi += ck.x * v.y + ck.y * v.x;
+    }
+    X[((size_t)r * nz + zi) * n + i] = make_double2(xr, xi);
+  }
+}
+
+}  // namespace edgpu
+
+extern "C" size_t edgpu_shifted_solve_workspace(int64_t n, int n_rhs, int nz, int k_cap) {
+  size_t b = 0;
+  b += sizeof(double2) * (size_t)n_rhs * k_cap * n + 256;       // V
+  b += 2 * sizeof(double) * (size_t)n_rhs * k_cap + 512;        // alpha, beta
+  b += sizeof(int32_t) * (size_t)n_rhs + sizeof(double) * n_rhs + 512;
+  b += 2 * sizeof(double2) * (size_t)n_rhs * nz * k_cap + 256;  // coefficients + forward-sweep scratch
+  return b + 1024;
+}
+
+extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
+                                   double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  if (!h || !Y || !zs || !X || !m_out || !status_dev || n_rhs < 1 || nz < 1 || k_cap < 1 || h->n < 1)
+    return EDGPU_ERR_ARG;
+  if (nz > kSmallThreads) return EDGPU_ERR_ARG;
+  if (workspace_bytes < edgpu_shifted_solve_workspace(h->n, n_rhs, nz, k_cap)) return EDGPU_ERR_WORKSPACE;
+  const int64_t n = h->n;
+  const size_t smem = sizeof(double2) * (size_t)n + sizeof(double2) * (size_t)k_cap + 34 * sizeof(double) + 16;
+  if (smem > 200 * 1024) return EDGPU_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    unsigned char* p = ws + off;
+    off += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  double2* V = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)n_rhs * k_cap * n));
+  double* alpha = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs * k_cap));
+  double* beta = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs * k_cap));
+  double* yn = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs));
+  double* coef = reinterpret_cast<double*>(carve(2 * sizeof(double2) * (size_t)n_rhs * nz * k_cap));
+  if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
+  const double2* Yc = reinterpret_cast<const double2*>(Y);
+  const double2* zc = reinterpret_cast<const double2*>(zs);
+  int per_sm = 0;
+  if (h->val_c) {
+    cudaFuncSetAttribute(shifted_small_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shifted_small_kernel<true>, kSmallThreads, smem);
+  } else {
+    cudaFuncSetAttribute(shifted_small_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shifted_small_kernel<false>, kSmallThreads, smem);
+  }
+  if (per_sm < 1) per_sm = 1;
+  int grid = grid_cap() * per_sm;
+  if (grid > n_rhs) grid = n_rhs;
+  if (h->val_c)
+    shifted_small_kernel<true><<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, h->val_c, n_rhs, Yc, zc, nz,
+                                                                 k_cap, tol, V, alpha, beta, m_out, yn, status_dev);
+  else
+    shifted_small_kernel<false><<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, h->val_r, n_rhs, Yc, zc, nz,
+                                                                  k_cap, tol, V, alpha, beta, m_out, yn, status_dev);
+  note_launch();
+  int rc = check_launch();
+  if (rc) return rc;
+  const int tot = n_rhs * nz;
+  shifted_coef_kernel<<<(tot + 127) / 128, 128, 0, s>>>(alpha, beta, m_out, yn, zc, n_rhs, nz, k_cap,
+                                                        reinterpret_cast<double2*>(coef),
+                                                        reinterpret_cast<double2*>(coef) + (size_t)tot * k_cap);
+  note_launch();
+  dim3 g3((unsigned)((n + 255) / 256 > 16 ? 16 : (n + 255) / 256), nz, n_rhs);
+  combine_batched_kernel<<<g3, 256, 0, s>>>(V, reinterpret_cast<const double2*>(coef), m_out, n, nz, k_cap,
+                                            reinterpret_cast<double2*>(X));
+  note_launch();
   return check_launch();
 }

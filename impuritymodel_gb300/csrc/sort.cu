@@ -85,20 +85,20 @@ static size_t scan_ws_elems(int64_t n) {
 static int scan_rec(const int64_t* in, int64_t* out, int64_t n, int64_t* ws, cudaStream_t s) {
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb <= 1) {
-    scan_down_kernel<<<1, kScanThreads, 0, s>>>(in, n, nullptr, out);
+    scan_down_kernel<<<1, kScanThreads, 0, s>>>(in, n, nullptr, out); note_launch();
     return check_launch();
   }
   int64_t* partial = ws;
   int64_t* partial_scan = ws + nb + 1;
   (void)partial_scan;
-  scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial);
+  scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial); note_launch();
   // Scan partial sums in place into a temp region after them: reuse a second level.
   int64_t* next_ws = ws + nb + 1;
   // The scan output of the partials needs nb + 1 entries; put it into `partial` itself via
   // a recursive call writing to the level's output buffer located in next level's space.
   int rc = scan_rec(partial, partial, nb, next_ws, s);
   if (rc) return rc;
-  scan_down_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial, out);
+  scan_down_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partial, out); note_launch();
   return check_launch();
 }
 
@@ -322,7 +322,7 @@ extern "C" int edgpu_vary_mask(int n_words, const uint64_t* keys, int64_t n, uin
   cudaMemsetAsync(vary_out, 0, sizeof(uint64_t) * n_words, s);
   if (n == 0) return check_launch();
   EDGPU_DISPATCH_W(n_words, {
-    vary_kernel<W><<<grid_for(n, 256), 256, 0, s>>>(keys, n, reinterpret_cast<unsigned long long*>(vary_out));
+    vary_kernel<W><<<grid_for(n, 256), 256, 0, s>>>(keys, n, reinterpret_cast<unsigned long long*>(vary_out)); note_launch();
   });
   return check_launch();
 }
@@ -360,12 +360,12 @@ extern "C" int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload,
       const int shift = 8 * byte;
       if (vary_mask && ((vary_mask[q] >> shift) & 0xFFull) == 0) continue;
       EDGPU_DISPATCH_W(n_words, {
-        radix_hist_kernel<W><<<(unsigned)nb, kSortThreads, 0, s>>>(kin, n, q, shift, hist, nb);
+        radix_hist_kernel<W><<<(unsigned)nb, kSortThreads, 0, s>>>(kin, n, q, shift, hist, nb); note_launch();
       });
       if ((rc = check_launch())) return rc;
       if ((rc = edgpu_scan_i64(hist, offs, hist_n, scan_ws, scan_bytes, stream))) return rc;
       EDGPU_DISPATCH_W(n_words, {
-        radix_scatter_kernel<W><<<(unsigned)nb, kSortThreads, 0, s>>>(kin, pin, kout, pout, n, q, shift, offs, nb);
+        radix_scatter_kernel<W><<<(unsigned)nb, kSortThreads, 0, s>>>(kin, pin, kout, pout, n, q, shift, offs, nb); note_launch();
       });
       if ((rc = check_launch())) return rc;
       uint64_t* tk = kin;
@@ -377,7 +377,7 @@ extern "C" int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload,
     }
   }
   if (kin != keys) {
-    EDGPU_DISPATCH_W(n_words, { copy_states_kernel<W><<<grid_for(n, 256), 256, 0, s>>>(kin, pin, keys, payload, n); });
+    EDGPU_DISPATCH_W(n_words, { copy_states_kernel<W><<<grid_for(n, 256), 256, 0, s>>>(kin, pin, keys, payload, n); note_launch(); });
     rc = check_launch();
   }
   return rc;
@@ -386,7 +386,7 @@ extern "C" int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload,
 extern "C" int edgpu_segment_heads(int n_words, const uint64_t* keys, int64_t n, int64_t* head, void* stream) {
   if (n < 0 || (n > 0 && (!keys || !head))) return EDGPU_ERR_ARG;
   if (n == 0) return EDGPU_OK;
-  EDGPU_DISPATCH_W(n_words, { heads_kernel<W><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(keys, n, head); });
+  EDGPU_DISPATCH_W(n_words, { heads_kernel<W><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(keys, n, head); note_launch(); });
   return check_launch();
 }
 
@@ -398,7 +398,7 @@ extern "C" int edgpu_segment_reduce(int n_words, const uint64_t* keys, const uin
   EDGPU_DISPATCH_W(n_words, {
     segment_reduce_kernel<W><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
         keys, payload, n, head_scan, reinterpret_cast<const double2*>(vals), out_keys, out_first,
-        reinterpret_cast<double2*>(out_vals));
+        reinterpret_cast<double2*>(out_vals)); note_launch();
   });
   return check_launch();
 }
@@ -408,7 +408,7 @@ extern "C" int edgpu_merge_states(int n_words, const uint64_t* a, int64_t na, co
   if (na < 0 || nb < 0 || !out) return EDGPU_ERR_ARG;
   if (na + nb == 0) return EDGPU_OK;
   EDGPU_DISPATCH_W(n_words, {
-    merge_kernel<W><<<grid_for(na + nb, 256), 256, 0, (cudaStream_t)stream>>>(a, na, b, nb, out);
+    merge_kernel<W><<<grid_for(na + nb, 256), 256, 0, (cudaStream_t)stream>>>(a, na, b, nb, out); note_launch();
   });
   return check_launch();
 }
@@ -418,7 +418,7 @@ extern "C" int edgpu_lookup_states(int n_words, const uint64_t* basis, int64_t n
   if (nq < 0 || n_basis < 0 || (nq > 0 && (!query || !out_index))) return EDGPU_ERR_ARG;
   if (nq == 0) return EDGPU_OK;
   EDGPU_DISPATCH_W(n_words, {
-    lookup_kernel<W><<<grid_for(nq, 256), 256, 0, (cudaStream_t)stream>>>(basis, n_basis, query, nq, out_index);
+    lookup_kernel<W><<<grid_for(nq, 256), 256, 0, (cudaStream_t)stream>>>(basis, n_basis, query, nq, out_index); note_launch();
   });
   return check_launch();
 }

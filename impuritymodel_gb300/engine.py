@@ -59,6 +59,7 @@ class DeviceOp:
         self.n_terms = t
         self.max_orbital = max_orb
         self.is_real = bool(np.all(coeff[:, 1] == 0.0))
+        self.nbytes = ops.nbytes + coeff.nbytes + flags.nbytes
         self.ops = torch.from_numpy(ops.view(np.int64)).to(device)
         self.coeff = torch.from_numpy(coeff).to(device)
         self.flags = torch.from_numpy(flags.view(np.int32)).to(device)
@@ -98,19 +99,37 @@ class CsrMatrix:
         self.val_r = val_r
         self.val_cf = None
         self.val_rf = None
+        self.mixed_shift = 0.0
         self.n = row_ptr.numel() - 1
         self.ncols = self.n if ncols is None else int(ncols)
         self.nnz = col.numel()
         self._struct = None
 
     def mixed(self):
-        """Add the complex64/float32 value copy used by the mixed-precision form."""
-        if self.val_r is not None and self.val_rf is None:
-            self.val_rf = self.val_r.to(torch.float32)
-            self._struct = None
-        if self.val_c is not None and self.val_cf is None:
-            self.val_cf = self.val_c.to(torch.float32)
-            self._struct = None
+        """Add the float32 / complex64 copy of H - shift*I used by the mixed-precision form.
+
+        The shift is the mean diagonal element: with diagonals near -800 eV a float32 copy
+        of H itself would carry ~5e-5 eV absolute rounding; H - shift keeps the float32
+        entries small.  Callers add ``mixed_shift`` back to the Lanczos alphas.
+        """
+        if self.val_rf is not None or self.val_cf is not None:
+            return self
+        rows = torch.repeat_interleave(torch.arange(self.n, device=self.row_ptr.device),
+                                       self.row_ptr[1:] - self.row_ptr[:-1])
+        diag = rows == self.col.to(torch.int64)
+        if self.val_r is not None:
+            d = self.val_r[diag]
+            self.mixed_shift = float(d.mean().item()) if d.numel() else 0.0
+            v = self.val_r.clone()
+            v[diag] -= self.mixed_shift
+            self.val_rf = v.to(torch.float32)
+        else:
+            d = self.val_c[diag, 0]
+            self.mixed_shift = float(d.mean().item()) if d.numel() else 0.0
+            v = self.val_c.clone()
+            v[diag, 0] -= self.mixed_shift
+            self.val_cf = v.to(torch.float32)
+        self._struct = None
         return self
 
     def struct(self):
@@ -144,6 +163,9 @@ class Engine:
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._ws = torch.empty(1 << 20, dtype=torch.uint8, device=self.device)
         self.scratch_entries = 256
+        # bytes moved across the host<->device boundary by the drop-in API (inputs/results)
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
 
     # -- plumbing -------------------------------------------------------------------------
     @property
@@ -166,11 +188,23 @@ class Engine:
 
     def upload_states(self, words):
         words = np.ascontiguousarray(words, dtype=np.uint64)
+        self.h2d_bytes += words.nbytes
         return torch.from_numpy(words.view(np.int64)).to(self.device)
 
-    @staticmethod
-    def download_states(t):
+    def download_states(self, t):
+        self.d2h_bytes += t.numel() * t.element_size()
         return t.cpu().numpy().view(np.uint64)
+
+    def to_device(self, arr):
+        """Host NumPy array -> device tensor (counted as API input traffic)."""
+        arr = np.ascontiguousarray(arr)
+        self.h2d_bytes += arr.nbytes
+        return torch.from_numpy(arr).to(self.device)
+
+    def to_host(self, t):
+        """Device tensor -> host NumPy array (counted as API result traffic)."""
+        self.d2h_bytes += t.numel() * t.element_size()
+        return t.cpu().numpy()
 
     # -- primitives -----------------------------------------------------------------------
     def scan(self, counts):
@@ -412,7 +446,7 @@ class Engine:
         return dims
 
     # -- Krylov ---------------------------------------------------------------------------
-    def lanczos(self, csr, v0, k_max, precision=0):
+    def lanczos(self, csr, v0, k_max, precision=0, timing=None):
         """Batched Lanczos on R start vectors v0 [N, R] complex128 (normalised)."""
         n, r = v0.shape
         if n != csr.n or csr.ncols != csr.n:
@@ -426,9 +460,22 @@ class Engine:
         v0r = torch.view_as_real(v0.contiguous()) if v0.is_complex() else v0
         ws, wsn = self.workspace(self.lib.edgpu_lanczos_workspace(n, r, K, precision))
         self.reset_status()
-        L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision, _ptr(alpha),
-                                       _ptr(beta), _ptr(self.status), ws, wsn, self.stream), "lanczos")
+        if timing is None:
+            L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
+                                           _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
+                    "lanczos")
+        else:
+            ms = (C.c_double * 3)()
+            L.check(self.lib.edgpu_lanczos_timed(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
+                                                 _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream,
+                                                 ms), "lanczos_timed")
+            vb = 8 if precision else 16
+            sb = (4 if precision else 8) * (2 if csr.val_c is not None else 1)
+            timing.append(dict(n=csr.n, nnz=csr.nnz, R=r, K=K, precision=precision, spmm_ms=ms[0], axpy_ms=ms[1],
+                               normalize_ms=ms[2], spmm_launches=K, vec_bytes=vb, val_bytes=sb))
         self.read_status("lanczos")
+        if precision and csr.mixed_shift:
+            alpha += csr.mixed_shift  # Lanczos ran on H - shift*I
         return alpha, beta
 
     def spmv(self, csr, x, precision=0):
@@ -443,6 +490,8 @@ class Engine:
             y = torch.empty((n, r), dtype=torch.complex64, device=self.device)
             L.check(self.lib.edgpu_spmv_c64(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r,
                                             self.stream), "spmv_c64")
+            if csr.mixed_shift:
+                y += csr.mixed_shift * x.to(torch.complex64)  # float32 copy holds H - shift*I
             return y
         xr = torch.view_as_real(x.contiguous())
         y = torch.empty((n, r), dtype=torch.complex128, device=self.device)
@@ -499,6 +548,28 @@ class Engine:
             if stop is not None and stop(alpha[:j].cpu().numpy(), beta[:j].cpu().numpy(), j):
                 break
         return V[:j], alpha[:j].cpu().numpy(), beta[:j].cpu().numpy()
+
+    def shifted_solve(self, csr, Y, zs, tol, k_cap):
+        """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).
+
+        Returns (X [R, nz, N] complex128, krylov sizes [R]) or None when the sector or the
+        shift count exceeds the single-CTA kernel's limits."""
+        r, n = Y.shape
+        nz = zs.shape[1]
+        k_cap = int(min(k_cap, n))
+        if nz > 512 or 16 * n + 16 * k_cap + 300 > 200 * 1024:
+            return None
+        zt = torch.as_tensor(np.ascontiguousarray(zs, dtype=np.complex128)).to(self.device)
+        X = torch.empty((r, nz, n), dtype=torch.complex128, device=self.device)
+        m = torch.empty(r, dtype=torch.int32, device=self.device)
+        ws, wsn = self.workspace(self.lib.edgpu_shifted_solve_workspace(n, r, nz, k_cap))
+        self.reset_status()
+        L.check(self.lib.edgpu_shifted_solve(C.byref(csr.struct()), _ptr(torch.view_as_real(Y.contiguous())), r,
+                                             _ptr(torch.view_as_real(zt)), nz, k_cap, float(tol),
+                                             _ptr(torch.view_as_real(X)), _ptr(m), _ptr(self.status), ws, wsn,
+                                             self.stream), "shifted_solve")
+        self.read_status("shifted_solve")
+        return X, m
 
     def combine(self, V, coeffs):
         """X[m] = sum_k coeffs[k, m] V[k] (complex128)."""

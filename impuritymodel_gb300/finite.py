@@ -78,6 +78,7 @@ def _device_op(op, eng):
     if hit is not None and hit[0] is op:
         return hit[1]
     d = DeviceOp(op, eng.device)
+    eng.h2d_bytes += d.nbytes
     if len(_OP_CACHE) > 64:
         _OP_CACHE.clear()
     _OP_CACHE[key] = (op, d)
@@ -113,9 +114,9 @@ def applyOp(n_spin_orbitals, op, psi, slaterWeightMin=1e-12, restrictions=None, 
     if opResult is None:
         words, amps = codec.psi_to_arrays(psi, n)
         s_t = eng.upload_states(words)
-        a_t = torch.from_numpy(amps).to(eng.device)
+        a_t = eng.to_device(amps)
         (out_s, out_a), = eng.apply_vectors([s_t], [a_t], dop, restr, slaterWeightMin)
-        return codec.arrays_to_psi(eng.download_states(out_s), out_a.cpu().numpy(), n)
+        return codec.arrays_to_psi(eng.download_states(out_s), eng.to_host(out_a), n)
     # memo path: compute per-state results for unseen states, then combine
     states = list(psi.keys())
     fresh = [s for s in states if s not in opResult]
@@ -241,9 +242,10 @@ def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
 class _SortedBasis:
     """A basis given in caller order, held sorted on the device with the permutation."""
 
-    def __init__(self, eng, basis, n):
-        self.words = codec.bytes_to_words(basis, n)
+    def __init__(self, eng, basis, n, words=None):
+        self.words = codec.bytes_to_words(basis, n) if words is None else words
         given = eng.upload_states(self.words)
+        self.given = given
         keys = given.clone()
         payload = torch.arange(keys.shape[0], dtype=torch.int32, device=eng.device)
         eng.sort_states(keys, payload)
@@ -515,6 +517,26 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
     return th[:kw], X
 
 
+def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7):
+    """Device form of :func:`eigensystem` on a :class:`_SortedBasis`.
+
+    Returns (energies [k] host array, list of (states [m, W], amps [m, 2]) device tensors in
+    caller basis order keeping ``|amp|^2 >= slaterWeightMin``).
+    """
+    csr = _device_hamiltonian(eng, dop, sb)
+    es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3))
+    vec_given = torch.empty_like(X)
+    vec_given[:, sb.perm] = X
+    psis = []
+    for vi in range(len(es)):
+        v = vec_given[vi]
+        keep = (v.real ** 2 + v.imag ** 2) >= slaterWeightMin
+        idx = torch.nonzero(keep).flatten()
+        amps = torch.view_as_real(v[idx]).contiguous()
+        psis.append((sb.given[idx].contiguous(), amps))
+    return np.asarray(es), psis
+
+
 def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", eigenValueTol=1e-9,
                 slaterWeightMin=1e-7):
     """Lowest eigenpairs and eigenstates as dicts (upstream finite.py:58-118).
@@ -540,7 +562,7 @@ def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", 
         vec_sorted = X.t().contiguous()
         vecs_t = torch.empty_like(vec_sorted)
         vecs_t[sb.perm] = vec_sorted
-        vecs = vecs_t.cpu().numpy()
+        vecs = eng.to_host(vecs_t)
     else:
         raise ValueError("Wrong diagonalization mode")
     psis = [

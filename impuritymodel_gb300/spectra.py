@@ -98,63 +98,73 @@ class Sector:
 
 
 def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
-                sector=None, return_coeffs=False, normalize=True, scales=None):
+                sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None):
     """Continued-fraction Green's functions of many start states on one sector.
 
-    ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states.  With
-    ``normalize=True`` each is normalised before the Lanczos and the result scaled by its
-    squared norm (upstream ``normalization**2 * getGreen(psi / normalization)``,
-    spectra.py:786-802).  With ``normalize=False`` the Lanczos starts from the amplitudes
-    as given (upstream getGreen on an arbitrary psi) and the result is scaled by
-    ``scales[r]`` (default 1).  Returns g [R, n_omega] complex128 (device).
+    ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states (lists), or
+    ``run_states`` is a packed ``(states [M, W], amps [M, 2], run_of_row [M], n_runs)``
+    tuple with ``run_amps`` None.  With ``normalize=True`` each start state is normalised
+    before the Lanczos and the result scaled by its squared norm (upstream
+    ``normalization**2 * getGreen(psi / normalization)``, spectra.py:786-802).  With
+    ``normalize=False`` the Lanczos starts from the amplitudes as given (upstream getGreen
+    on an arbitrary psi) and the result is scaled by ``scales[r]`` (default 1).
+    Returns g [R, n_omega] complex128 (device).
     """
-    runs = len(run_states)
     omega = np.asarray(omega, dtype=np.float64)
-    if runs == 0:
-        return torch.zeros((0, len(omega)), dtype=torch.complex128, device=eng.device)
-    sizes = torch.tensor([int(s.shape[0]) for s in run_states], device=eng.device)
-    states = torch.cat(run_states, 0)
-    amps = torch.cat(run_amps, 0)
-    run_of_row = torch.repeat_interleave(torch.arange(runs, device=eng.device), sizes)
+    if run_amps is None:
+        states, amps, run_of_row, runs = run_states
+    else:
+        runs = len(run_states)
+        if runs == 0:
+            return torch.zeros((0, len(omega)), dtype=torch.complex128, device=eng.device)
+        sizes = torch.tensor([int(x.shape[0]) for x in run_states], device=eng.device)
+        states = torch.cat(run_states, 0)
+        amps = torch.cat(run_amps, 0)
+        run_of_row = torch.repeat_interleave(torch.arange(runs, device=eng.device), sizes)
     n2 = torch.zeros(runs, dtype=torch.float64, device=eng.device)
     if amps.shape[0]:
         n2.index_add_(0, run_of_row, amps[:, 0] ** 2 + amps[:, 1] ** 2)
     n2_h = n2.cpu().numpy()
     g = torch.zeros((runs, len(omega)), dtype=torch.complex128, device=eng.device)
-    live = [r for r in range(runs) if n2_h[r] > 0]
-    if not live:
+    live = np.nonzero(n2_h > 0)[0]
+    if live.size == 0:
         return (g, None) if return_coeffs else g
     if sector is None:
         sector = Sector(eng, dop, restr, states[n2[run_of_row] > 0], precision)
     rows = eng.lookup(sector.basis, states)
     if bool((rows < 0).any()):
         raise RuntimeError("start state outside the sector basis")
-    v0 = torch.zeros((sector.n, runs), dtype=torch.complex128, device=eng.device)
+    # live runs renumbered 0..L-1
+    remap = torch.full((runs,), -1, dtype=torch.int64, device=eng.device)
+    live_t = torch.from_numpy(live).to(eng.device)
+    remap[live_t] = torch.arange(live.size, device=eng.device)
+    lr = remap[run_of_row]
+    sel = lr >= 0
     vals = torch.complex(amps[:, 0], amps[:, 1])
     if normalize:
         norm = torch.sqrt(n2)
-        vals = vals / torch.where(norm > 0, norm, 1.0)[run_of_row]
+        vals = vals / torch.where(norm > 0, norm, torch.ones_like(norm))[run_of_row]
         scale_h = n2_h
     else:
         scale_h = np.ones(runs) if scales is None else np.asarray(scales, dtype=np.float64)
-    v0.index_put_((rows, run_of_row), vals, accumulate=True)
-    dims = sector.run_dims(eng, rows, run_of_row, runs)
-    k = torch.clamp(dims, max=int(krylovSize))
-    k = torch.where(n2 > 0, k, torch.zeros_like(k))
-    k_h = k.cpu().numpy().astype(np.int32)
-    live_idx = torch.tensor(live, device=eng.device)
-    alpha, beta = eng.lanczos(sector.csr, v0[:, live_idx].contiguous(), k_h[live], precision=precision)
+    v0 = torch.zeros((sector.n, live.size), dtype=torch.complex128, device=eng.device)
+    v0.index_put_((rows[sel], lr[sel]), vals[sel], accumulate=True)
+    dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
+    k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
+    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision, timing=timing)
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
-    gl = eng.cfrac(alpha, beta, k_h[live], omega, delta, e_live, scale_h[live])
-    g[live_idx] = gl
+    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live])
+    if capture is not None:
+        capture.append(dict(csr=sector.csr, v0=v0, k=k_h, e=e_live, scale=scale_h[live], live=live, g=g,
+                            omega=omega, delta=delta))
     if return_coeffs:
-        return g, (alpha, beta, k_h[live], live)
+        return g, (alpha, beta, k_h, live)
     return g
 
 
 def _psi_tensors(eng, psi, n):
     words, amps = codec.psi_to_arrays(psi, n)
-    return eng.upload_states(words), torch.from_numpy(amps).to(eng.device)
+    return eng.upload_states(words), eng.to_device(amps)
 
 
 # ---------------------------------------------------------------------------------------
@@ -181,7 +191,27 @@ def getGreen(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeigh
     restr = make_restrictions(restrictions, n)
     s_t, a_t = _psi_tensors(eng, psi, n)
     g = green_batch(eng, dop, restr, [s_t], [a_t], [e], omega, delta, krylovSize, precision, normalize=False)
-    return g[0].cpu().numpy()
+    return eng.to_host(g[0])
+
+
+def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7,
+                   precision=0, capture=None):
+    """Device form of :func:`getSpectra`: ``psi_t`` is a list of (states, amps) device tensors.
+
+    Returns g [n_states, n_ops, n_w] complex128 on the device.
+    """
+    ne = len(es)
+    w = np.asarray(w, dtype=np.float64)
+    run_states, run_amps, e_runs = [], [], []
+    for tdop in t_dops:
+        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], tdop, restr, slaterWeightMin)
+        for i, (s_, a_) in enumerate(outs):
+            run_states.append(s_)
+            run_amps.append(a_)
+            e_runs.append(es[i])
+    g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision,
+                    capture=capture)
+    return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
 
 
 def getSpectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=None, krylovSize=150,
@@ -196,21 +226,12 @@ def getSpectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=None
     eng = get_engine()
     n = int(n_spin_orbitals)
     words_for(n)
-    w = np.asarray(w, dtype=np.float64)
-    ne = len(es)
     dop = _device_op(hOp, eng)
     restr = make_restrictions(restrictions, n)
-    psi_t = [_psi_tensors(eng, psis[i], n) for i in range(ne)]
-    run_states, run_amps, e_runs = [], [], []
-    for top in tOps:
-        tdop = _device_op(top, eng)
-        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], tdop, restr, slaterWeightMin)
-        for i, (s, a) in enumerate(outs):
-            run_states.append(s)
-            run_amps.append(a)
-            e_runs.append(es[i])
-    g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision)
-    return g.view(len(tOps), ne, len(w)).permute(1, 0, 2).cpu().numpy()
+    psi_t = [_psi_tensors(eng, psis[i], n) for i in range(len(es))]
+    t_dops = [_device_op(top, eng) for top in tOps]
+    g = spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision)
+    return eng.to_host(g.contiguous())
 
 
 def _shifted_solutions(eng, sector, y, zs, tol, k_cap):
@@ -266,20 +287,29 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
     eng = get_engine()
     n = int(n_spin_orbitals)
     words_for(n)
-    wIns = np.asarray(wIns, dtype=np.float64)
-    wLoss = np.asarray(wLoss, dtype=np.float64)
-    ne, nin, nout, nwi = len(es), len(tOpsIn), len(tOpsOut), len(wIns)
-    gs = np.zeros((ne, nin, nout, nwi, len(wLoss)), dtype=complex)
-    if ne == 0 or nin == 0 or nout == 0 or nwi == 0:
-        return gs
     dop = _device_op(hOp, eng)
     restr = make_restrictions(restrictions, n)
-    psi_t = [_psi_tensors(eng, psis[i], n) for i in range(ne)]
+    psi_t = [_psi_tensors(eng, psis[i], n) for i in range(len(es))]
+    g = rixs_device(eng, dop, restr, [_device_op(t, eng) for t in tOpsIn], [_device_op(t, eng) for t in tOpsOut],
+                    psi_t, es, wIns, wLoss, delta1, delta2, krylovSize, slaterWeightMin, precision, solve_tol,
+                    share_out_memo, max_krylov)
+    return eng.to_host(g)
+
+
+def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
+                slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
+                timing=None, capture=None):
+    """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device)."""
+    wIns = np.asarray(wIns, dtype=np.float64)
+    wLoss = np.asarray(wLoss, dtype=np.float64)
+    ne, nin, nout, nwi = len(es), len(tin_dops), len(tout_dops), len(wIns)
+    gs = torch.zeros((ne, nin, nout, nwi, len(wLoss)), dtype=torch.complex128, device=eng.device)
+    if ne == 0 or nin == 0 or nout == 0 or nwi == 0:
+        return gs
     # 1. core-hole states psi1 = T_in psi
     psi1 = {}
-    for t_in, top in enumerate(tOpsIn):
-        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], _device_op(top, eng), restr,
-                                 slaterWeightMin)
+    for t_in, tdop in enumerate(tin_dops):
+        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], tdop, restr, slaterWeightMin)
         for ie, o in enumerate(outs):
             psi1[(t_in, ie)] = o
     nonempty = [v[0] for v in psi1.values() if v[0].shape[0]]
@@ -287,29 +317,30 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
         return gs
     # 2. core-hole sector
     core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
-    # 3. shifted solves: X[(t_in, ie)] [n_wIn, Nc]
-    t_outs = [_device_op(top, eng) for top in tOpsOut]
-    eff_out = [t_outs[0]] * nout if share_out_memo else t_outs
-    # outgoing operators as sparse maps core basis -> output states
+    # 3. outgoing operators as sparse maps core basis -> output states
     out_maps = []
     for k in range(nout):
         if share_out_memo and k > 0:
             out_maps.append(out_maps[0])
             continue
-        out_maps.append(_transfer_matrix(eng, eff_out[k], restr, core.basis))
-    x_blocks = []
-    keys = []
-    for (t_in, ie), (s1, a1) in psi1.items():
-        if s1.shape[0] == 0:
-            continue
-        y = torch.zeros(core.n, dtype=torch.complex128, device=eng.device)
-        y.index_put_((eng.lookup(core.basis, s1),), torch.complex(a1[:, 0], a1[:, 1]), accumulate=True)
-        zs = wIns + 1j * delta1 + es[ie]
-        X = _shifted_solutions(eng, core, y, zs, solve_tol, min(core.n, max_krylov))
-        x_blocks.append(X)
-        keys.append((t_in, ie))
-    # 4. psi3 = T_out psi2 for every (t_in, ie, w_in, t_out)
-    run_states, run_amps, e_runs, slots, scales = [], [], [], [], []
+        out_maps.append(_transfer_matrix(eng, tout_dops[0] if share_out_memo else tout_dops[k], restr, core.basis))
+    # 4. shifted solves x(z) = (z - H)^{-1} psi1 for every incoming energy and every
+    # (t_in, eigenstate) right-hand side
+    keys = [k for k, (s1, _) in psi1.items() if s1.shape[0]]
+    Y = torch.zeros((len(keys), core.n), dtype=torch.complex128, device=eng.device)
+    for r, key in enumerate(keys):
+        s1, a1 = psi1[key]
+        Y[r].index_put_((eng.lookup(core.basis, s1),), torch.complex(a1[:, 0], a1[:, 1]), accumulate=True)
+    zs = np.array([wIns + 1j * delta1 + es[ie] for (_, ie) in keys])
+    solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, min(core.n, max_krylov))
+    if solved is not None:
+        x_blocks = list(solved[0])
+    else:
+        x_blocks = [_shifted_solutions(eng, core, Y[r], zs[r], solve_tol, min(core.n, max_krylov))
+                    for r in range(len(keys))]
+    # 5. psi3 = T_out psi2 for every (t_in, ie, w_in, t_out), pruned and normalised as upstream
+    st_l, am_l, run_l, e_runs, slots, scales = [], [], [], [], [], []
+    run0 = 0
     for k in range(nout):
         tm = out_maps[k]
         for (t_in, ie), X in zip(keys, x_blocks):
@@ -319,23 +350,25 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
             nrm = torch.sqrt((P.real ** 2 + P.imag ** 2).sum(1, keepdim=True))
             Pn = P / torch.where(nrm > 0, nrm, torch.ones_like(nrm))
             keep = (Pn.real ** 2 + Pn.imag ** 2) >= slaterWeightMin
-            nrm2_h = (nrm[:, 0] ** 2).cpu().numpy()
-            for iw in range(nwi):
-                nz = torch.nonzero(keep[iw]).flatten()
-                run_states.append(tm.out_states[nz])
-                amp = Pn[iw, nz]
-                run_amps.append(torch.stack([amp.real, amp.imag], 1).contiguous())
-                e_runs.append(es[ie])
-                scales.append(nrm2_h[iw])
-                slots.append((ie, t_in, k, iw))
-    # 5. ground-like sector Lanczos + continued fractions for all runs at once.  Upstream
+            iw_idx, o_idx = torch.nonzero(keep, as_tuple=True)  # row-major: grouped by iw
+            st_l.append(tm.out_states[o_idx])
+            amp = Pn[iw_idx, o_idx]
+            am_l.append(torch.stack([amp.real, amp.imag], 1))
+            run_l.append(iw_idx + run0)
+            scales.append((nrm[:, 0] ** 2).cpu().numpy())
+            e_runs.extend([es[ie]] * nwi)
+            slots.extend((ie, t_in, k, iw) for iw in range(nwi))
+            run0 += nwi
+    packed = (torch.cat(st_l, 0).contiguous(), torch.cat(am_l, 0).contiguous(), torch.cat(run_l, 0), run0)
+    scales = np.concatenate(scales)
+    # 6. ground-like sector Lanczos + continued fractions for all runs at once.  Upstream
     # runs getGreen on the normalised-then-pruned psi3 and scales by the squared norm taken
     # before the second pruning (spectra.py:1097-1124).
-    g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, wLoss, delta2, krylovSize, precision,
-                    normalize=False, scales=scales)
-    g_h = g.cpu().numpy()
-    for r, (ie, t_in, k, iw) in enumerate(slots):
-        gs[ie, t_in, k, iw, :] = g_h[r]
+    g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
+                    normalize=False, scales=scales, timing=timing, capture=capture)
+    idx = torch.tensor([((ie * nin + t_in) * nout + k) * nwi + iw for (ie, t_in, k, iw) in slots],
+                       device=eng.device)
+    gs.view(-1, len(wLoss))[idx] = g
     return gs
 
 

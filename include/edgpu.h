@@ -187,12 +187,26 @@ int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* st
  * K = max over k_max.  Outputs alpha[R][K], beta[R][K] (beta[r][j] for j < k_max[r]-1).
  * precision: 0 = complex128 vectors and values; 1 = complex64 vectors, float32 SpMV
  * accumulation, float64 alpha/beta reductions.  Breakdown (beta == 0 before k_max) sets
- * *status_dev = EDGPU_ERR_BREAKDOWN.
+ * *status_dev = EDGPU_ERR_BREAKDOWN.  Sectors whose three Krylov vectors fit in shared
+ * memory run as one persistent launch with one CTA per run; larger ones as three
+ * grid-wide kernels per step.
  */
 size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision);
 int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
                   double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                   void* stream);
+
+/*
+ * edgpu_lanczos with CUDA-event timing of its kernels on the launching stream:
+ * kernel_ms (host, 3 doubles) receives the summed milliseconds of the SpMM + alpha,
+ * axpy + beta and normalise launches.  Synchronises on the last event before returning.
+ */
+int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                        double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                        void* stream, double* kernel_ms);
+
+/* Number of kernels the library has launched in this process so far. */
+long long edgpu_launch_count(void);
 
 /*
  * Lanczos with full (twice classical Gram-Schmidt) reorthogonalisation, one run, complex128,
@@ -207,6 +221,19 @@ size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap);
 int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
                          double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                          void* stream);
+
+/*
+ * Shifted solves X[r][z] = (zs[r][z] - H)^{-1} Y[r] for n_rhs right-hand sides (Y: [n_rhs][n]
+ * complex128) and nz <= 512 complex shifts each, from one Krylov space per right-hand side
+ * (Lanczos with two classical Gram-Schmidt passes, FP64), iterated until every shift's
+ * residual estimate ||r|| / ||y|| <= tol or k_cap steps.  X: [n_rhs][nz][n] complex128;
+ * m_out[r]: Krylov size used.  Replaces upstream's BiCGSTAB per incoming energy in getRIXSmap
+ * (spectra.py:962,1080).  Requires n * 16 + k_cap * 16 bytes of shared memory <= 200 KiB.
+ */
+size_t edgpu_shifted_solve_workspace(int64_t n, int n_rhs, int nz, int k_cap);
+int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
+                        double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
+                        size_t workspace_bytes, void* stream);
 
 /* X[m][n] = sum_k C[k][m] V[k][n] (complex128): Ritz vectors / shifted-solve solutions. */
 int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, double* X, void* stream);
