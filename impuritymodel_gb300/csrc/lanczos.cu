@@ -397,8 +397,121 @@ inline unsigned grid_1d(int64_t n, int threads) {
   return (unsigned)b;
 }
 
+// Row-parallel SpMM for y = H x with x, y [n][R]: thread = (row i, group g of RV runs),
+// L = R / RV threads per row, one row per thread, 16-byte vector loads of x (float4 holds
+// two complex64 runs, double2 one complex128 run) and UNROLL independent gathers in flight.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int runs = 2;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int runs = 1;
+};
+
+template <typename T, bool VALC>
+__global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t* __restrict__ rp,
+                                                        const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                                        int R, int L, const typename Cx<T>::V* __restrict__ X,
+                                                        typename Cx<T>::V* __restrict__ Y) {
+  using Q = typename Vec16<T>::type;
+  constexpr int RV = Vec16<T>::runs;
+  constexpr int UNROLL = 4;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = gt / L;
+  const int g = (int)(gt - i * L);
+  if (i >= n) return;
+  const int64_t r0 = (int64_t)g * RV;
+  T ar[RV], ai[RV];
+#pragma unroll
+  for (int q = 0; q < RV; ++q) ar[q] = ai[q] = 0;
+  const int64_t e0 = __ldg(rp + i), e1 = __ldg(rp + i + 1);
+  int64_t e = e0;
+  for (; e + UNROLL <= e1; e += UNROLL) {
+    int c[UNROLL];
+    T hr[UNROLL], hi[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      c[u] = __ldg(col + e + u);
+      if (VALC) {
+        hr[u] = __ldg(vals + 2 * (e + u));
+        hi[u] = __ldg(vals + 2 * (e + u) + 1);
+      } else {
+        hr[u] = __ldg(vals + e + u);
+        hi[u] = 0;
+      }
+    }
+    Q xv[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) xv[u] = __ldg(reinterpret_cast<const Q*>(X + (int64_t)c[u] * R + r0));
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const T* xs = reinterpret_cast<const T*>(&xv[u]);
+#pragma unroll
+      for (int q = 0; q < RV; ++q) {
+        const T xr = xs[2 * q], xi = xs[2 * q + 1];
+        ar[q] += hr[u] * xr;
+        ai[q] += hr[u] * xi;
+        if (VALC) {
+          ar[q] -= hi[u] * xi;
+          ai[q] += hi[u] * xr;
+        }
+      }
+    }
+  }
+  for (; e < e1; ++e) {
+    const int c = __ldg(col + e);
+    T hr, hi = 0;
+    if (VALC) {
+      hr = __ldg(vals + 2 * e);
+      hi = __ldg(vals + 2 * e + 1);
+    } else {
+      hr = __ldg(vals + e);
+    }
+    const Q xv = __ldg(reinterpret_cast<const Q*>(X + (int64_t)c * R + r0));
+    const T* xs = reinterpret_cast<const T*>(&xv);
+#pragma unroll
+    for (int q = 0; q < RV; ++q) {
+      const T xr = xs[2 * q], xi = xs[2 * q + 1];
+      ar[q] += hr * xr - hi * xi;
+      ai[q] += hr * xi + hi * xr;
+    }
+  }
+  Q out;
+  T* os = reinterpret_cast<T*>(&out);
+#pragma unroll
+  for (int q = 0; q < RV; ++q) {
+    os[2 * q] = ar[q];
+    os[2 * q + 1] = ai[q];
+  }
+  *reinterpret_cast<Q*>(Y + i * R + r0) = out;
+}
+
 template <typename T>
 int spmv_impl(const edgpu_csr* h, const typename Cx<T>::V* x, typename Cx<T>::V* y, int R, cudaStream_t s) {
+  constexpr int RV = Vec16<T>::runs;
+  if (R % RV == 0) {
+    const int L = R / RV;
+    const int64_t threads = h->n * (int64_t)L;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    if (sizeof(T) == 8) {
+      if (h->val_c)
+        spmm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_c, R, L, x, y);
+      else
+        spmm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_r, R, L, x, y);
+    } else {
+      if (h->val_cf)
+        spmm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_cf, R, L, x, y);
+      else
+        spmm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_rf, R, L, x, y);
+    }
+    note_launch();
+    return check_launch();
+  }
   RunTile t = make_tile(h->n, R);
   dim3 grid(t.nrb, t.nrt), block(t.rt, t.rb);
   if (sizeof(T) == 8) {

@@ -98,7 +98,8 @@ class Sector:
 
 
 def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
-                sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None):
+                sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
+                perturb=None):
     """Continued-fraction Green's functions of many start states on one sector.
 
     ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states (lists), or
@@ -149,6 +150,13 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
         scale_h = np.ones(runs) if scales is None else np.asarray(scales, dtype=np.float64)
     v0 = torch.zeros((sector.n, live.size), dtype=torch.complex128, device=eng.device)
     v0.index_put_((rows[sel], lr[sel]), vals[sel], accumulate=True)
+    if perturb is not None:
+        # verification only: relative start-vector perturbation (eps, seed) to measure how
+        # much the unreorthogonalised recurrence amplifies rounding-level differences
+        eps, seed = perturb
+        gen = torch.Generator(device=eng.device)
+        gen.manual_seed(int(seed))
+        v0 = v0 * (1.0 + eps * torch.randn(v0.shape, dtype=torch.float64, device=eng.device, generator=gen))
     dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
     k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
     alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision, timing=timing)
@@ -195,7 +203,7 @@ def getGreen(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeigh
 
 
 def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7,
-                   precision=0, capture=None):
+                   precision=0, capture=None, perturb=None):
     """Device form of :func:`getSpectra`: ``psi_t`` is a list of (states, amps) device tensors.
 
     Returns g [n_states, n_ops, n_w] complex128 on the device.
@@ -210,7 +218,7 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
             run_amps.append(a_)
             e_runs.append(es[i])
     g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision,
-                    capture=capture)
+                    capture=capture, perturb=perturb)
     return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
 
 
@@ -298,7 +306,7 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
 
 def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                 slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-                timing=None, capture=None):
+                timing=None, capture=None, perturb=None):
     """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device)."""
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
@@ -365,7 +373,7 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     # runs getGreen on the normalised-then-pruned psi3 and scales by the squared norm taken
     # before the second pruning (spectra.py:1097-1124).
     g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
-                    normalize=False, scales=scales, timing=timing, capture=capture)
+                    normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb)
     idx = torch.tensor([((ie * nin + t_in) * nout + k) * nwi + iw for (ie, t_in, k, iw) in slots],
                        device=eng.device)
     gs.view(-1, len(wLoss))[idx] = g

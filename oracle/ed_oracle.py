@@ -626,7 +626,7 @@ def exact_green(h, psi0, omega, delta, e):
 
 
 def get_green(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeightMin, restrictions=None,
-              memo=None, return_coeffs=False, exact=False):
+              memo=None, return_coeffs=False, exact=False, perturb=None):
     """``spectra.getGreen`` sparse mode (spectra.py:551-681); ``exact=True`` returns the
     exact resolvent of the same sector instead of the Krylov continued fraction."""
     g = np.zeros(len(omega), dtype=complex)
@@ -640,6 +640,11 @@ def get_green(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeig
     for ps, amp in psi.items():
         psi0[index[ps]] = amp
     k = min(krylovSize, n)
+    if perturb is not None:
+        # relative perturbation of the start vector (eps, numpy Generator): probes how much
+        # upstream's unreorthogonalised recurrence amplifies rounding-level differences
+        eps, rng = perturb
+        psi0 = psi0 * (1.0 + eps * rng.standard_normal(n))
     if exact:
         g = exact_green(h, psi0, omega, delta, e)
         return (g, None, None, n) if return_coeffs else g
@@ -651,7 +656,7 @@ def get_green(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeig
 
 
 def get_spectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=None, krylovSize=150,
-                slaterWeightMin=1e-7, return_coeffs=False, exact=False):
+                slaterWeightMin=1e-7, return_coeffs=False, exact=False, perturb=None):
     """``spectra.getSpectra`` in its default ``H_build`` mode (spectra.py:684-806)."""
     n = len(es)
     gs = np.zeros((n, len(tOps), len(w)), dtype=complex)
@@ -665,7 +670,7 @@ def get_spectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=Non
             for state in psi_r.keys():
                 psi_r[state] /= normalization
             g, a, b, dim = get_green(n_spin_orbitals, es[i], psi_r, hOp, w, delta, krylovSize, slaterWeightMin,
-                                     restrictions, memo=memo, return_coeffs=True, exact=exact)
+                                     restrictions, memo=memo, return_coeffs=True, exact=exact, perturb=perturb)
             gs[i, t, :] = normalization**2 * g
             coeffs[(i, t)] = (a, b, dim, normalization)
     if return_coeffs:
@@ -675,7 +680,7 @@ def get_spectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=Non
 
 def get_rixs_map(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, delta1, delta2, restrictions=None,
                  krylovSize=150, slaterWeightMin=1e-7, solver="bicgstab", rtol=1e-5, share_out_memo=True,
-                 exact=False):
+                 exact=False, perturb=None):
     """``spectra.getRIXSmap`` (spectra.py:809-1130), ``wIn``/``H_build_wIn`` branch.
 
     ``solver='bicgstab'`` calls SciPy's BiCGSTAB with the given ``rtol`` as upstream does
@@ -727,5 +732,5 @@ def get_rixs_map(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, d
                             psi3.pop(state)
                     gs[ie, t_in, t_out, iw, :] = normalization**2 * get_green(
                         n_spin_orbitals, e, psi3, hOp, wLoss, delta2, krylovSize, slaterWeightMin, restrictions,
-                        memo=memo_gnd, exact=exact)
+                        memo=memo_gnd, exact=exact, perturb=perturb)
     return gs

@@ -1,0 +1,141 @@
+"""C ABI exports and host-side logic (no GPU): the library loads and exports every symbol
+declared in include/edgpu.h; operator compilation, restriction masks, codec round trips;
+replica sharding over two gloo ranks."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from impuritymodel_gb300 import _lib, build
+
+    build()
+    return _lib.load()
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "edgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(edgpu_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+    from impuritymodel_gb300._lib import SIGNATURES
+
+    assert set(SIGNATURES) == set(names)
+
+
+def test_abi_version_and_status_strings(lib):
+    assert lib.edgpu_abi_version() == 1
+    assert lib.edgpu_status_string(0) == b"ok"
+    assert b"breakdown" in lib.edgpu_status_string(3).lower()
+
+
+def test_entry_points_reject_bad_arguments_without_a_gpu(lib):
+    # argument validation happens before any CUDA call
+    from impuritymodel_gb300 import _lib as L
+
+    assert lib.edgpu_apply_columns(0, None, 1, None, None, 0.0, None, 0, 0, None, None, None, None, None, 0, 0, None,
+                                   None) == L.EDGPU_ERR_ARG
+    assert lib.edgpu_sort_states(9, None, None, 10, None, None, 0, None) == L.EDGPU_ERR_ARG
+    assert lib.edgpu_cfrac(None, None, None, 1, 1, None, 1, 0.1, None, None, None, None) == L.EDGPU_ERR_ARG
+
+
+def test_operator_compilation():
+    from impuritymodel_gb300.engine import DeviceOp
+
+    op = {((3, "c"), (3, "a")): 1.5, ((0, "c"), (70, "a")): 0.5 + 0.25j,
+          ((1, "c"), (2, "c"), (2, "a"), (1, "a")): -2.0, ((1, "c"), (2, "c"), (4, "a"), (5, "a")): 0.1}
+    d = DeviceOp(op, torch.device("cpu"))
+    ops = d.ops.numpy().view(np.uint64)
+    flags = d.flags.numpy().view(np.uint32)
+    assert [int(f) & 1 for f in flags] == [1, 0, 1, 0]
+    assert [(int(f) >> 8) & 7 for f in flags] == [2, 2, 4, 4]
+    slot = lambda t, k: (int(ops[t]) >> (16 * k)) & 0xFFFF  # noqa: E731
+    assert slot(1, 0) == 0x8000 | 0x4000 | 0 and slot(1, 1) == 0x8000 | 70
+    assert slot(0, 2) == 0
+    assert not d.is_real
+    assert np.allclose(d.coeff.numpy()[1], [0.5, 0.25])
+    with pytest.raises(ValueError):
+        DeviceOp({((0, "x"),): 1.0}, torch.device("cpu"))
+
+
+def test_restriction_masks():
+    from impuritymodel_gb300.engine import make_restrictions
+
+    r = make_restrictions({frozenset([0, 63, 64, 100]): (1, 3)}, 128)
+    assert r.n == 1 and r.lo[0] == 1 and r.hi[0] == 3
+    assert r.mask[0][0] == (1 << 63) | 1
+    assert r.mask[0][1] == (1 << 63) | (1 << (63 - 36))
+
+
+def test_codec_round_trip():
+    from impuritymodel_gb300 import codec
+
+    rng = np.random.default_rng(0)
+    for n in (7, 26, 64, 66, 316):
+        states = [codec.tuple_to_bytes(tuple(sorted(rng.choice(n, n // 3, replace=False))), n) for _ in range(50)]
+        w = codec.bytes_to_words(states, n)
+        assert codec.words_to_bytes(w, n) == states
+        # lexicographic word order == bytes order
+        order = np.lexsort([w[:, q] for q in range(w.shape[1] - 1, -1, -1)])
+        assert [states[i] for i in order] == sorted(states)
+
+
+def test_job_tasks_partition():
+    from impuritymodel_gb300.finite import get_job_tasks
+
+    for ranks in (1, 2, 3, 7):
+        got = sorted(t for r in range(ranks) for t in get_job_tasks(r, ranks, list(range(50))))
+        assert got == list(range(50))
+
+
+def _replica_worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    from impuritymodel_gb300.finite import get_job_tasks
+
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    mine = list(get_job_tasks(rank, world, list(range(23))))
+    gathered = [None] * world
+    dist.all_gather_object(gathered, mine)
+    t = torch.tensor([0.5 + rank], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    if rank == 0:
+        out.put((sorted(x for g in gathered for x in g), float(t.item())))
+    dist.destroy_process_group()
+
+
+def test_replicas_over_two_gloo_ranks():
+    """Independent units (incoming energies) split over ranks with no data exchange; the
+    host gathers them and times are reduced with MAX, as bench.py does for N > 1."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    units, tmax = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert units == list(range(23))
+    assert tmax == 1.5
