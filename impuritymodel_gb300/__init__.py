@@ -11,6 +11,6 @@ __version__ = "0.1.0"
 
 
 def build(verbose=False, force=False):
-    from .build import build as _build
+    from .nvcc_build import build as _build
 
     return _build(verbose=verbose, force=force)

@@ -1,7 +1,7 @@
 """ctypes binding of ``libedgpu.so`` (the C ABI declared in ``include/edgpu.h``).
 
 The library is loaded from ``impuritymodel_gb300/_lib/libedgpu.so`` (built in-tree by
-``impuritymodel_gb300.build``).  There is no fallback: if the library is missing the
+``impuritymodel_gb300.nvcc_build``).  There is no fallback: if the library is missing the
 import of the engine raises.
 """
 
@@ -118,7 +118,7 @@ def load(path=None):
     p = path or LIB_PATH
     if not os.path.exists(p):
         raise ImportError(
-            "libedgpu.so not found at %s; build it with `python -m impuritymodel_gb300.build` "
+            "libedgpu.so not found at %s; build it with `python -m impuritymodel_gb300.nvcc_build` "
             "(there is no CPU fallback)" % p
         )
     lib = C.CDLL(p)
