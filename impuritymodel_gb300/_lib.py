@@ -27,6 +27,7 @@ FILTER_NOT_IN_BASIS = 2
 
 MAX_RESTRICTIONS = 8
 MAX_WORDS = 8
+EDGPU_LANCZOS_NOALLOC_BYTES = 16 << 20  # size of the library's static scratch array
 
 # Exported symbols and their signatures (restype, argtypes).
 _P = C.c_void_p
@@ -85,6 +86,7 @@ SIGNATURES = {
     "edgpu_lanczos": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),
     "edgpu_launch_count": (C.c_longlong, []),
+    "edgpu_lanczos_noalloc": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P]),
     "edgpu_lanczos_reorth_workspace": (_SZ, [_I64, _I]),
     "edgpu_lanczos_reorth": (_I, [C.POINTER(CSR), _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_shifted_solve_workspace": (_SZ, [_I64, _I, _I, _I]),

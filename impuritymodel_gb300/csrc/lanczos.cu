@@ -1227,3 +1227,57 @@ extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rh
   note_launch();
   return check_launch();
 }
+
+// =======================================================================================
+// Allocation-free batched Lanczos (edgpu_lanczos_noalloc).
+//
+// For callers that cannot allocate device memory themselves.  The grid-wide batched
+// Lanczos needs three [n][R] vectors and per-block partial sums as scratch; here that
+// scratch is this file's static device array, which every GPU that loads the library
+// holds until the process exits.  Host code must not hand the array's name to a kernel
+// (in host code it is only a stand-in symbol): its device address is looked up once per
+// device with cudaGetSymbolAddress, with that device current, and cached.
+// =======================================================================================
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_lanczos_noalloc_scratch[EDGPU_LANCZOS_NOALLOC_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+int noalloc_scratch_address(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return EDGPU_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return EDGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_lanczos_noalloc_scratch) != cudaSuccess || !p) return EDGPU_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return EDGPU_OK;
+}
+}  // namespace
+
+extern "C" int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K,
+                                     int precision, double* alpha, double* beta, int32_t* status_dev, void* stream) {
+  if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  if (precision == 0 && !h->val_c && !h->val_r) return EDGPU_ERR_ARG;
+  if (precision != 0 && !h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
+  if (edgpu_lanczos_workspace(h->n, R, K, precision) > (size_t)EDGPU_LANCZOS_NOALLOC_BYTES)
+    return EDGPU_ERR_WORKSPACE;
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch_address(&scratch);
+  if (rc) return rc;
+  unsigned char* ws = reinterpret_cast<unsigned char*>(scratch);
+  const size_t bytes = (size_t)EDGPU_LANCZOS_NOALLOC_BYTES;
+  cudaStream_t s = (cudaStream_t)stream;
+  // Every buffer in the scratch is written before it is read (the start vectors are
+  // copied in, v_{j-1} is first read after step 0 wrote it, partial sums are written by
+  // the kernel that precedes their reader), so nothing has to be cleared between calls.
+  if (precision == 0) return edgpu::lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, bytes, s);
+  return edgpu::lanczos_impl<float>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, bytes, s);
+}

@@ -209,6 +209,28 @@ int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, const int32
 long long edgpu_launch_count(void);
 
 /*
+ * edgpu_lanczos without any device allocation by the caller or the library, for callers
+ * that cannot allocate device memory: for instance a host code whose memory manager owns
+ * the whole GPU and forbids cudaMalloc, or a solver loop embedded in another program where
+ * an allocation would synchronise the device between time steps.  The caller passes the
+ * inputs and outputs of edgpu_lanczos (no workspace); this always runs the grid-wide
+ * batched Lanczos (three kernels per step) and keeps its scratch (three [n][R] vectors
+ * and partial sums, size edgpu_lanczos_workspace(n, R, K, precision)) in a static
+ * device array of EDGPU_LANCZOS_NOALLOC_BYTES inside the library, which every GPU that
+ * loads the library holds until the process exits.  Larger problems are rejected with
+ * EDGPU_ERR_WORKSPACE before anything runs.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress,
+ * with that device current); make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different streams, or
+ * threads without ordering) race on it and must be serialised by the caller.  No part of
+ * the scratch needs to start at zero.
+ * No counterpart in upstream impurityModel.
+ */
+#define EDGPU_LANCZOS_NOALLOC_BYTES (16u << 20)
+int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
+                          double* alpha, double* beta, int32_t* status_dev, void* stream);
+
+/*
  * Lanczos with full (twice classical Gram-Schmidt) reorthogonalisation, one run, complex128,
  * storing the Krylov basis V[K_cap][n].  Runs steps j0 .. j1-1 (resumable: the caller keeps
  * V, alpha, beta and the work vector between calls).  Step j0 == 0 copies v0 into V[0].
