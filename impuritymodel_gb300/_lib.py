@@ -93,6 +93,8 @@ SIGNATURES = {
     "edgpu_shifted_solve": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_combine": (_I, [_P, _I, _I64, _P, _I, _P, _P]),
     "edgpu_cfrac": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P]),
+    "edgpu_cfrac_f32_workspace": (_SZ, [_I, _I]),
+    "edgpu_cfrac_f32": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P, _SZ, _P]),
 }
 
 _lib = None

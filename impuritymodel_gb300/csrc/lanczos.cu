@@ -172,14 +172,9 @@ __global__ void normalize_kernel(int64_t n, int R, const typename Cx<T>::V* __re
   for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ti; i < n; i += (int64_t)gridDim.x * blockDim.y) {
     V w = Wv[i * R + r];
     V o;
-    if (sizeof(T) == 8) {
-      // upstream divides: v = w / beta
-      o.x = beta > 0.0 ? (T)((double)w.x / beta) : (T)0;
-      o.y = beta > 0.0 ? (T)((double)w.y / beta) : (T)0;
-    } else {
-      o.x = w.x * inv;
-      o.y = w.y * inv;
-    }
+    // one reciprocal per run and step: FP64 division is many times the cost of an FMA
+    o.x = w.x * inv;
+    o.y = w.y * inv;
     Vn[i * R + r] = o;
   }
 }
@@ -256,6 +251,7 @@ __global__ void subtract_proj_kernel(const double2* __restrict__ V, int m, int64
                                      double2* __restrict__ w) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double2 x = w[i];
+#pragma unroll 8
     for (int k = 0; k < m; ++k) {
       const double2 c = h[k];
       const double2 v = V[(int64_t)k * n + i];
@@ -335,6 +331,7 @@ __global__ void combine_kernel(const double2* __restrict__ V, int K, int64_t n, 
   const int m = blockIdx.y;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double xr = 0.0, xi = 0.0;
+#pragma unroll 8
     for (int k = 0; k < K; ++k) {
       const double2 c = C[(int64_t)k * M + m];
       const double2 v = V[(int64_t)k * n + i];
@@ -368,18 +365,11 @@ __global__ void cfrac_kernel(const double* __restrict__ alpha, const double* __r
       dr -= b2 * gr;
       di -= b2 * gi;
     }
-    // g = 1 / (dr + i di), Smith's algorithm
-    if (fabs(dr) >= fabs(di)) {
-      const double q = di / dr;
-      const double den = dr + di * q;
-      gr = 1.0 / den;
-      gi = -q / den;
-    } else {
-      const double q = dr / di;
-      const double den = dr * q + di;
-      gr = q / den;
-      gi = -1.0 / den;
-    }
+    // g = 1 / (dr + i di) = (dr - i di) / |d|^2; |d| >= delta > 0 and the entries are
+    // energies of order 1e3 eV at most, so |d|^2 neither overflows nor underflows
+    const double inv = 1.0 / (dr * dr + di * di);
+    gr = dr * inv;
+    gi = -di * inv;
   }
   const double s = scale ? scale[r] : 1.0;
   g[tid] = kl > 0 ? make_double2(s * gr, s * gi) : make_double2(0.0, 0.0);
@@ -388,6 +378,47 @@ __global__ void cfrac_kernel(const double* __restrict__ alpha, const double* __r
 bool small_fits(int64_t n, int precision);
 int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
                   double* alpha, double* beta, int32_t* status, cudaStream_t s);
+
+// Mixed form: a'[r][i] = float(alpha - e_r), b2[r][i] = float(beta^2) (FP64 subtraction
+// first, so the large common energy cancels exactly), then the fraction in float32.
+__global__ void cfrac_prep_kernel(const double* __restrict__ alpha, const double* __restrict__ beta,
+                                  const int32_t* __restrict__ k_len, int K, int R, const double* __restrict__ e,
+                                  float* __restrict__ ap, float* __restrict__ b2) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)R * K) return;
+  const int r = (int)(t / K);
+  const int i = (int)(t % K);
+  ap[t] = (float)(alpha[t] - e[r]);
+  b2[t] = (float)(beta[t] * beta[t]);
+  (void)k_len;
+}
+
+__global__ void cfrac_f32_kernel(const float* __restrict__ ap, const float* __restrict__ b2,
+                                 const int32_t* __restrict__ k_len, int K, int R, const double* __restrict__ omega,
+                                 int n_omega, double delta, const double* __restrict__ scale, double2* __restrict__ g) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (int64_t)R * n_omega) return;
+  const int r = (int)(tid / n_omega);
+  const int w = (int)(tid % n_omega);
+  const int kl = k_len[r];
+  const float zr = (float)omega[w];
+  const float zi = (float)delta;
+  const float* a = ap + (int64_t)r * K;
+  const float* b = b2 + (int64_t)r * K;
+  float gr = 0.f, gi = 0.f;
+  for (int i = kl - 1; i >= 0; --i) {
+    float dr = zr - a[i], di = zi;
+    if (i != kl - 1) {
+      dr -= b[i] * gr;
+      di -= b[i] * gi;
+    }
+    const float inv = 1.0f / (dr * dr + di * di);
+    gr = dr * inv;
+    gi = -di * inv;
+  }
+  const double s = scale ? scale[r] : 1.0;
+  g[tid] = kl > 0 ? make_double2(s * (double)gr, s * (double)gi) : make_double2(0.0, 0.0);
+}
 
 inline unsigned grid_1d(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
@@ -420,7 +451,7 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t
                                                         typename Cx<T>::V* __restrict__ Y) {
   using Q = typename Vec16<T>::type;
   constexpr int RV = Vec16<T>::runs;
-  constexpr int UNROLL = 4;
+  constexpr int UNROLL = 8;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t i = gt / L;
   const int g = (int)(gt - i * L);
@@ -436,12 +467,13 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t
     T hr[UNROLL], hi[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      c[u] = __ldg(col + e + u);
+      // CSR entries are read once: streaming loads keep x resident in L2
+      c[u] = __ldcs(col + e + u);
       if (VALC) {
-        hr[u] = __ldg(vals + 2 * (e + u));
-        hi[u] = __ldg(vals + 2 * (e + u) + 1);
+        hr[u] = __ldcs(vals + 2 * (e + u));
+        hi[u] = __ldcs(vals + 2 * (e + u) + 1);
       } else {
-        hr[u] = __ldg(vals + e + u);
+        hr[u] = __ldcs(vals + e + u);
         hi[u] = 0;
       }
     }
@@ -488,7 +520,7 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t
     os[2 * q] = ar[q];
     os[2 * q + 1] = ai[q];
   }
-  *reinterpret_cast<Q*>(Y + i * R + r0) = out;
+  __stcs(reinterpret_cast<Q*>(Y + i * R + r0), out);
 }
 
 template <typename T>
@@ -788,6 +820,27 @@ extern "C" int edgpu_combine(const double* V, int K, int64_t n, const double* C,
   return check_launch();
 }
 
+extern "C" size_t edgpu_cfrac_f32_workspace(int K, int R) { return 2 * sizeof(float) * (size_t)K * R + 512; }
+
+extern "C" int edgpu_cfrac_f32(const double* alpha, const double* beta, const int32_t* k_len, int K, int R,
+                               const double* omega, int n_omega, double delta, const double* e, const double* scale,
+                               double* g, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!alpha || !beta || !k_len || !omega || !e || !g || K < 1 || R < 0 || n_omega < 0) return EDGPU_ERR_ARG;
+  const int64_t tot = (int64_t)R * n_omega;
+  if (tot == 0) return EDGPU_OK;
+  if (!workspace || workspace_bytes < edgpu_cfrac_f32_workspace(K, R)) return EDGPU_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* ap = reinterpret_cast<float*>(workspace);
+  float* b2 = ap + (size_t)K * R;
+  const int64_t tk = (int64_t)K * R;
+  cfrac_prep_kernel<<<(unsigned)((tk + 255) / 256), 256, 0, s>>>(alpha, beta, k_len, K, R, e, ap, b2);
+  note_launch();
+  cfrac_f32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ap, b2, k_len, K, R, omega, n_omega, delta, scale,
+                                                               reinterpret_cast<double2*>(g));
+  note_launch();
+  return check_launch();
+}
+
 extern "C" int edgpu_cfrac(const double* alpha, const double* beta, const int32_t* k_len, int K, int R,
                            const double* omega, int n_omega, double delta, const double* e, const double* scale,
                            double* g, void* stream) {
@@ -898,17 +951,12 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_kernel(
         beta[(int64_t)r * K + j] = b;
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
       }
+      const T inv = b > 0.0 ? (T)(1.0 / b) : (T)0;
       for (int64_t i = tid; i < n; i += bs) {
         const V w = y[i];
         V o;
-        if (sizeof(T) == 8) {
-          o.x = b > 0.0 ? (T)((double)w.x / b) : (T)0;
-          o.y = b > 0.0 ? (T)((double)w.y / b) : (T)0;
-        } else {
-          const T inv = b > 0.0 ? (T)(1.0 / b) : (T)0;
-          o.x = w.x * inv;
-          o.y = w.y * inv;
-        }
+        o.x = w.x * inv;
+        o.y = w.y * inv;
         p[i] = o;  // overwrite v_{j-1} with v_{j+1}
       }
       __syncthreads();
@@ -958,10 +1006,13 @@ int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_
 
 // ---------------------------------------------------------------------------------------
 // Shifted solves (z - H) x = y for many z from one Krylov space, CTA per right-hand side.
-// Full reorthogonalisation (two classical Gram-Schmidt passes) in FP64; the Krylov basis
-// lives in global memory V[rhs][k_cap][n] (L2-resident for small sectors).  Thread t < nz
-// tracks shift z_t: LU pivots d_k = (z - a_k) - b_{k-1}^2 / d_{k-1} and the last component
-// q_m of (z - T_m)^{-1} e_1, so the residual estimate b_{m-1} |q_m| costs O(1) per step.
+// The Lanczos vectors v_{j-1}, v_j and w live in shared memory; each v_j is also written to
+// V[rhs][j][n] for assembling x(z) = |y| V (z - T)^{-1} e_1 afterwards.  No
+// reorthogonalisation: the three-term relation H V = V T + b v e^T holds to rounding even
+// after orthogonality is lost, so the residual estimate below stays valid and the loop
+// simply runs until it is met.  Thread t < nz tracks shift z_t: LU pivots
+// d_k = (z - a_k) - b_{k-1}^2 / d_{k-1} and the last component q_m of (z - T_m)^{-1} e_1,
+// so the residual ||r|| / ||y|| = b_{m-1} |q_m| costs O(1) per step.
 // Replaces upstream's per-energy BiCGSTAB (spectra.py:962,1080).
 // ---------------------------------------------------------------------------------------
 template <bool VALC>
@@ -971,11 +1022,11 @@ __global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
     double2* __restrict__ V, double* __restrict__ alpha, double* __restrict__ beta, int32_t* __restrict__ m_out,
     double* __restrict__ ynorm_out, int32_t* status) {
   extern __shared__ __align__(16) unsigned char sm[];
-  double2* w = reinterpret_cast<double2*>(sm);
-  double2* hc = w + n;  // k_cap reorthogonalisation coefficients
-  double* red = reinterpret_cast<double*>(hc + k_cap);
+  double2* X = reinterpret_cast<double2*>(sm);
+  double2* P = X + n;
+  double2* Wv = P + n;
+  double* red = reinterpret_cast<double*>(Wv + n);
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nwarps = bs >> 5;
   for (int r = blockIdx.x; r < n_rhs; r += gridDim.x) {
     double2* Vr = V + (size_t)r * k_cap * n;
     const double2* y = Y + (size_t)r * n;
@@ -987,20 +1038,27 @@ __global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
       if (tid == 0) m_out[r] = 0;
       continue;
     }
-    for (int64_t i = tid; i < n; i += bs) Vr[i] = make_double2(y[i].x / yn, y[i].y / yn);
+    const double iyn = 1.0 / yn;
+    for (int64_t i = tid; i < n; i += bs) {
+      const double2 v = make_double2(y[i].x * iyn, y[i].y * iyn);
+      X[i] = v;
+      P[i] = make_double2(0.0, 0.0);
+      Vr[i] = v;
+    }
     __syncthreads();
+    double2* x = X;
+    double2* p = P;
     double2 z = make_double2(0.0, 0.0), d = make_double2(1.0, 0.0), q = make_double2(1.0, 0.0);
     if (tid < nz) z = zs[(size_t)r * nz + tid];
     double bprev = 0.0;
     int m = k_cap;
     for (int j = 0; j < k_cap; ++j) {
-      const double2* vj = Vr + (size_t)j * n;
       acc = 0.0;
       for (int64_t i = tid; i < n; i += bs) {
         double yr = 0.0, yi = 0.0;
         const int64_t e1 = rp[i + 1];
         for (int64_t e = rp[i]; e < e1; ++e) {
-          const double2 xv = vj[col[e]];
+          const double2 xv = x[col[e]];
           if (VALC) {
             const double hr = vals[2 * e], hi = vals[2 * e + 1];
             yr += hr * xv.x - hi * xv.y;
@@ -1011,58 +1069,22 @@ __global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
             yi += h * xv.y;
           }
         }
-        w[i] = make_double2(yr, yi);
-        acc += yr * vj[i].x + yi * vj[i].y;
+        Wv[i] = make_double2(yr, yi);
+        acc += yr * x[i].x + yi * x[i].y;
       }
       const double a = block_sum(acc, red);
       if (tid == 0) alpha[(size_t)r * k_cap + j] = a;
-      for (int64_t i = tid; i < n; i += bs) {
-        double2 t = w[i];
-        const double2 c = vj[i];
-        t.x -= a * c.x;
-        t.y -= a * c.y;
-        if (j > 0) {
-          const double2 pv = Vr[(size_t)(j - 1) * n + i];
-          t.x -= bprev * pv.x;
-          t.y -= bprev * pv.y;
-        }
-        w[i] = t;
-      }
-      __syncthreads();
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int k = warp; k <= j; k += nwarps) {
-          const double2* vk = Vr + (size_t)k * n;
-          double hr = 0.0, hi = 0.0;
-          for (int64_t i = lane; i < n; i += 32) {
-            const double2 v = vk[i], x = w[i];
-            hr += v.x * x.x + v.y * x.y;
-            hi += v.x * x.y - v.y * x.x;
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            hr += __shfl_down_sync(0xffffffffu, hr, o);
-            hi += __shfl_down_sync(0xffffffffu, hi, o);
-          }
-          if (lane == 0) hc[k] = make_double2(hr, hi);
-        }
-        __syncthreads();
-        for (int64_t i = tid; i < n; i += bs) {
-          double2 x = w[i];
-          for (int k = 0; k <= j; ++k) {
-            const double2 c = hc[k];
-            const double2 v = Vr[(size_t)k * n + i];
-            x.x -= c.x * v.x - c.y * v.y;
-            x.y -= c.x * v.y + c.y * v.x;
-          }
-          w[i] = x;
-        }
-        __syncthreads();
-      }
       acc = 0.0;
-      for (int64_t i = tid; i < n; i += bs) acc += w[i].x * w[i].x + w[i].y * w[i].y;
+      for (int64_t i = tid; i < n; i += bs) {
+        double2 t = Wv[i];
+        const double2 c = x[i], pv = p[i];
+        t.x = (t.x - a * c.x) - bprev * pv.x;
+        t.y = (t.y - a * c.y) - bprev * pv.y;
+        Wv[i] = t;
+        acc += t.x * t.x + t.y * t.y;
+      }
       const double b = sqrt(block_sum(acc, red));
       if (tid == 0) beta[(size_t)r * k_cap + j] = b;
-      // shift-wise LU pivot and residual estimate for T_{j+1}
       bool ok = true;
       if (tid < nz) {
         double2 dn = make_double2(z.x - a, z.y);
@@ -1072,21 +1094,34 @@ __global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
           dn.x -= b2 * d.x / den;
           dn.y += b2 * d.y / den;
         }
-        // q_{j+1} = q_j * (j > 0 ? bprev : 1) / dn
         const double2 qn = make_double2(j > 0 ? q.x * bprev : 1.0, j > 0 ? q.y * bprev : 0.0);
         const double den = dn.x * dn.x + dn.y * dn.y;
         q = make_double2((qn.x * dn.x + qn.y * dn.y) / den, (qn.y * dn.x - qn.x * dn.y) / den);
         d = dn;
         ok = b * sqrt(q.x * q.x + q.y * q.y) <= tol;
       }
-      const bool done = __syncthreads_and(ok) || !(b > 0.0) || j + 1 == k_cap;
-      if (done) {
+      const bool conv = __syncthreads_and(ok);
+      if (conv || !(b > 0.0) || j + 1 == k_cap) {
         m = j + 1;
-        if (!(b >= 0.0) && tid == 0) atomicExch(status, (int32_t)EDGPU_ERR_NAN);
+        if (tid == 0) {
+          if (!(b >= 0.0))
+            atomicExch(status, (int32_t)EDGPU_ERR_NAN);
+          else if (!conv && b > 0.0)
+            atomicExch(status, (int32_t)EDGPU_ERR_NOCONV);
+        }
         break;
       }
-      for (int64_t i = tid; i < n; i += bs) Vr[(size_t)(j + 1) * n + i] = make_double2(w[i].x / b, w[i].y / b);
+      const double ib = 1.0 / b;
+      double2* vn = Vr + (size_t)(j + 1) * n;
+      for (int64_t i = tid; i < n; i += bs) {
+        const double2 v = make_double2(Wv[i].x * ib, Wv[i].y * ib);
+        p[i] = v;  // v_{j-1} is no longer needed: its buffer becomes v_{j+1}
+        vn[i] = v;
+      }
       __syncthreads();
+      double2* t = p;
+      p = x;
+      x = t;
       bprev = b;
     }
     if (tid == 0) m_out[r] = m;
@@ -1149,6 +1184,7 @@ __global__ void combine_batched_kernel(const double2* __restrict__ V, const doub
   const double2* Vr = V + (size_t)r * k_cap * n;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double xr = 0.0, xi = 0.0;
+#pragma unroll 8
     for (int k = 0; k < m; ++k) {
       const double2 ck = c[k];
       const double2 v = Vr[(size_t)k * n + i];
@@ -1178,7 +1214,7 @@ extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rh
   if (nz > kSmallThreads) return EDGPU_ERR_ARG;
   if (workspace_bytes < edgpu_shifted_solve_workspace(h->n, n_rhs, nz, k_cap)) return EDGPU_ERR_WORKSPACE;
   const int64_t n = h->n;
-  const size_t smem = sizeof(double2) * (size_t)n + sizeof(double2) * (size_t)k_cap + 34 * sizeof(double) + 16;
+  const size_t smem = 3 * sizeof(double2) * (size_t)n + 34 * sizeof(double) + 16;
   if (smem > 200 * 1024) return EDGPU_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);

@@ -161,7 +161,7 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
     alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision, timing=timing)
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
-    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live])
+    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live], precision=precision)
     if capture is not None:
         capture.append(dict(csr=sector.csr, v0=v0, k=k_h, e=e_live, scale=scale_h[live], live=live, g=g,
                             omega=omega, delta=delta))
@@ -340,7 +340,8 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
         s1, a1 = psi1[key]
         Y[r].index_put_((eng.lookup(core.basis, s1),), torch.complex(a1[:, 0], a1[:, 1]), accumulate=True)
     zs = np.array([wIns + 1j * delta1 + es[ie] for (_, ie) in keys])
-    solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, min(core.n, max_krylov))
+    # without reorthogonalisation the recurrence may need a few times the sector dimension
+    solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, min(6 * core.n + 50, max_krylov))
     if solved is not None:
         x_blocks = list(solved[0])
     else:

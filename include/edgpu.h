@@ -247,10 +247,10 @@ int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, i
 /*
  * Shifted solves X[r][z] = (zs[r][z] - H)^{-1} Y[r] for n_rhs right-hand sides (Y: [n_rhs][n]
  * complex128) and nz <= 512 complex shifts each, from one Krylov space per right-hand side
- * (Lanczos with two classical Gram-Schmidt passes, FP64), iterated until every shift's
- * residual estimate ||r|| / ||y|| <= tol or k_cap steps.  X: [n_rhs][nz][n] complex128;
- * m_out[r]: Krylov size used.  Replaces upstream's BiCGSTAB per incoming energy in getRIXSmap
- * (spectra.py:962,1080).  Requires n * 16 + k_cap * 16 bytes of shared memory <= 200 KiB.
+ * (Lanczos, FP64, CTA per right-hand side), iterated until every shift's residual estimate
+ * ||r|| / ||y|| <= tol or k_cap steps.  X: [n_rhs][nz][n] complex128; m_out[r]: Krylov size
+ * used.  Replaces upstream's BiCGSTAB per incoming energy in getRIXSmap (spectra.py:962,1080).
+ * Requires 3 * n * 16 bytes of shared memory <= 200 KiB.
  */
 size_t edgpu_shifted_solve_workspace(int64_t n, int n_rhs, int nz, int k_cap);
 int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
@@ -267,6 +267,16 @@ int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, dou
  */
 int edgpu_cfrac(const double* alpha, const double* beta, const int32_t* k_len, int K, int R, const double* omega,
                 int n_omega, double delta, const double* e, const double* scale, double* g, void* stream);
+
+/*
+ * Continued fractions of edgpu_cfrac in float32 for the mixed-precision form: alpha - e_r and
+ * beta^2 are formed in float64 first (so the common energy offset cancels exactly), then
+ * the fraction is evaluated in float32; results are scaled and stored as complex128.
+ */
+size_t edgpu_cfrac_f32_workspace(int K, int R);
+int edgpu_cfrac_f32(const double* alpha, const double* beta, const int32_t* k_len, int K, int R, const double* omega,
+                    int n_omega, double delta, const double* e, const double* scale, double* g, void* workspace,
+                    size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }
