@@ -267,9 +267,15 @@ __global__ void reorth_alpha_update_kernel(int64_t n, double2* w, const double2*
                                            const double* palpha, int nrb, double* alpha, const double* beta, int j,
                                            double* pnorm) {
   __shared__ double red[256];
-  double a = 0.0;
-  for (int b = 0; b < nrb; ++b) a += palpha[b];
-  if (blockIdx.x == 0 && threadIdx.x == 0) alpha[j] = a;
+  __shared__ double a_s;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nrb; ++b) t += palpha[b];
+    a_s = t;
+    if (blockIdx.x == 0) alpha[j] = t;
+  }
+  __syncthreads();
+  const double a = a_s;
   const double bp = (j > 0) ? beta[j - 1] : 0.0;
   double acc = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -294,6 +300,83 @@ __global__ void reorth_alpha_update_kernel(int64_t n, double2* w, const double2*
   }
 }
 
+// h[k] = <V_k, w> for k < m: one block per k, whole vector, deterministic block tree.
+__global__ void __launch_bounds__(256) dot_per_k_kernel(const double2* __restrict__ V, int m, int64_t n,
+                                                        const double2* __restrict__ w, double2* __restrict__ h) {
+  __shared__ double red_r[8], red_i[8];
+  const int k = blockIdx.x;
+  if (k >= m) return;
+  const double2* vk = V + (int64_t)k * n;
+  double hr = 0.0, hi = 0.0;
+#pragma unroll 4
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 v = vk[i], x = w[i];
+    hr += v.x * x.x + v.y * x.y;
+    hi += v.x * x.y - v.y * x.x;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    hr += __shfl_down_sync(0xffffffffu, hr, o);
+    hi += __shfl_down_sync(0xffffffffu, hi, o);
+  }
+  if (lane == 0) {
+    red_r[warp] = hr;
+    red_i[warp] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      a += red_r[q];
+      b += red_i[q];
+    }
+    h[k] = make_double2(a, b);
+  }
+}
+
+// w -= sum_k h[k] V_k, block = 32 rows x 8 k-residue classes (smem reduction over the 8);
+// with_norm: per-block partial |w|^2 of the updated rows into pnorm[blockIdx.x].
+__global__ void __launch_bounds__(256) project_out_kernel(const double2* __restrict__ V, int m, int64_t n,
+                                                          const double2* __restrict__ h, double2* __restrict__ w,
+                                                          double* __restrict__ pnorm, int with_norm) {
+  __shared__ double2 part[8][32];
+  __shared__ double nrm[32];
+  const int ri = threadIdx.x & 31, kc = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 32 + ri;
+  double2 acc = make_double2(0.0, 0.0);
+  if (i < n) {
+#pragma unroll 4
+    for (int k = kc; k < m; k += 8) {
+      const double2 c = h[k];
+      const double2 v = V[(int64_t)k * n + i];
+      acc.x += c.x * v.x - c.y * v.y;
+      acc.y += c.x * v.y + c.y * v.x;
+    }
+  }
+  part[kc][ri] = acc;
+  __syncthreads();
+  if (kc == 0) {
+    double nr = 0.0;
+    if (i < n) {
+      double2 x = w[i];
+      for (int q = 0; q < 8; ++q) {
+        x.x -= part[q][ri].x;
+        x.y -= part[q][ri].y;
+      }
+      w[i] = x;
+      nr = x.x * x.x + x.y * x.y;
+    }
+    nrm[ri] = nr;
+  }
+  __syncthreads();
+  if (with_norm && threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < 32; ++q) t += nrm[q];
+    pnorm[blockIdx.x] = t;
+  }
+}
+
 __global__ void norm_partial_kernel(int64_t n, const double2* w, double* pnorm) {
   __shared__ double red[256];
   double acc = 0.0;
@@ -312,13 +395,18 @@ __global__ void norm_partial_kernel(int64_t n, const double2* w, double* pnorm) 
 
 __global__ void reorth_normalize_kernel(int64_t n, const double2* w, double2* vnext, const double* pnorm, int nb,
                                         double* beta, int j, int32_t* status) {
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += pnorm[b];
-  const double bt = sqrt(s);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    beta[j] = bt;
-    if (!(bt > 0.0)) atomicExch(status, (int32_t)(bt == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+  __shared__ double bt_s;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += pnorm[b];
+    bt_s = sqrt(s);
+    if (blockIdx.x == 0) {
+      beta[j] = bt_s;
+      if (!(bt_s > 0.0)) atomicExch(status, (int32_t)(bt_s == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+    }
   }
+  __syncthreads();
+  const double bt = bt_s;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 y = w[i];
     vnext[i] = bt > 0.0 ? make_double2(y.x / bt, y.y / bt) : make_double2(0.0, 0.0);
@@ -748,6 +836,7 @@ extern "C" size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap) {
   b += sizeof(double) * (size_t)nrb * 2 + 512;             // alpha/norm partials
   b += sizeof(double2) * (size_t)(K_cap + 1) * nrb + 256;  // dot partials
   b += sizeof(double2) * (size_t)(K_cap + 1) + 256;        // h
+  b += sizeof(double) * (size_t)((n + 31) / 32 + 1) + 256;  // projection-block norm partials
   return b + 1024;
 }
 
@@ -774,7 +863,7 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
   double* pn = reinterpret_cast<double*>(carve(sizeof(double) * nrb));
   double2* pd = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1) * nrb));
   double2* hc = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1)));
-  (void)carve(sizeof(double2) * (size_t)n);
+  double* pnp = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)((n + 31) / 32 + 1)));
   if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
   if (j0 == 0) {
     copy_c128_kernel<<<grid_1d(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0), V, n);
@@ -796,16 +885,17 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
                                                    alpha, beta, j, pn); note_launch();
     if ((rc = check_launch())) return rc;
     if (j + 1 >= K_cap) break;
-    // two passes of classical Gram-Schmidt against V[0..j]
+    // two passes of classical Gram-Schmidt against V[0..j]; the second pass also forms the
+    // per-block partial norms of the final w
     const int m = j + 1;
+    const unsigned prb = (unsigned)((n + 31) / 32);
     for (int pass = 0; pass < 2; ++pass) {
-      dim3 g2(nrb, (m + kDotTile - 1) / kDotTile);
-      multidot_kernel<<<g2, 256, 0, s>>>(V, m, n, w, pd); note_launch();
-      sum_partials_kernel<<<(m + 127) / 128, 128, 0, s>>>(pd, m, nrb, hc); note_launch();
-      subtract_proj_kernel<<<nrb, 256, 0, s>>>(V, m, n, hc, w); note_launch();
+      dot_per_k_kernel<<<m, 256, 0, s>>>(V, m, n, w, hc); note_launch();
+      project_out_kernel<<<prb, 256, 0, s>>>(V, m, n, hc, w, pnp, pass == 1); note_launch();
     }
-    norm_partial_kernel<<<nrb, 256, 0, s>>>(n, w, pn); note_launch();
-    reorth_normalize_kernel<<<nrb, 256, 0, s>>>(n, w, V + (int64_t)(j + 1) * n, pn, nrb, beta, j, status_dev); note_launch();
+    reorth_normalize_kernel<<<nrb, 256, 0, s>>>(n, w, V + (int64_t)(j + 1) * n, pnp, (int)prb, beta, j, status_dev); note_launch();
+    (void)pd;
+    (void)pn;
     if ((rc = check_launch())) return rc;
   }
   return EDGPU_OK;

@@ -502,7 +502,7 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
         return bool(np.all(res <= tol_rel * np.maximum(1.0, np.abs(th[:k]))))
 
     while True:
-        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop)
+        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32)
         kk = len(a)
         th, s, res = residuals(a, bfull, kk)
         exact = kk >= n or (kk < k_cap and bfull[kk - 1] == 0.0)

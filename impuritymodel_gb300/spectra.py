@@ -16,7 +16,9 @@ Krylov space per (in-operator, eigenstate) (full reorthogonalisation, FP64, rela
 residual ``solve_tol``) instead of one BiCGSTAB per energy at rtol 1e-5.
 
 ``precision=1`` selects the mixed form: complex64 Lanczos vectors and H values with
-float32 SpMV accumulation, float64 alpha/beta reductions.
+float32 SpMV accumulation, float64 alpha/beta reductions, float32 continued fractions.
+``precision=2`` keeps the Krylov recurrences in FP64 and evaluates only the continued
+fractions in float32 (after forming alpha - e in FP64).
 """
 
 from __future__ import annotations
@@ -73,7 +75,7 @@ class Sector:
     def __init__(self, eng, dop, restr, start_states, precision=0):
         self.basis, _ = eng.expand(eng.sort_unique(start_states), dop, restr)
         self.csr = eng.build_csr(self.basis, dop, restr)
-        if precision:
+        if precision == 1:
             self.csr.mixed()
         self.n = self.basis.shape[0]
         self._labels = None
@@ -99,7 +101,7 @@ class Sector:
 
 def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
                 sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
-                perturb=None):
+                perturb=None, stages=None):
     """Continued-fraction Green's functions of many start states on one sector.
 
     ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states (lists), or
@@ -130,8 +132,10 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     live = np.nonzero(n2_h > 0)[0]
     if live.size == 0:
         return (g, None) if return_coeffs else g
+    _mark(stages, "green:norms")
     if sector is None:
         sector = Sector(eng, dop, restr, states[n2[run_of_row] > 0], precision)
+    _mark(stages, "green:sector")
     rows = eng.lookup(sector.basis, states)
     if bool((rows < 0).any()):
         raise RuntimeError("start state outside the sector basis")
@@ -157,17 +161,43 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
         gen = torch.Generator(device=eng.device)
         gen.manual_seed(int(seed))
         v0 = v0 * (1.0 + eps * torch.randn(v0.shape, dtype=torch.float64, device=eng.device, generator=gen))
+    _mark(stages, "green:v0")
     dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
     k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
-    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision, timing=timing)
+    _mark(stages, "green:run_dims")
+    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=1 if precision == 1 else 0, timing=timing)
+    _mark(stages, "green:lanczos")
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
-    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live], precision=precision)
+    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live], precision=1 if precision else 0)
+    _mark(stages, "green:cfrac")
     if capture is not None:
         capture.append(dict(csr=sector.csr, v0=v0, k=k_h, e=e_live, scale=scale_h[live], live=live, g=g,
                             omega=omega, delta=delta))
     if return_coeffs:
         return g, (alpha, beta, k_h, live)
     return g
+
+
+class StageTimer:
+    """Optional per-stage wall-clock timing (synchronises the device at each mark)."""
+
+    def __init__(self):
+        self.t = {}
+        self._last = None
+
+    def mark(self, label):
+        torch.cuda.synchronize()
+        import time
+
+        now = time.perf_counter()
+        if self._last is not None:
+            self.t[label] = self.t.get(label, 0.0) + now - self._last
+        self._last = now
+
+
+def _mark(stages, label):
+    if stages is not None:
+        stages.mark(label)
 
 
 def _psi_tensors(eng, psi, n):
@@ -306,8 +336,9 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
 
 def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                 slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-                timing=None, capture=None, perturb=None):
+                timing=None, capture=None, perturb=None, stages=None):
     """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device)."""
+    _mark(stages, "start")
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
     ne, nin, nout, nwi = len(es), len(tin_dops), len(tout_dops), len(wIns)
@@ -323,8 +354,10 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     nonempty = [v[0] for v in psi1.values() if v[0].shape[0]]
     if not nonempty:
         return gs
+    _mark(stages, "rixs:psi1")
     # 2. core-hole sector
     core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
+    _mark(stages, "rixs:core_sector")
     # 3. outgoing operators as sparse maps core basis -> output states
     out_maps = []
     for k in range(nout):
@@ -332,6 +365,7 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
             out_maps.append(out_maps[0])
             continue
         out_maps.append(_transfer_matrix(eng, tout_dops[0] if share_out_memo else tout_dops[k], restr, core.basis))
+    _mark(stages, "rixs:transfer")
     # 4. shifted solves x(z) = (z - H)^{-1} psi1 for every incoming energy and every
     # (t_in, eigenstate) right-hand side
     keys = [k for k, (s1, _) in psi1.items() if s1.shape[0]]
@@ -347,37 +381,47 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     else:
         x_blocks = [_shifted_solutions(eng, core, Y[r], zs[r], solve_tol, min(core.n, max_krylov))
                     for r in range(len(keys))]
-    # 5. psi3 = T_out psi2 for every (t_in, ie, w_in, t_out), pruned and normalised as upstream
+    _mark(stages, "rixs:shifted")
+    # 5. psi3 = T_out psi2 for every (t_in, ie, w_in, t_out), pruned and normalised as upstream:
+    # one SpMV over all (right-hand side, incoming energy) rows per distinct outgoing map
+    X_all = torch.stack(x_blocks).reshape(len(keys) * nwi, core.n)
     st_l, am_l, run_l, e_runs, slots, scales = [], [], [], [], [], []
     run0 = 0
+    pruned = {}
     for k in range(nout):
         tm = out_maps[k]
-        for (t_in, ie), X in zip(keys, x_blocks):
-            P = tm.apply(eng, X)  # [n_wIn, n_out_states] complex128
+        if id(tm) not in pruned:
+            P = tm.apply(eng, X_all)  # [n_rhs * n_wIn, n_out_states] complex128
             a2 = P.real ** 2 + P.imag ** 2
             P = torch.where(a2 >= slaterWeightMin, P, torch.zeros_like(P))
             nrm = torch.sqrt((P.real ** 2 + P.imag ** 2).sum(1, keepdim=True))
             Pn = P / torch.where(nrm > 0, nrm, torch.ones_like(nrm))
             keep = (Pn.real ** 2 + Pn.imag ** 2) >= slaterWeightMin
-            iw_idx, o_idx = torch.nonzero(keep, as_tuple=True)  # row-major: grouped by iw
-            st_l.append(tm.out_states[o_idx])
-            amp = Pn[iw_idx, o_idx]
-            am_l.append(torch.stack([amp.real, amp.imag], 1))
-            run_l.append(iw_idx + run0)
-            scales.append((nrm[:, 0] ** 2).cpu().numpy())
+            row_idx, o_idx = torch.nonzero(keep, as_tuple=True)  # grouped by row
+            amp = Pn[row_idx, o_idx]
+            pruned[id(tm)] = (tm.out_states[o_idx], torch.stack([amp.real, amp.imag], 1), row_idx,
+                              (nrm[:, 0] ** 2).cpu().numpy())
+        st_k, am_k, row_k, sc_k = pruned[id(tm)]
+        st_l.append(st_k)
+        am_l.append(am_k)
+        run_l.append(row_k + run0)
+        scales.append(sc_k)
+        for (t_in, ie) in keys:
             e_runs.extend([es[ie]] * nwi)
             slots.extend((ie, t_in, k, iw) for iw in range(nwi))
-            run0 += nwi
+        run0 += len(keys) * nwi
     packed = (torch.cat(st_l, 0).contiguous(), torch.cat(am_l, 0).contiguous(), torch.cat(run_l, 0), run0)
     scales = np.concatenate(scales)
+    _mark(stages, "rixs:psi3")
     # 6. ground-like sector Lanczos + continued fractions for all runs at once.  Upstream
     # runs getGreen on the normalised-then-pruned psi3 and scales by the squared norm taken
     # before the second pruning (spectra.py:1097-1124).
     g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
-                    normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb)
+                    normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb, stages=stages)
     idx = torch.tensor([((ie * nin + t_in) * nout + k) * nwi + iw for (ie, t_in, k, iw) in slots],
                        device=eng.device)
     gs.view(-1, len(wLoss))[idx] = g
+    _mark(stages, "rixs:assemble")
     return gs
 
 
