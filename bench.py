@@ -518,6 +518,34 @@ def run_hv_only():
     print(json.dumps({"roofline": roof}))
 
 
+def run_profile_step(args):
+    """One pipeline step of the chosen form inside NVTX range 'pipeline_step' (for ncu)."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from impuritymodel_gb300 import _lib
+    from impuritymodel_gb300.engine import get_engine
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    eng = get_engine()
+    lib = _lib.load()
+    pipe = Pipeline(eng)
+    prec = {"plain_fp64": 0, "fp64_krylov_fp32_cfrac": 2, "mixed_c64": 1}[args.form]
+    for _ in range(args.warmup):
+        pipe.step(prec)
+    torch.cuda.synchronize()
+    n0 = lib.edgpu_launch_count()
+    t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("pipeline_step")
+    pipe.step(prec)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"form": args.form, "step_s": round(dt, 5), "library_launches": lib.edgpu_launch_count() - n0}))
+
+
 def traffic_from_profile(roof):
     """DRAM bytes per launch from the committed ncu summary of the same kernel, scaled to
     this launch's algorithmic bytes (ratio measured on the capture)."""
@@ -673,6 +701,10 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--hv-only", action="store_true",
                     help="only the H.v roofline measurement (the case profiled under ncu)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="warm up, then run one pipeline step inside the NVTX range 'pipeline_step'")
+    ap.add_argument("--form", choices=["plain_fp64", "fp64_krylov_fp32_cfrac", "mixed_c64"],
+                    default="fp64_krylov_fp32_cfrac", help="form used by --profile-step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -680,6 +712,8 @@ def main():
         run_reference(args)
     elif args.hv_only:
         run_hv_only()
+    elif args.profile_step:
+        run_profile_step(args)
     else:
         run_gpu(args)
 
