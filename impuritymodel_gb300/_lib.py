@@ -25,6 +25,7 @@ FILTER_NONE = 0
 FILTER_IN_BASIS = 1
 FILTER_NOT_IN_BASIS = 2
 
+ABI_VERSION = 2  # EDGPU_ABI_VERSION in include/edgpu.h
 MAX_RESTRICTIONS = 8
 MAX_WORDS = 8
 EDGPU_LANCZOS_NOALLOC_BYTES = 16 << 20  # size of the library's static scratch array
@@ -60,6 +61,7 @@ class CSR(C.Structure):
         ("val_r", _P),
         ("val_cf", _P),
         ("val_rf", _P),
+        ("val_df", _P),
     ]
 
 

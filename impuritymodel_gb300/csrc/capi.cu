@@ -10,7 +10,7 @@ void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 extern "C" long long edgpu_launch_count(void) { return edgpu::g_launches.load(std::memory_order_relaxed); }
 
-extern "C" int edgpu_abi_version(void) { return 1; }
+extern "C" int edgpu_abi_version(void) { return EDGPU_ABI_VERSION; }
 
 extern "C" const char* edgpu_status_string(int status) {
   switch (status) {

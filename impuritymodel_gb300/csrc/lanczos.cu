@@ -775,7 +775,7 @@ extern "C" int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int 
 
 extern "C" size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision) {
   (void)K;
-  const size_t vs = precision ? sizeof(float2) : sizeof(double2);
+  const size_t vs = precision == 1 ? sizeof(float2) : sizeof(double2);
   RunTile t = make_tile(n > 0 ? n : 1, R > 0 ? R : 1);
   size_t b = 0;
   for (int k = 0; k < 3; ++k) b += ((vs * (size_t)n * R) + 255) & ~(size_t)255;
@@ -783,10 +783,19 @@ extern "C" size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision
   return b + 256;
 }
 
+// The df64 form (precision 3) exists for real H in the shared-memory path; everything else
+// it asks for runs in FP64.
+static int effective_precision(const edgpu_csr* h, int precision) {
+  if (precision != 3) return precision;
+  return (h->val_df && !h->val_c && small_fits(h->n, 3)) ? 3 : 0;
+}
+
 extern "C" int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
                              double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                              void* stream) {
   if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  if (precision < 0 || precision > 3 || precision == 2) return EDGPU_ERR_ARG;
+  precision = effective_precision(h, precision);
   if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
   if (small_fits(h->n, precision))
@@ -802,6 +811,8 @@ extern "C" int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, 
                                    size_t workspace_bytes, void* stream, double* kernel_ms) {
   if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1 || !kernel_ms)
     return EDGPU_ERR_ARG;
+  if (precision < 0 || precision > 3 || precision == 2) return EDGPU_ERR_ARG;
+  precision = effective_precision(h, precision);
   if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
   if (small_fits(h->n, precision)) {
@@ -1059,8 +1070,136 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Double-float ("df64") arithmetic: a value is an unevaluated sum hi + lo of two floats,
+// about 48 significand bits.  Error-free transformations (Knuth's two-sum, Dekker's
+// fast two-sum, the FMA two-product) use __fadd_rn/__fsub_rn/__fmul_rn, which the compiler
+// never contracts into FMAs, so the transformations stay exact.  On GB300 a df64
+// multiply-add costs ~12 FP32 instructions against one FP64 FMA issued at 1/64 of the FP32
+// rate, so it is several times faster than FP64 for the Krylov recurrences.
+// ---------------------------------------------------------------------------------------
+struct dfl {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_split(double a) {
+  const float hi = (float)a;
+  return {hi, (float)(a - (double)hi)};
+}
+
+__device__ __forceinline__ double df_val(dfl a) { return (double)a.hi + (double)a.lo; }
+
+// |a| >= |b| or a == 0
+__device__ __forceinline__ dfl df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// acc + a * b
+__device__ __forceinline__ dfl df_fma(dfl acc, dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  const dfl s = df_two_sum(acc.hi, p);
+  return df_fast_two_sum(s.hi, __fadd_rn(__fadd_rn(s.lo, pe), acc.lo));
+}
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+
+// Upstream's Lanczos recurrence in df64 for a real H (values as hi/lo float pairs); alpha
+// and beta are reduced in FP64 from df64 per-thread partials.  Vectors are float4
+// (re.hi, re.lo, im.hi, im.lo) in shared memory, one CTA per run.
+__global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
+    int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv, int R,
+    const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
+    double* __restrict__ beta, int32_t* status) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  float4* A = reinterpret_cast<float4*>(sm);
+  float4* B = A + n;
+  float4* Cv = B + n;
+  double* red = reinterpret_cast<double*>(Cv + n);
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const dfl zero = {0.f, 0.f};
+  for (int r = blockIdx.x; r < R; r += gridDim.x) {
+    const int km = k_max[r];
+    if (km <= 0) continue;
+    for (int64_t i = tid; i < n; i += bs) {
+      const double2 v = v0[i * R + r];
+      const dfl re = df_split(v.x), im = df_split(v.y);
+      A[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      B[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    float4* x = A;
+    float4* p = B;
+    float4* y = Cv;
+    double bprev = 0.0;
+    for (int j = 0; j < km; ++j) {
+      dfl acc = zero;
+      for (int64_t i = tid; i < n; i += bs) {
+        dfl yr = zero, yi = zero;
+        const int64_t e1 = rp[i + 1];
+        for (int64_t e = rp[i]; e < e1; ++e) {
+          const float2 hh = hv[e];
+          const dfl h = {hh.x, hh.y};
+          const float4 xv = x[col[e]];
+          yr = df_fma(yr, h, {xv.x, xv.y});
+          yi = df_fma(yi, h, {xv.z, xv.w});
+        }
+        y[i] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+        const float4 xi = x[i];
+        acc = df_fma(acc, yr, {xi.x, xi.y});
+        acc = df_fma(acc, yi, {xi.z, xi.w});
+      }
+      const double a = block_sum(df_val(acc), red);
+      if (tid == 0) alpha[(int64_t)r * K + j] = a;
+      if (j + 1 == km) break;
+      const dfl na = df_split(-a), nb = df_split(-bprev);
+      acc = zero;
+      for (int64_t i = tid; i < n; i += bs) {
+        const float4 w = y[i], xi = x[i], pi = p[i];
+        const dfl wr = df_fma(df_fma({w.x, w.y}, na, {xi.x, xi.y}), nb, {pi.x, pi.y});
+        const dfl wi = df_fma(df_fma({w.z, w.w}, na, {xi.z, xi.w}), nb, {pi.z, pi.w});
+        y[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+        acc = df_fma(acc, wr, wr);
+        acc = df_fma(acc, wi, wi);
+      }
+      const double b = sqrt(block_sum(df_val(acc), red));
+      if (tid == 0) {
+        beta[(int64_t)r * K + j] = b;
+        if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+      }
+      const dfl ib = df_split(b > 0.0 ? 1.0 / b : 0.0);
+      for (int64_t i = tid; i < n; i += bs) {
+        const float4 w = y[i];
+        const dfl vr = df_mul({w.x, w.y}, ib), vi = df_mul({w.z, w.w}, ib);
+        p[i] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);  // v_{j-1}'s buffer becomes v_{j+1}
+      }
+      __syncthreads();
+      float4* t = p;
+      p = x;
+      x = t;
+      bprev = b;
+    }
+    __syncthreads();
+  }
+}
+
 size_t small_smem_bytes(int64_t n, int precision) {
-  const size_t v = precision ? sizeof(float2) : sizeof(double2);
+  const size_t v = precision == 1 ? sizeof(float2) : sizeof(double2);  // df64 rows are float4
   return 3 * v * (size_t)n + 34 * sizeof(double) + 16;
 }
 
@@ -1083,8 +1222,29 @@ int launch_small(const edgpu_csr* h, const T* vals, const double* v0, int R, con
   return check_launch();
 }
 
+int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
+                    double* beta, int32_t* status, cudaStream_t s) {
+  const size_t smem = small_smem_bytes(h->n, 3);
+  cudaFuncSetAttribute(lanczos_small_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_small_df_kernel, kSmallThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  int grid = grid_cap() * per_sm;
+  if (grid > R) grid = R;
+  lanczos_small_df_kernel<<<grid, kSmallThreads, smem, s>>>(h->n, h->row_ptr, h->col,
+                                                            reinterpret_cast<const float2*>(h->val_df), R,
+                                                            reinterpret_cast<const double2*>(v0), k_max, K, alpha,
+                                                            beta, status);
+  note_launch();
+  return check_launch();
+}
+
 int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
                   double* alpha, double* beta, int32_t* status, cudaStream_t s) {
+  if (precision == 3) {
+    if (h->val_df && !h->val_c) return launch_small_df(h, v0, R, k_max, K, alpha, beta, status, s);
+    precision = 0;  // complex H: FP64
+  }
   if (precision == 0) {
     if (h->val_c) return launch_small<double, true>(h, h->val_c, v0, R, k_max, K, alpha, beta, status, 0, s);
     return launch_small<double, false>(h, h->val_r, v0, R, k_max, K, alpha, beta, status, 0, s);
@@ -1391,6 +1551,7 @@ int noalloc_scratch_address(void** out) {
 extern "C" int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K,
                                      int precision, double* alpha, double* beta, int32_t* status_dev, void* stream) {
   if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  if (precision == 3) precision = 0;  // the df64 form has no grid-wide variant
   if (precision == 0 && !h->val_c && !h->val_r) return EDGPU_ERR_ARG;
   if (precision != 0 && !h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
   if (edgpu_lanczos_workspace(h->n, R, K, precision) > (size_t)EDGPU_LANCZOS_NOALLOC_BYTES)

@@ -100,6 +100,7 @@ class CsrMatrix:
         self.val_r = val_r
         self.val_cf = None
         self.val_rf = None
+        self.val_df = None
         self.mixed_shift = 0.0
         self.n = row_ptr.numel() - 1
         self.ncols = self.n if ncols is None else int(ncols)
@@ -133,6 +134,20 @@ class CsrMatrix:
         self._struct = None
         return self
 
+    def double_float(self):
+        """Add the (hi, lo) float-pair copy of a real H used by the double-float Lanczos form.
+
+        hi = fl32(h), lo = fl32(h - hi): hi + lo equals h to about 2^-48 relative, so no
+        shift is needed.  Complex matrices keep no copy (the form then runs in FP64).
+        """
+        if self.val_df is not None or self.val_r is None:
+            return self
+        hi = self.val_r.to(torch.float32)
+        lo = (self.val_r - hi.to(torch.float64)).to(torch.float32)
+        self.val_df = torch.stack([hi, lo], dim=1).contiguous()
+        self._struct = None
+        return self
+
     def struct(self):
         if self._struct is None:
             s = L.CSR()
@@ -146,6 +161,7 @@ class CsrMatrix:
                 s.val_r = self.row_ptr.data_ptr()
             s.val_cf = self.val_cf.data_ptr() if self.val_cf is not None and self.nnz else None
             s.val_rf = self.val_rf.data_ptr() if self.val_rf is not None and self.nnz else None
+            s.val_df = self.val_df.data_ptr() if self.val_df is not None and self.nnz else None
             self._struct = s
         return self._struct
 
@@ -456,8 +472,12 @@ class Engine:
         K = int(kmax.max().item())
         alpha = torch.zeros((r, K), dtype=torch.float64, device=self.device)
         beta = torch.zeros((r, K), dtype=torch.float64, device=self.device)
-        if precision:
+        if precision == 1:
             csr.mixed()
+        elif precision == 3:
+            csr.double_float()
+        elif precision != 0:
+            raise ValueError("lanczos: precision must be 0, 1 or 3")
         v0r = torch.view_as_real(v0.contiguous()) if v0.is_complex() else v0
         ws, wsn = self.workspace(self.lib.edgpu_lanczos_workspace(n, r, K, precision))
         self.reset_status()
@@ -470,12 +490,12 @@ class Engine:
             L.check(self.lib.edgpu_lanczos_timed(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
                                                  _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream,
                                                  ms), "lanczos_timed")
-            vb = 8 if precision else 16
-            sb = (4 if precision else 8) * (2 if csr.val_c is not None else 1)
+            vb = 8 if precision == 1 else 16
+            sb = (4 if precision == 1 else 8) * (2 if csr.val_c is not None else 1)
             timing.append(dict(n=csr.n, nnz=csr.nnz, R=r, K=K, precision=precision, spmm_ms=ms[0], axpy_ms=ms[1],
                                normalize_ms=ms[2], spmm_launches=K, vec_bytes=vb, val_bytes=sb))
         self.read_status("lanczos")
-        if precision and csr.mixed_shift:
+        if precision == 1 and csr.mixed_shift:
             alpha += csr.mixed_shift  # Lanczos ran on H - shift*I
         return alpha, beta
 

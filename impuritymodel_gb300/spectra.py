@@ -19,6 +19,9 @@ residual ``solve_tol``) instead of one BiCGSTAB per energy at rtol 1e-5.
 float32 SpMV accumulation, float64 alpha/beta reductions, float32 continued fractions.
 ``precision=2`` keeps the Krylov recurrences in FP64 and evaluates only the continued
 fractions in float32 (after forming alpha - e in FP64).
+``precision=3`` runs the Lanczos recurrences of real Hamiltonians in double-float
+arithmetic (unevaluated float pairs, ~48 significand bits, FP64 alpha/beta reductions) and
+the continued fractions in float32 as in ``precision=2``.
 """
 
 from __future__ import annotations
@@ -165,7 +168,8 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
     k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
     _mark(stages, "green:run_dims")
-    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=1 if precision == 1 else 0, timing=timing)
+    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision if precision in (1, 3) else 0,
+                              timing=timing)
     _mark(stages, "green:lanczos")
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
     g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live], precision=1 if precision else 0)

@@ -80,8 +80,12 @@ typedef struct edgpu_csr {
   const double* val_r;  /* real float64 values (used when val_c is NULL) */
   const float* val_cf;  /* complex64 copy for the mixed-precision form, or NULL */
   const float* val_rf;  /* float32 copy for the mixed-precision form, or NULL */
+  const float* val_df;  /* real values as (hi, lo) float pairs, hi + lo = value to ~2^-48
+                           relative, for the double-float Lanczos form; or NULL */
 } edgpu_csr;
 
+/* Bumped whenever a struct layout or a signature changes. */
+#define EDGPU_ABI_VERSION 2
 int edgpu_abi_version(void);
 const char* edgpu_status_string(int status);
 
@@ -186,7 +190,10 @@ int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* st
  * k_max[R]: per-run Krylov size (upstream min(krylovSize, dim of the run's basis)).
  * K = max over k_max.  Outputs alpha[R][K], beta[R][K] (beta[r][j] for j < k_max[r]-1).
  * precision: 0 = complex128 vectors and values; 1 = complex64 vectors, float32 SpMV
- * accumulation, float64 alpha/beta reductions.  Breakdown (beta == 0 before k_max) sets
+ * accumulation, float64 alpha/beta reductions; 3 = double-float vectors and values
+ * (each number an unevaluated sum of two floats, ~48 significand bits, from h->val_df),
+ * float64 alpha/beta reductions, for real H in the shared-memory path; precision 3
+ * anywhere else runs as 0.  Breakdown (beta == 0 before k_max) sets
  * *status_dev = EDGPU_ERR_BREAKDOWN.  Sectors whose three Krylov vectors fit in shared
  * memory run as one persistent launch with one CTA per run; larger ones as three
  * grid-wide kernels per step.

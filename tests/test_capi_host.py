@@ -37,7 +37,11 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.edgpu_abi_version() == 1
+    from impuritymodel_gb300 import _lib as L
+
+    assert lib.edgpu_abi_version() == L.ABI_VERSION == 2
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "edgpu.h")).read()
+    assert "#define EDGPU_ABI_VERSION %d" % L.ABI_VERSION in hdr
     assert lib.edgpu_status_string(0) == b"ok"
     assert b"breakdown" in lib.edgpu_status_string(3).lower()
 

@@ -187,3 +187,53 @@ def test_rixs_against_oracle(eng, c1):
     ens = _ensemble(lambda perturb: O.get_rixs_map(*args, solver="direct", perturb=perturb), members=3)
     # against upstream's own BiCGSTAB (rtol 1e-5) map: its noise floor
     _accuracy_class(gs, ens, exact, z["gs_rixs"])
+
+
+def test_double_float_lanczos_tracks_fp64(eng, c1):
+    """The double-float Lanczos (precision 3, ~48-bit significands) on the 60-state sector of
+    the golden Lanczos case: the first 20 alpha/beta agree with upstream's at 1e-9 like the
+    FP64 form, and the continued fraction (K = dim) at 1e-6."""
+    z = c1["z"]
+    n = c1["n"]
+    psi1 = decode_psi(z, "psi1", n)
+    dop = finite._device_op(c1["hop"], eng)
+    restr = spectra.make_restrictions(c1["restr"], n)
+    st, am = spectra._psi_tensors(eng, psi1, n)
+    out = {}
+    for prec in (0, 3):
+        _, (alpha, beta, k_h, _) = spectra.green_batch(eng, dop, restr, [st], [am], [0.0], [0.0], 0.1, 150, prec,
+                                                       return_coeffs=True)
+        out[prec] = (alpha.cpu().numpy()[0, : k_h[0]], beta.cpu().numpy()[0, : k_h[0]])
+    a3, b3 = out[3]
+    assert a3.shape == z["alpha"].shape
+    assert np.abs(a3[:20] - z["alpha"][:20]).max() < 1e-9
+    assert np.abs(b3[:20] - z["beta"][:20]).max() < 1e-9
+    assert np.abs(a3[:20] - out[0][0][:20]).max() < 1e-9
+    w = np.linspace(-30, 30, 1500)
+    g = O.continued_fraction(a3, b3, w, 0.1, -700.0)
+    g_ref = O.continued_fraction(z["alpha"], z["beta"], w, 0.1, -700.0)
+    assert _rel(g, g_ref) < SPEC_RTOL
+
+
+@pytest.mark.parametrize("precision", [2, 3])
+def test_reduced_forms_accuracy(eng, c1, precision):
+    """FP32 continued fractions (2) and double-float Lanczos with FP32 continued fractions
+    (3): XAS against upstream at 1e-5 relative (float32 resolvents), PS and RIXS in the
+    same accuracy class against the exact resolvent as the FP64 form."""
+    z = c1["z"]
+    from impuritymodel_gb300 import models as M
+
+    mod = M.make_model("config1")
+    n, hop, restr, psis, es = c1["n"], c1["hop"], c1["restr"], c1["psis"], c1["es"]
+    gs = spectra.getSpectra(n, hop, mod.xas_ops(), psis, es, z["w"], 0.1, restr, precision=precision)
+    assert _rel(gs, z["gs_xas"]) < 1e-5
+    args = (n, hop, mod.ps_ops()[:3], psis, es, -z["w"], -0.1, restr)
+    gs = spectra.getSpectra(*args, precision=precision)
+    gx = O.get_spectra(*args, exact=True)
+    ens = _ensemble(lambda perturb: O.get_spectra(*args, perturb=perturb))
+    _accuracy_class(gs, ens, gx, z["gs_ps"])
+    rargs = (n, hop, mod.xas_ops(), mod.rixs_out_ops(), psis[:1], es[:1], z["w_in"], z["w_loss"], 0.2, 0.05, restr)
+    gr = spectra.getRIXSmap(*rargs, precision=precision)
+    exact = O.get_rixs_map(*rargs, solver="direct", exact=True)
+    ens = _ensemble(lambda perturb: O.get_rixs_map(*rargs, solver="direct", perturb=perturb), members=3)
+    _accuracy_class(gr, ens, exact, z["gs_rixs"])
