@@ -532,11 +532,14 @@ struct Vec16<double> {
   static constexpr int runs = 1;
 };
 
+constexpr int kRowsThreads = 128;  // smaller blocks shorten the tail of ragged rows
+
 template <typename T, bool VALC>
-__global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t* __restrict__ rp,
-                                                        const int32_t* __restrict__ col, const T* __restrict__ vals,
-                                                        int R, int L, const typename Cx<T>::V* __restrict__ X,
-                                                        typename Cx<T>::V* __restrict__ Y) {
+__global__ void __launch_bounds__(kRowsThreads) spmm_rows_kernel(int64_t n, const int64_t* __restrict__ rp,
+                                                                 const int32_t* __restrict__ col,
+                                                                 const T* __restrict__ vals, int R, int L,
+                                                                 const typename Cx<T>::V* __restrict__ X,
+                                                                 typename Cx<T>::V* __restrict__ Y) {
   using Q = typename Vec16<T>::type;
   constexpr int RV = Vec16<T>::runs;
   constexpr int UNROLL = 8;
@@ -548,26 +551,29 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t
   T ar[RV], ai[RV];
 #pragma unroll
   for (int q = 0; q < RV; ++q) ar[q] = ai[q] = 0;
-  const int64_t e0 = __ldg(rp + i), e1 = __ldg(rp + i + 1);
-  int64_t e = e0;
-  for (; e + UNROLL <= e1; e += UNROLL) {
+  const int64_t e1 = __ldg(rp + i + 1);
+  // Batches of UNROLL entries, the last one predicated: every row needs at most three
+  // dependent memory round trips per batch (row pointers, CSR entries, gathers of x).
+  for (int64_t e = __ldg(rp + i); e < e1; e += UNROLL) {
     int c[UNROLL];
     T hr[UNROLL], hi[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
+      const bool ok = e + u < e1;
       // CSR entries are read once: streaming loads keep x resident in L2
-      c[u] = __ldcs(col + e + u);
+      c[u] = ok ? __ldcs(col + e + u) : 0;
       if (VALC) {
-        hr[u] = __ldcs(vals + 2 * (e + u));
-        hi[u] = __ldcs(vals + 2 * (e + u) + 1);
+        hr[u] = ok ? __ldcs(vals + 2 * (e + u)) : T(0);
+        hi[u] = ok ? __ldcs(vals + 2 * (e + u) + 1) : T(0);
       } else {
-        hr[u] = __ldcs(vals + e + u);
+        hr[u] = ok ? __ldcs(vals + e + u) : T(0);
         hi[u] = 0;
       }
     }
     Q xv[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) xv[u] = __ldg(reinterpret_cast<const Q*>(X + (int64_t)c[u] * R + r0));
+    for (int u = 0; u < UNROLL; ++u)
+      xv[u] = (e + u < e1) ? __ldg(reinterpret_cast<const Q*>(X + (int64_t)c[u] * R + r0)) : Q{};
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       const T* xs = reinterpret_cast<const T*>(&xv[u]);
@@ -581,24 +587,6 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(int64_t n, const int64_t
           ai[q] += hi[u] * xr;
         }
       }
-    }
-  }
-  for (; e < e1; ++e) {
-    const int c = __ldg(col + e);
-    T hr, hi = 0;
-    if (VALC) {
-      hr = __ldg(vals + 2 * e);
-      hi = __ldg(vals + 2 * e + 1);
-    } else {
-      hr = __ldg(vals + e);
-    }
-    const Q xv = __ldg(reinterpret_cast<const Q*>(X + (int64_t)c * R + r0));
-    const T* xs = reinterpret_cast<const T*>(&xv);
-#pragma unroll
-    for (int q = 0; q < RV; ++q) {
-      const T xr = xs[2 * q], xi = xs[2 * q + 1];
-      ar[q] += hr * xr - hi * xi;
-      ai[q] += hr * xi + hi * xr;
     }
   }
   Q out;
@@ -617,17 +605,18 @@ int spmv_impl(const edgpu_csr* h, const typename Cx<T>::V* x, typename Cx<T>::V*
   if (R % RV == 0) {
     const int L = R / RV;
     const int64_t threads = h->n * (int64_t)L;
-    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    const unsigned blocks = (unsigned)((threads + kRowsThreads - 1) / kRowsThreads);
+    const int bt = kRowsThreads;
     if (sizeof(T) == 8) {
       if (h->val_c)
-        spmm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_c, R, L, x, y);
+        spmm_rows_kernel<T, true><<<blocks, bt, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_c, R, L, x, y);
       else
-        spmm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_r, R, L, x, y);
+        spmm_rows_kernel<T, false><<<blocks, bt, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_r, R, L, x, y);
     } else {
       if (h->val_cf)
-        spmm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_cf, R, L, x, y);
+        spmm_rows_kernel<T, true><<<blocks, bt, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_cf, R, L, x, y);
       else
-        spmm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_rf, R, L, x, y);
+        spmm_rows_kernel<T, false><<<blocks, bt, 0, s>>>(h->n, h->row_ptr, h->col, (const T*)h->val_rf, R, L, x, y);
     }
     note_launch();
     return check_launch();
