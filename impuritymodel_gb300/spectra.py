@@ -321,8 +321,9 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
 
     ``share_out_memo=True`` reproduces upstream's single memo dict shared by all outgoing
     operators (``tOut_big = [{}] * len(tOpsOut)``): every product state's outgoing action
-    is the one of ``tOpsOut[0]``, the first operator to meet it.  ``False`` applies each
-    outgoing operator itself.
+    is the one of ``tOpsOut[0]``, the first operator to meet it, so all outgoing slices are
+    equal; their final-state Green's functions are computed once and copied.  ``False``
+    applies each outgoing operator itself.
     """
     if parallelization_mode not in ("serial", "H_build", "wIn", "H_build_wIn"):
         raise Exception("Incorrect value of variable parallelization_mode.")
@@ -392,8 +393,13 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     st_l, am_l, run_l, e_runs, slots, scales = [], [], [], [], [], []
     run0 = 0
     pruned = {}
+    alias = {}  # outgoing channel -> earlier channel with the same map (identical spectra)
     for k in range(nout):
         tm = out_maps[k]
+        first = next(k0 for k0 in range(k + 1) if out_maps[k0] is tm)
+        if first != k:
+            alias[k] = first
+            continue
         if id(tm) not in pruned:
             P = tm.apply(eng, X_all)  # [n_rhs * n_wIn, n_out_states] complex128
             a2 = P.real ** 2 + P.imag ** 2
@@ -425,6 +431,8 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     idx = torch.tensor([((ie * nin + t_in) * nout + k) * nwi + iw for (ie, t_in, k, iw) in slots],
                        device=eng.device)
     gs.view(-1, len(wLoss))[idx] = g
+    for k, k0 in alias.items():
+        gs[:, :, k] = gs[:, :, k0]
     _mark(stages, "rixs:assemble")
     return gs
 
