@@ -8,6 +8,7 @@
 // Vectors of a batch are stored [n][R] (run index fastest) so that the R threads of one
 // row read the row's CSR entries once (broadcast) and gather x[col][0..R) contiguously.
 // All reductions are deterministic: per-block partials in fixed order, summed in fixed order.
+#include <atomic>
 #include <vector>
 
 #include "common.cuh"
@@ -829,6 +830,16 @@ extern "C" int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, 
                              kernel_ms);
 }
 
+namespace edgpu {
+size_t reorth_coop_scratch_bytes();
+int lanczos_reorth_coop(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* Vd, double* wd,
+                        double* alpha, double* beta, int32_t* status_dev, double* scratch, double2* hc,
+                        cudaStream_t s);
+}  // namespace edgpu
+static std::atomic<int> g_reorth_fused{1};
+
+extern "C" void edgpu_set_reorth_fused(int enabled) { g_reorth_fused.store(enabled ? 1 : 0); }
+
 extern "C" size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap) {
   const int64_t nrb = grid_1d(n > 0 ? n : 1, 256);
   size_t b = 0;
@@ -837,8 +848,10 @@ extern "C" size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap) {
   b += sizeof(double2) * (size_t)(K_cap + 1) * nrb + 256;  // dot partials
   b += sizeof(double2) * (size_t)(K_cap + 1) + 256;        // h
   b += sizeof(double) * (size_t)((n + 31) / 32 + 1) + 256;  // projection-block norm partials
+  b += reorth_coop_scratch_bytes() + 256;                   // per-block partials of the fused form
   return b + 1024;
 }
+
 
 extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* Vd,
                                     double* wd, double* alpha, double* beta, int32_t* status_dev, void* workspace,
@@ -848,6 +861,7 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
   if (j0 == 0 && !v0) return EDGPU_ERR_ARG;
   if (workspace_bytes < edgpu_lanczos_reorth_workspace(h->n, K_cap)) return EDGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
+  if (j0 == j1) return EDGPU_OK;
   const int64_t n = h->n;
   double2* V = reinterpret_cast<double2*>(Vd);
   double2* w = reinterpret_cast<double2*>(wd);
@@ -864,7 +878,12 @@ extern "C" int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0
   double2* pd = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1) * nrb));
   double2* hc = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)(K_cap + 1)));
   double* pnp = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)((n + 31) / 32 + 1)));
+  double* coop = reinterpret_cast<double*>(carve(reorth_coop_scratch_bytes()));
   if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
+  if (g_reorth_fused.load()) {
+    const int rcc = lanczos_reorth_coop(h, v0, j0, j1, K_cap, Vd, wd, alpha, beta, status_dev, coop, hc, s);
+    if (rcc >= 0) return rcc;
+  }
   if (j0 == 0) {
     copy_c128_kernel<<<grid_1d(n, 256), 256, 0, s>>>(reinterpret_cast<const double2*>(v0), V, n);
     note_launch();

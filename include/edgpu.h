@@ -245,11 +245,18 @@ int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int
  * (finite.py:105) and the BiCGSTAB solves of ``getRIXSmap`` (spectra.py:962,1080) through
  * Ritz pairs and shifted tridiagonal solves on the host.
  * w: work vector [n] complex128 (carries H v_{j} - ... between calls).
+ * Sectors with n <= 65536 run each call as one cooperative launch (one block per SM, the
+ * phases of a step separated by grid barriers); larger ones, or devices without cooperative
+ * launch, as seven grid-wide kernels per step.
  */
 size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap);
 int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
                          double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                          void* stream);
+/* Process-wide switch (default 1): 0 sends every edgpu_lanczos_reorth call to the
+ * per-step kernels (both paths compute the same recurrence; used to test one against the
+ * other).  No counterpart in upstream impurityModel. */
+void edgpu_set_reorth_fused(int enabled);
 
 /*
  * Shifted solves X[r][z] = (zs[r][z] - H)^{-1} Y[r] for n_rhs right-hand sides (Y: [n_rhs][n]
