@@ -51,6 +51,17 @@ class Restrictions(C.Structure):
     ]
 
 
+class Ragged(C.Structure):
+    _fields_ = [
+        ("n_sectors", _I),
+        ("n_runs", _I),
+        ("sec_row0", _P),
+        ("run_sec", _P),
+        ("run_vec0", _P),
+        ("max_rows", _I64),
+    ]
+
+
 class CSR(C.Structure):
     _fields_ = [
         ("n", _I64),
@@ -95,6 +106,11 @@ SIGNATURES = {
     "edgpu_shifted_solve_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_shifted_solve": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_combine": (_I, [_P, _I, _I64, _P, _I, _P, _P]),
+    "edgpu_lanczos_ragged_smem": (_SZ, [_I64]),
+    "edgpu_lanczos_ragged": (_I, [C.POINTER(CSR), C.c_void_p, _P, _P, _I, _P, _P, _P, _P]),
+    "edgpu_lanczos_reorth_ragged_smem": (_SZ, [_I64, _I]),
+    "edgpu_lanczos_reorth_ragged": (_I, [C.POINTER(CSR), C.c_void_p, _P, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "edgpu_combine_ragged": (_I, [_P, C.c_void_p, _P, _P, _P, _I, _I, _P, _P]),
     "edgpu_cfrac": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P]),
     "edgpu_cfrac_f32_workspace": (_SZ, [_I, _I]),
     "edgpu_cfrac_f32": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P, _SZ, _P]),

@@ -613,6 +613,74 @@ class Engine:
                                        _ptr(torch.view_as_real(X)), self.stream), "combine")
         return X
 
+    # -- ragged batches (sectors of many models, one launch per solve) ---------------------
+    def lanczos_ragged(self, batch, v0, k_max, alpha=None, beta=None, check=True):
+        """Upstream's Lanczos for every run of a RaggedBatch; v0 packed complex128 [sum n_r].
+
+        ``k_max`` is a host array or a device int32 tensor; with preallocated ``alpha``/
+        ``beta`` and ``check=False`` the call enqueues work only (no host synchronisation),
+        so it can be captured in a CUDA graph."""
+        if torch.is_tensor(k_max):
+            kmax = k_max
+            K = alpha.shape[1]
+        else:
+            k_h = np.asarray(k_max, dtype=np.int32)
+            K = int(k_h.max()) if k_h.size else 1
+            kmax = torch.from_numpy(k_h).to(self.device)
+        if alpha is None:
+            alpha = torch.zeros((batch.n_runs, K), dtype=torch.float64, device=self.device)
+            beta = torch.zeros((batch.n_runs, K), dtype=torch.float64, device=self.device)
+        self.reset_status()
+        L.check(self.lib.edgpu_lanczos_ragged(C.byref(batch.csr.struct()), C.byref(batch.struct()),
+                                              _ptr(torch.view_as_real(v0)), _ptr(kmax), K, _ptr(alpha), _ptr(beta),
+                                              _ptr(self.status), self.stream), "lanczos_ragged")
+        if check:
+            self.read_status("lanczos_ragged")
+        return alpha, beta
+
+    def lanczos_reorth_ragged(self, batch, v0, k_max):
+        """Reorthogonalised Lanczos for every run of a RaggedBatch (one launch).
+
+        Returns (V packed complex128, run_V0 host offsets, alpha, beta) with run r's basis
+        ``V[run_V0[r] : run_V0[r] + k_max[r] * n_r]`` as [k_max[r], n_r]."""
+        k_h = np.asarray(k_max, dtype=np.int32)
+        K = int(k_h.max()) if k_h.size else 1
+        sizes = batch.run_rows_h
+        run_V0 = np.zeros(batch.n_runs + 1, dtype=np.int64)
+        np.cumsum(k_h.astype(np.int64) * sizes, out=run_V0[1:])
+        V = torch.empty(int(run_V0[-1]), dtype=torch.complex128, device=self.device)
+        rv = torch.from_numpy(run_V0).to(self.device)
+        kmax = torch.from_numpy(k_h).to(self.device)
+        alpha = torch.zeros((batch.n_runs, K), dtype=torch.float64, device=self.device)
+        beta = torch.zeros((batch.n_runs, K), dtype=torch.float64, device=self.device)
+        self.reset_status()
+        L.check(self.lib.edgpu_lanczos_reorth_ragged(C.byref(batch.csr.struct()), C.byref(batch.struct()),
+                                                     _ptr(torch.view_as_real(v0)), _ptr(kmax), K, _ptr(rv),
+                                                     _ptr(torch.view_as_real(V)), _ptr(alpha), _ptr(beta),
+                                                     _ptr(self.status), self.stream), "lanczos_reorth_ragged")
+        self.read_status("lanczos_reorth_ragged")
+        return V, run_V0, alpha, beta
+
+    def combine_ragged(self, batch, V, run_V0, k_len, S):
+        """Ritz vectors X[r][q] = sum_k S[r, k, q] V_r[k]; returns packed [Q * sum n_r]."""
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        R, K, Q = S.shape
+        s_t = torch.from_numpy(S).to(self.device)
+        rv = torch.from_numpy(np.asarray(run_V0, dtype=np.int64)).to(self.device)
+        kl = torch.from_numpy(np.asarray(k_len, dtype=np.int32)).to(self.device)
+        X = torch.empty(Q * int(batch.run_vec0_h[-1]), dtype=torch.complex128, device=self.device)
+        L.check(self.lib.edgpu_combine_ragged(_ptr(torch.view_as_real(V)), C.byref(batch.struct()), _ptr(rv),
+                                              _ptr(kl), _ptr(s_t), K, Q, _ptr(torch.view_as_real(X)), self.stream),
+                "combine_ragged")
+        return X
+
+    def cfrac_device(self, alpha, beta, kl, om, delta, e, sc, g):
+        """Continued fractions with every input already on the device (capturable)."""
+        r, K = alpha.shape
+        L.check(self.lib.edgpu_cfrac(_ptr(alpha), _ptr(beta), _ptr(kl), K, r, _ptr(om), om.numel(), float(delta),
+                                     _ptr(e), _ptr(sc), _ptr(torch.view_as_real(g)), self.stream), "cfrac")
+        return g
+
 
 _ENGINES = {}
 

@@ -102,39 +102,53 @@ class Sector:
         return dims
 
 
-def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
-                sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
-                perturb=None, stages=None):
-    """Continued-fraction Green's functions of many start states on one sector.
+class GreenSetup:
+    """Start vectors of a batch of Green's-function runs on one sector (see green_setup)."""
+
+    def __init__(self, runs, live, sector, v0, k, scale):
+        self.runs = runs  # runs requested
+        self.live = live  # host indices of runs with a nonzero start state
+        self.sector = sector
+        self.v0 = v0  # [sector.n, len(live)] complex128
+        self.k = k  # host Krylov sizes of the live runs
+        self.scale = scale  # host scale of every run (normalisation**2 or the given scales)
+
+
+def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision=0, sector=None, normalize=True,
+                scales=None, perturb=None, stages=None):
+    """Sector, start vectors and Krylov sizes of a batch of Green's-function runs.
 
     ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states (lists), or
     ``run_states`` is a packed ``(states [M, W], amps [M, 2], run_of_row [M], n_runs)``
     tuple with ``run_amps`` None.  With ``normalize=True`` each start state is normalised
-    before the Lanczos and the result scaled by its squared norm (upstream
+    and its squared norm becomes the run's scale (upstream
     ``normalization**2 * getGreen(psi / normalization)``, spectra.py:786-802).  With
-    ``normalize=False`` the Lanczos starts from the amplitudes as given (upstream getGreen
-    on an arbitrary psi) and the result is scaled by ``scales[r]`` (default 1).
-    Returns g [R, n_omega] complex128 (device).
+    ``normalize=False`` the start states are used as given (upstream getGreen on an arbitrary
+    psi) and ``scales[r]`` (default 1) is the scale.  Each run's Krylov size is upstream's
+    ``min(krylovSize, dim of its own closure)``.  Returns a GreenSetup, or None when every
+    start state is empty.
     """
-    omega = np.asarray(omega, dtype=np.float64)
     if run_amps is None:
         states, amps, run_of_row, runs = run_states
     else:
         runs = len(run_states)
         if runs == 0:
-            return torch.zeros((0, len(omega)), dtype=torch.complex128, device=eng.device)
+            return None
         sizes = torch.tensor([int(x.shape[0]) for x in run_states], device=eng.device)
         states = torch.cat(run_states, 0)
         amps = torch.cat(run_amps, 0)
         run_of_row = torch.repeat_interleave(torch.arange(runs, device=eng.device), sizes)
     n2 = torch.zeros(runs, dtype=torch.float64, device=eng.device)
     if amps.shape[0]:
-        n2.index_add_(0, run_of_row, amps[:, 0] ** 2 + amps[:, 1] ** 2)
+        # per-run squared norms as segment sums in a fixed order (rows are grouped by run), so
+        # reruns give identical bits (an atomic scatter-add would not)
+        a2 = torch.stack([amps[:, 0] ** 2 + amps[:, 1] ** 2, torch.zeros_like(amps[:, 0])], 1).contiguous()
+        rk, _, s2 = eng.unique_sorted(run_of_row.view(-1, 1).contiguous(), None, a2)
+        n2[rk[:, 0]] = s2[:, 0]
     n2_h = n2.cpu().numpy()
-    g = torch.zeros((runs, len(omega)), dtype=torch.complex128, device=eng.device)
     live = np.nonzero(n2_h > 0)[0]
     if live.size == 0:
-        return (g, None) if return_coeffs else g
+        return None
     _mark(stages, "green:norms")
     if sector is None:
         sector = Sector(eng, dop, restr, states[n2[run_of_row] > 0], precision)
@@ -168,14 +182,34 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
     k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
     _mark(stages, "green:run_dims")
-    alpha, beta = eng.lanczos(sector.csr, v0, k_h, precision=precision if precision in (1, 3) else 0,
+    return GreenSetup(runs, live, sector, v0, k_h, scale_h)
+
+
+def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
+                sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
+                perturb=None, stages=None):
+    """Continued-fraction Green's functions of many start states on one sector.
+
+    Arguments as :func:`green_setup`; ``e_runs[r]`` is the energy added to the frequency of
+    run r.  Returns g [R, n_omega] complex128 (device).
+    """
+    omega = np.asarray(omega, dtype=np.float64)
+    st = green_setup(eng, dop, restr, run_states, run_amps, krylovSize, precision, sector, normalize, scales,
+                     perturb, stages)
+    runs = len(run_states) if run_amps is not None else run_states[3]
+    g = torch.zeros((runs, len(omega)), dtype=torch.complex128, device=eng.device)
+    if st is None:
+        return (g, None) if return_coeffs else g
+    live, k_h = st.live, st.k
+    alpha, beta = eng.lanczos(st.sector.csr, st.v0, k_h, precision=precision if precision in (1, 3) else 0,
                               timing=timing)
     _mark(stages, "green:lanczos")
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
-    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, scale_h[live], precision=1 if precision else 0)
+    live_t = torch.from_numpy(live).to(eng.device)
+    g[live_t] = eng.cfrac(alpha, beta, k_h, omega, delta, e_live, st.scale[live], precision=1 if precision else 0)
     _mark(stages, "green:cfrac")
     if capture is not None:
-        capture.append(dict(csr=sector.csr, v0=v0, k=k_h, e=e_live, scale=scale_h[live], live=live, g=g,
+        capture.append(dict(csr=st.sector.csr, v0=st.v0, k=k_h, e=e_live, scale=st.scale[live], live=live, g=g,
                             omega=omega, delta=delta))
     if return_coeffs:
         return g, (alpha, beta, k_h, live)

@@ -275,6 +275,47 @@ int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const do
 int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, double* X, void* stream);
 
 /*
+ * Ragged batches: the sectors of many models (different sizes and Hamiltonians) concatenated
+ * into one CSR.  The edgpu_csr then holds the concatenated row_ptr (global offsets into col
+ * and the values) and column indices LOCAL to each sector.  Sector s owns rows
+ * [sec_row0[s], sec_row0[s+1]); run r works on sector run_sec[r] and its vectors live at
+ * offset run_vec0[r] of packed complex128 arrays (run_vec0[r+1] - run_vec0[r] = the sector's
+ * size).  max_rows (host) bounds every sector size used by the runs.
+ * Replaces upstream's one-model-at-a-time calls (eigensystem, finite.py:58-118, and getGreen,
+ * spectra.py:551-681) for an ensemble of models; no single upstream function takes a batch.
+ */
+typedef struct edgpu_ragged {
+  int32_t n_sectors;
+  int32_t n_runs;
+  const int64_t* sec_row0; /* [n_sectors + 1], device */
+  const int32_t* run_sec;  /* [n_runs], device */
+  const int64_t* run_vec0; /* [n_runs + 1], device */
+  int64_t max_rows;
+} edgpu_ragged;
+
+/* Upstream's Lanczos recurrence (as edgpu_lanczos, precision 0) for every run of a ragged
+ * batch in one launch, one CTA per run with its three vectors in shared memory
+ * (edgpu_lanczos_ragged_smem(max_rows) <= 200 KiB).  alpha/beta [n_runs][K]. */
+size_t edgpu_lanczos_ragged_smem(int64_t max_rows);
+int edgpu_lanczos_ragged(const edgpu_csr* h, const edgpu_ragged* rg, const double* v0, const int32_t* k_max, int K,
+                         double* alpha, double* beta, int32_t* status_dev, void* stream);
+
+/* Lanczos with full reorthogonalisation (two classical Gram-Schmidt passes) for every run of
+ * a ragged batch in one launch, one CTA per run.  Run r keeps its Krylov basis at
+ * V + 2 * run_V0[r] doubles ([k_max[r]][n] complex128, caller-allocated); beta[r][k_max-1] is
+ * the last step's residual norm (Ritz residual estimates); breakdown before k_max sets
+ * *status_dev = EDGPU_ERR_BREAKDOWN and ends that run. */
+size_t edgpu_lanczos_reorth_ragged_smem(int64_t max_rows, int K);
+int edgpu_lanczos_reorth_ragged(const edgpu_csr* h, const edgpu_ragged* rg, const double* v0, const int32_t* k_max,
+                                int K, const int64_t* run_V0, double* V, double* alpha, double* beta,
+                                int32_t* status_dev, void* stream);
+
+/* Ritz vectors of a ragged batch: X[r][q] = sum_{k < k_len[r]} S[r][k][q] V_r[k] for q < Q
+ * (S real [n_runs][K][Q]); X packed complex128 at offset Q * run_vec0[r]. */
+int edgpu_combine_ragged(const double* V, const edgpu_ragged* rg, const int64_t* run_V0, const int32_t* k_len,
+                         const double* S, int K, int Q, double* X, void* stream);
+
+/*
  * Continued fractions (upstream spectra.py:678-680) for R runs on n_omega points:
  * g[r][w] = scale[r] / (z - a0 - b0^2 / (z - a1 - ...)), z = omega[w] + i*delta + e[r],
  * depth k_len[r] (alpha[r][0..k_len), beta[r][0..k_len-1), row stride K).
