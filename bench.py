@@ -159,7 +159,7 @@ class Pipeline:
         self.sb = finite._SortedBasis(eng, list(self.basis), self.n)
         self.w, self.w_in, self.w_loss = meshes()
 
-    def step(self, precision=0, timing=None, capture=None, perturb=None):
+    def step(self, precision=0, timing=None, capture=None, perturb=None, batched=True):
         from impuritymodel_gb300 import finite, spectra
 
         W = WORKLOAD
@@ -168,11 +168,11 @@ class Pipeline:
         es, psi_t = es[:ne], psi_t[:ne]
         g_xas = spectra.spectra_device(self.eng, self.dop, self.restr, self.xas_dops, psi_t, es, self.w,
                                        W["xas"]["delta"], W["krylov"], W["slater_weight_min"], precision,
-                                       capture=capture, perturb=perturb)
+                                       capture=capture, perturb=perturb, batched=batched)
         g_rixs = spectra.rixs_device(self.eng, self.dop, self.restr, self.xas_dops, self.out_dops, psi_t, es,
                                      self.w_in, self.w_loss, W["rixs"]["delta_in"], W["rixs"]["delta_loss"],
                                      W["krylov"], W["slater_weight_min"], precision, timing=timing,
-                                     capture=capture, perturb=perturb)
+                                     capture=capture, perturb=perturb, batched=batched)
         return es, g_xas, g_rixs
 
     def e2e_step(self, precision=0):
@@ -348,6 +348,80 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     }
 
 
+def batched_configs(eng, n_models=256):
+    """The batched workloads: an ensemble of seeded models (10-50 bath spin-orbitals) solved
+    for their 3 lowest eigenstates + XAS as ragged batches, and the RIXS map of the 26-orbital
+    model at 300 incoming x 2000 loss energies.  Each is timed once after a warm-up run."""
+    import torch
+
+    from impuritymodel_gb300 import ensemble, finite, models, spectra
+    from impuritymodel_gb300.engine import DeviceOp, make_restrictions
+
+    out = {}
+    members = [models.random_model(seed, 1 + seed % 5) for seed in range(n_models)]
+    w = np.linspace(-10.0, 20.0, 2000)
+
+    def ens_run(ms, graph):
+        t0 = time.perf_counter()
+        secs = [ensemble.ModelSectors(eng, m) for m in ms]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        es, psis = ensemble.ensemble_ground_states(eng, secs, 3)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        solve, run_map = ensemble.ensemble_xas_setup(eng, secs, es, psis, w, 0.2)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        if graph:
+            solve.capture()
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            solve.replay()
+        else:
+            solve.run()
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        return dict(sectors_s=t1 - t0, gs_s=t2 - t1, xas_setup_s=t3 - t2, xas_solve_s=t4 - t3,
+                    total_s=(t4 - t0)), secs, solve
+
+    ens_run(members[:8], True)  # warm-up (module loading, graph machinery)
+    n0 = eng.lib.edgpu_launch_count()
+    t, secs, solve = ens_run(members, True)
+    sizes = [s.csr.n for s in secs]
+    xs = [int(c.n) for c in solve.batch.csrs]
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(5):
+        solve.replay(check=False)
+    b.record()
+    torch.cuda.synchronize()
+    eng.read_status("ensemble replay")
+    out["ensemble_gs_xas"] = dict(
+        models=n_models, bath_spin_orbitals="10 * (1 + (seed mod 5)), seeds 0..%d" % (n_models - 1), states=3,
+        xas_points=int(w.size), gs_sector_rows=[min(sizes), max(sizes)], xas_sector_rows=[min(xs), max(xs)],
+        xas_runs=int(solve.batch.n_runs), library_launches=int(eng.lib.edgpu_launch_count() - n0),
+        graph_replay_ms=round(a.elapsed_time(b) / 5, 3), **{k: round(v, 4) for k, v in t.items()})
+    # RIXS map of the 26-orbital model, 300 x 2000
+    m1 = models.make_model("config1")
+    n = m1.n_spin_orbitals
+    dop = DeviceOp(m1.hOp, eng.device)
+    restr = make_restrictions(m1.restrictions, n)
+    sb = finite._SortedBasis(eng, list(finite.get_basis(*m1.basis_args())), n)
+    tin = [DeviceOp(x, eng.device) for x in m1.xas_ops()]
+    tout = [DeviceOp(x, eng.device) for x in m1.rixs_out_ops()]
+    w_in, w_loss = np.linspace(-10.0, 20.0, 300), np.linspace(-2.0, 12.0, 2000)
+    es, psi_t = finite.eigensystem_device(eng, dop, sb, 3)
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spectra.rixs_device(eng, dop, restr, tin, tout, psi_t, es, w_in, w_loss, 0.2, 0.05, 150, 1e-7, 3)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    out["rixs_26orb_300win"] = dict(states=len(es), w_in=int(w_in.size), w_loss=int(w_loss.size), pol_in=3,
+                                    pol_out=3, form="df64_krylov_fp32_cfrac", s=round(dt, 4))
+    return out
+
+
 def read_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -433,6 +507,11 @@ def run_gpu(args):
         outs[name] = o
     plain_times, plain_out = time_steps(lambda: pipe.step(0), max(1, args.steps // 2), args.warmup, flush_buf)
     form_times["plain_fp64"] = statistics.mean(plain_times)
+    # upstream's call structure on the GPU (one Green's function / one shifted solve per
+    # launch, FP64): the reference point of the batched forms
+    unb_times, unb_out = time_steps(lambda: pipe.step(0, batched=False), 1, 1, flush_buf)
+    t_unbatched = statistics.mean(unb_times)
+    unb_err = {k: rel_l1_t(a, b) for k, a, b in (("xas", unb_out[1], plain_out[1]), ("rixs", unb_out[2], plain_out[2]))}
     best_name = min((n for n in forms if ok[n]), key=lambda n: form_times[n])
     best_prec = forms[best_name]
     # production form: timed region for `value`, clocks and launch counts
@@ -479,6 +558,7 @@ def run_gpu(args):
     if roof is not None:
         traffic = traffic_from_profile(roof)
         roof["traffic"] = traffic
+    batched = batched_configs(eng) if (rank == 0 and not args.skip_batched) else None
     cpu = cpu_baseline(args.cpu_sample_seconds) if (rank == 0 and not args.skip_cpu) else None
     if rank == 0:
         line = {
@@ -498,6 +578,9 @@ def run_gpu(args):
                            parallelism="replicas" if world > 1 else "single GPU"),
             "plain_fp64_s": round(t_plain, 5),
             "speedup_vs_plain": round(t_plain / best, 3),
+            "plain_fp64_unbatched_s": round(t_unbatched, 4),
+            "speedup_vs_plain_unbatched": round(t_unbatched / best, 1),
+            "unbatched_vs_plain_rel_l1": unb_err,
             "forms": err,
             "e2e": {"value": round(e2e_t, 5), "unit": "s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
@@ -506,6 +589,7 @@ def run_gpu(args):
             "roofline": roof,
             "pipeline_kernel": pipeline_kernel_stats(timing),
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line))
     if world > 1:
@@ -707,6 +791,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true", help="skip the ensemble / 300-w_in RIXS lines")
     ap.add_argument("--hv-only", action="store_true",
                     help="only the H.v roofline measurement (the case profiled under ncu)")
     ap.add_argument("--profile-step", action="store_true",

@@ -216,6 +216,26 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     return g
 
 
+def green_runs_one_by_one(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
+                          normalize=True, scales=None):
+    """Upstream's call structure on the GPU: one Green's function per Lanczos launch, each on
+    the closure of its own start state (upstream getGreen per run, spectra.py:551-681).  The
+    reference point of the batched forms; same arguments as green_batch."""
+    if run_amps is None:
+        states, amps, run_of_row, runs = run_states
+        rr = run_of_row.cpu().numpy()
+        bounds = np.searchsorted(rr, np.arange(runs + 1))
+        run_states = [states[bounds[r]:bounds[r + 1]] for r in range(runs)]
+        run_amps = [amps[bounds[r]:bounds[r + 1]] for r in range(runs)]
+    runs = len(run_states)
+    g = torch.zeros((runs, len(np.atleast_1d(omega))), dtype=torch.complex128, device=eng.device)
+    for r in range(runs):
+        sc = None if scales is None else [scales[r]]
+        g[r] = green_batch(eng, dop, restr, [run_states[r]], [run_amps[r]], [e_runs[r]], omega, delta, krylovSize,
+                           precision, normalize=normalize, scales=sc)[0]
+    return g
+
+
 class StageTimer:
     """Optional per-stage wall-clock timing (synchronises the device at each mark)."""
 
@@ -271,9 +291,10 @@ def getGreen(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeigh
 
 
 def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7,
-                   precision=0, capture=None, perturb=None):
+                   precision=0, capture=None, perturb=None, batched=True):
     """Device form of :func:`getSpectra`: ``psi_t`` is a list of (states, amps) device tensors.
 
+    ``batched=False`` runs upstream's call structure (one Green's function at a time).
     Returns g [n_states, n_ops, n_w] complex128 on the device.
     """
     ne = len(es)
@@ -285,8 +306,11 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
             run_states.append(s_)
             run_amps.append(a_)
             e_runs.append(es[i])
-    g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision,
-                    capture=capture, perturb=perturb)
+    if batched:
+        g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision,
+                        capture=capture, perturb=perturb)
+    else:
+        g = green_runs_one_by_one(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision)
     return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
 
 
@@ -375,8 +399,11 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
 
 def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                 slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-                timing=None, capture=None, perturb=None, stages=None):
-    """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device)."""
+                timing=None, capture=None, perturb=None, stages=None, batched=True):
+    """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device).
+
+    ``batched=False`` runs upstream's call structure: one shifted solve per incoming energy
+    and one final-state Green's function per (incoming energy, outgoing channel)."""
     _mark(stages, "start")
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
@@ -414,7 +441,25 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
         Y[r].index_put_((eng.lookup(core.basis, s1),), torch.complex(a1[:, 0], a1[:, 1]), accumulate=True)
     zs = np.array([wIns + 1j * delta1 + es[ie] for (_, ie) in keys])
     # without reorthogonalisation the recurrence may need a few times the sector dimension
-    solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, min(6 * core.n + 50, max_krylov))
+    k_solve = min(6 * core.n + 50, max_krylov)
+    if batched:
+        solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve)
+    else:
+        solved = None
+        blocks = []
+        for r in range(len(keys)):
+            cols = []
+            for iw in range(nwi):
+                one = eng.shifted_solve(core.csr, Y[r:r + 1], zs[r:r + 1, iw:iw + 1], solve_tol, k_solve)
+                if one is None:
+                    break
+                cols.append(one[0][0, 0])
+            if len(cols) < nwi:
+                blocks = None
+                break
+            blocks.append(torch.stack(cols))
+        if blocks is not None:
+            solved = (torch.stack(blocks), None)
     if solved is not None:
         x_blocks = list(solved[0])
     else:
@@ -431,7 +476,7 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     for k in range(nout):
         tm = out_maps[k]
         first = next(k0 for k0 in range(k + 1) if out_maps[k0] is tm)
-        if first != k:
+        if first != k and batched:
             alias[k] = first
             continue
         if id(tm) not in pruned:
@@ -460,8 +505,13 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     # 6. ground-like sector Lanczos + continued fractions for all runs at once.  Upstream
     # runs getGreen on the normalised-then-pruned psi3 and scales by the squared norm taken
     # before the second pruning (spectra.py:1097-1124).
-    g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
-                    normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb, stages=stages)
+    if batched:
+        g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
+                        normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb,
+                        stages=stages)
+    else:
+        g = green_runs_one_by_one(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
+                                  normalize=False, scales=scales)
     idx = torch.tensor([((ie * nin + t_in) * nout + k) * nwi + iw for (ie, t_in, k, iw) in slots],
                        device=eng.device)
     gs.view(-1, len(wLoss))[idx] = g
