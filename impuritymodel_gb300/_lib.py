@@ -111,6 +111,7 @@ SIGNATURES = {
     "edgpu_lanczos_reorth_ragged_smem": (_SZ, [_I64, _I]),
     "edgpu_lanczos_reorth_ragged": (_I, [C.POINTER(CSR), C.c_void_p, _P, _P, _I, _P, _P, _P, _P, _P, _P]),
     "edgpu_combine_ragged": (_I, [_P, C.c_void_p, _P, _P, _P, _I, _I, _P, _P]),
+    "edgpu_gemm_bf16": (_I, [_P, _P, _I, _I, _I, _P, _P, _P]),
     "edgpu_cfrac": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P]),
     "edgpu_cfrac_f32_workspace": (_SZ, [_I, _I]),
     "edgpu_cfrac_f32": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P, _SZ, _P]),

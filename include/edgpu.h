@@ -310,6 +310,15 @@ int edgpu_lanczos_reorth_ragged(const edgpu_csr* h, const edgpu_ragged* rg, cons
                                 int K, const int64_t* run_V0, double* V, double* alpha, double* beta,
                                 int32_t* status_dev, void* stream);
 
+/*
+ * C[M][N] (float32) = A[M][K] * B[N][K]^T with A and B row-major BF16 (K-major), on the
+ * tcgen05 tensor cores: operand tiles in shared memory, FP32 accumulator in tensor memory.
+ * M % 128 == 0, K % 64 == 0, N % 16 == 0, A and B 16-byte aligned.  A completion wait that
+ * runs out of its iteration limit sets *status_dev = EDGPU_ERR_NOCONV.  No counterpart in
+ * upstream impurityModel (the GEMM of the basis-pruning network).
+ */
+int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev, void* stream);
+
 /* Ritz vectors of a ragged batch: X[r][q] = sum_{k < k_len[r]} S[r][k][q] V_r[k] for q < Q
  * (S real [n_runs][K][Q]); X packed complex128 at offset Q * run_vec0[r]. */
 int edgpu_combine_ragged(const double* V, const edgpu_ragged* rg, const int64_t* run_V0, const int32_t* k_len,
