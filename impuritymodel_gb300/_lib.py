@@ -112,6 +112,13 @@ SIGNATURES = {
     "edgpu_lanczos_reorth_ragged": (_I, [C.POINTER(CSR), C.c_void_p, _P, _P, _I, _P, _P, _P, _P, _P, _P]),
     "edgpu_combine_ragged": (_I, [_P, C.c_void_p, _P, _P, _P, _I, _I, _P, _P]),
     "edgpu_gemm_bf16": (_I, [_P, _P, _I, _I, _I, _P, _P, _P]),
+    "edgpu_gemm_bf16_epi": (_I, [_I, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "edgpu_mlp_bits": (_I, [_P, _I, _I64, _I, _P, _P, _P]),
+    "edgpu_mlp_head": (_I, [_P, _P, _P, _I64, _I, _P, _P]),
+    "edgpu_mlp_head_backward": (_I, [_P, _P, _P, _P, _I64, _I, _P, _P, _P, _P]),
+    "edgpu_mlp_row_dot": (_I, [_P, _I, _I64, _P, _P, _P]),
+    "edgpu_mlp_adam": (_I, [_P, _P, _P, _P, _I64, C.c_float, C.c_float, C.c_float, C.c_float, _P]),
+    "edgpu_mlp_to_bf16": (_I, [_P, _I, _I, _P, _P, _P]),
     "edgpu_cfrac": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P]),
     "edgpu_cfrac_f32_workspace": (_SZ, [_I, _I]),
     "edgpu_cfrac_f32": (_I, [_P, _P, _P, _I, _I, _P, _I, _D, _P, _P, _P, _P, _SZ, _P]),

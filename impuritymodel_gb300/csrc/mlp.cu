@@ -246,9 +246,187 @@ int gemm_bf16(int epi, const GemmArgs& g, cudaStream_t s) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Network pieces around the GEMMs (CUDA cores): input bits, output head, bias gradients,
+// Adam, BF16 copies of the weights.
+// ---------------------------------------------------------------------------------------
+
+// X[b][i] = occupation of spin-orbital i (bit 63 - i%64 of word i/64) for i < n_in, BF16;
+// Xt = X^T when not null.
+__global__ void mlp_bits_kernel(const uint64_t* __restrict__ states, int W, int64_t B, int n_in,
+                                __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ Xt) {
+  const int64_t total = B * (int64_t)n_in;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / n_in;
+    const int i = (int)(t - b * n_in);
+    const int q = i >> 6;
+    float v = 0.0f;
+    if (q < W) v = (float)((states[b * W + q] >> (63 - (i & 63))) & 1ull);
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    X[t] = h;
+    if (Xt) Xt[(int64_t)i * B + b] = h;
+  }
+}
+
+// y[b] = sum_j H[b][j] w3[j] + b3 (warp per row, FP32)
+__global__ void mlp_head_kernel(const __nv_bfloat16* __restrict__ H, const float* __restrict__ w3, const float* b3,
+                                int64_t B, int n_h, float* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < B;
+       b += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    float acc = 0.0f;
+    for (int j = lane; j < n_h; j += 32) acc += __bfloat162float(H[b * n_h + j]) * w3[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[b] = acc + b3[0];
+  }
+}
+
+// Mean-squared-error head backward: dy = 2 (y - t) / B; dH[b][j] = dy w3[j] (H[b][j] > 0)
+// as BF16 dH and dHt; loss partials per block.
+__global__ void mlp_head_backward_kernel(const __nv_bfloat16* __restrict__ H, const float* __restrict__ y,
+                                         const float* __restrict__ target, const float* __restrict__ w3, int64_t B,
+                                         int n_h, float* __restrict__ dy, __nv_bfloat16* __restrict__ dH,
+                                         __nv_bfloat16* __restrict__ dHt) {
+  const int64_t total = B * (int64_t)n_h;
+  const float inv = 2.0f / (float)B;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / n_h;
+    const int j = (int)(t - b * n_h);
+    const float d = (y[b] - target[b]) * inv;
+    if (j == 0) dy[b] = d;
+    const float g = __bfloat162float(H[t]) > 0.0f ? d * w3[j] : 0.0f;
+    const __nv_bfloat16 gb = __float2bfloat16_rn(g);
+    dH[t] = gb;
+    dHt[(int64_t)j * B + b] = gb;
+  }
+}
+
+// out[r] = sum_c M[r][c] * (v ? v[c] : 1) for a row-major [rows][cols] BF16 matrix, block per
+// row, fixed-order reduction (bias gradients from the transposed activations / deltas).
+__global__ void mlp_row_dot_kernel(const __nv_bfloat16* __restrict__ M, int rows, int64_t cols,
+                                   const float* __restrict__ v, float* __restrict__ out) {
+  __shared__ float red[32];
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    float acc = 0.0f;
+    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x)
+      acc += __bfloat162float(M[(int64_t)r * cols + c]) * (v ? v[c] : 1.0f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.0f;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+      out[r] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// Adam on a flat FP32 parameter vector (bias-corrected step size lr_t from the host).
+__global__ void mlp_adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                                float* __restrict__ v, int64_t n, float lr_t, float beta1, float beta2, float eps) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = beta1 * m[i] + (1.0f - beta1) * gi;
+    const float vi = beta2 * v[i] + (1.0f - beta2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr_t * mi / (sqrtf(vi) + eps);
+  }
+}
+
+// BF16 copy of a row-major [rows][cols] FP32 matrix, and of its transpose when Wt is set.
+__global__ void mlp_to_bf16_kernel(const float* __restrict__ Wf, int rows, int cols, __nv_bfloat16* __restrict__ Wb,
+                                   __nv_bfloat16* __restrict__ Wt) {
+  const int64_t total = (int64_t)rows * cols;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / cols), c = (int)(t - (int64_t)r * cols);
+    const __nv_bfloat16 h = __float2bfloat16_rn(Wf[t]);
+    if (Wb) Wb[t] = h;
+    if (Wt) Wt[(int64_t)c * rows + r] = h;
+  }
+}
+
+inline unsigned mlp_grid(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)grid_cap() * 8;
+  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
 }  // namespace edgpu
 
 using namespace edgpu;
+
+extern "C" int edgpu_gemm_bf16_epi(int epi, const void* A, const void* B, int M, int N, int K, float* C,
+                                   const float* bias, const void* mask, void* Y, void* Yt, int32_t* status_dev,
+                                   void* stream) {
+  GemmArgs g{};
+  g.A = reinterpret_cast<const __nv_bfloat16*>(A);
+  g.B = reinterpret_cast<const __nv_bfloat16*>(B);
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.C = C;
+  g.bias = bias;
+  g.mask = reinterpret_cast<const __nv_bfloat16*>(mask);
+  g.Y = reinterpret_cast<__nv_bfloat16*>(Y);
+  g.Yt = reinterpret_cast<__nv_bfloat16*>(Yt);
+  g.status = status_dev;
+  return gemm_bf16(epi, g, (cudaStream_t)stream);
+}
+
+extern "C" int edgpu_mlp_bits(const uint64_t* states, int W, int64_t B, int n_in, void* X, void* Xt, void* stream) {
+  if (!states || W < 1 || B < 1 || n_in < 1 || !X) return EDGPU_ERR_ARG;
+  mlp_bits_kernel<<<mlp_grid(B * n_in, 256), 256, 0, (cudaStream_t)stream>>>(
+      states, W, B, n_in, reinterpret_cast<__nv_bfloat16*>(X), reinterpret_cast<__nv_bfloat16*>(Xt));
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_mlp_head(const void* H, const float* w3, const float* b3, int64_t B, int n_h, float* y,
+                              void* stream) {
+  if (!H || !w3 || !b3 || B < 1 || n_h < 1 || !y) return EDGPU_ERR_ARG;
+  mlp_head_kernel<<<mlp_grid(B * 32, 256), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const __nv_bfloat16*>(H), w3, b3, B, n_h, y);
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_mlp_head_backward(const void* H, const float* y, const float* target, const float* w3,
+                                       int64_t B, int n_h, float* dy, void* dH, void* dHt, void* stream) {
+  if (!H || !y || !target || !w3 || B < 1 || n_h < 1 || !dy || !dH || !dHt) return EDGPU_ERR_ARG;
+  mlp_head_backward_kernel<<<mlp_grid(B * n_h, 256), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const __nv_bfloat16*>(H), y, target, w3, B, n_h, dy, reinterpret_cast<__nv_bfloat16*>(dH),
+      reinterpret_cast<__nv_bfloat16*>(dHt));
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_mlp_row_dot(const void* M, int rows, int64_t cols, const float* v, float* out, void* stream) {
+  if (!M || rows < 1 || cols < 1 || !out) return EDGPU_ERR_ARG;
+  mlp_row_dot_kernel<<<rows < 4096 ? rows : 4096, 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const __nv_bfloat16*>(M), rows, cols, v, out);
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_mlp_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr_t, float beta1,
+                              float beta2, float eps, void* stream) {
+  if (!p || !g || !m || !v || n < 1) return EDGPU_ERR_ARG;
+  mlp_adam_kernel<<<mlp_grid(n, 256), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr_t, beta1, beta2, eps);
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_mlp_to_bf16(const float* Wf, int rows, int cols, void* Wb, void* Wt, void* stream) {
+  if (!Wf || rows < 1 || cols < 1 || (!Wb && !Wt)) return EDGPU_ERR_ARG;
+  mlp_to_bf16_kernel<<<mlp_grid((int64_t)rows * cols, 256), 256, 0, (cudaStream_t)stream>>>(
+      Wf, rows, cols, reinterpret_cast<__nv_bfloat16*>(Wb), reinterpret_cast<__nv_bfloat16*>(Wt));
+  note_launch();
+  return check_launch();
+}
 
 extern "C" int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev,
                                void* stream) {

@@ -1,0 +1,230 @@
+"""Learned basis pruning: a small network over occupation bitstrings ranks basis states.
+
+No counterpart in upstream impurityModel, whose bases keep every restricted configuration
+(``get_basis``, finite.py:294-374) and every state of a closure (``expand_basis``,
+finite.py:1696-1803).  The network (occupation bits of up to 320 spin-orbitals -> 256 -> 256
+-> 1, ReLU) is trained on the GPU by the library's own kernels (tcgen05 BF16 GEMMs with
+FP32 accumulation, FP32 Adam master weights) to predict log10 of the ground-state weight
+``|<s|psi_0>|^2`` of each basis state, from plain exact diagonalisation of seeded models.
+Pruning keeps the best-ranked fraction of a basis; the full basis stays the fallback and the
+judge of the energy error (``pruned_ground_state`` reports both).
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .engine import _ptr, get_engine
+
+N_IN = 320  # 316 spin-orbitals of the largest model, padded to a multiple of 64
+N_H = 256
+WORDS = N_IN // 64
+ROWS = 128  # batch granularity of the tensor-core GEMMs
+FLOOR = 1e-14  # weights below this count as 10^-14
+
+
+def pad_words(states, words=WORDS):
+    """[N, W] int64 state words -> [N, words] (extra words zero: spin-orbitals beyond W*64 empty)."""
+    n, w = states.shape
+    if w == words:
+        return states.contiguous()
+    out = torch.zeros((n, words), dtype=torch.int64, device=states.device)
+    out[:, : min(w, words)] = states[:, :words]
+    return out
+
+
+class BasisNet:
+    """Device parameters, Adam state and the forward/backward passes of the network."""
+
+    def __init__(self, eng=None, seed=0, lr=1e-3):
+        self.eng = eng or get_engine()
+        dev = self.eng.device
+        g = torch.Generator().manual_seed(int(seed))
+        shapes = [("W1", (N_H, N_IN)), ("b1", (N_H,)), ("W2", (N_H, N_H)), ("b2", (N_H,)), ("w3", (N_H,)),
+                  ("b3", (1,))]
+        sizes = [int(np.prod(s)) for _, s in shapes]
+        self.P = torch.zeros(sum(sizes), dtype=torch.float32, device=dev)
+        self.G = torch.zeros_like(self.P)
+        self.m = torch.zeros_like(self.P)
+        self.v = torch.zeros_like(self.P)
+        self.p, self.g = {}, {}
+        off = 0
+        for (name, shape), sz in zip(shapes, sizes):
+            self.p[name] = self.P[off: off + sz].view(shape)
+            self.g[name] = self.G[off: off + sz].view(shape)
+            off += sz
+        self.p["W1"].copy_(torch.randn((N_H, N_IN), generator=g) * math.sqrt(2.0 / N_IN))
+        self.p["W2"].copy_(torch.randn((N_H, N_H), generator=g) * math.sqrt(2.0 / N_H))
+        self.p["w3"].copy_(torch.randn((N_H,), generator=g) * math.sqrt(1.0 / N_H))
+        self.p["b3"].fill_(-7.0)  # middle of the log10 weight range
+        self.W1b = torch.empty((N_H, N_IN), dtype=torch.bfloat16, device=dev)
+        self.W2b = torch.empty((N_H, N_H), dtype=torch.bfloat16, device=dev)
+        self.W2t = torch.empty((N_H, N_H), dtype=torch.bfloat16, device=dev)
+        self.lr = lr
+        self.t = 0
+        self.refresh()
+
+    # -- kernels -------------------------------------------------------------------------
+    def _lib(self):
+        return self.eng.lib
+
+    def refresh(self):
+        """BF16 operand copies of the FP32 master weights (W2 also transposed)."""
+        e = self.eng
+        L.check(self._lib().edgpu_mlp_to_bf16(_ptr(self.p["W1"]), N_H, N_IN, _ptr(self.W1b), None, e.stream),
+                "mlp_to_bf16")
+        L.check(self._lib().edgpu_mlp_to_bf16(_ptr(self.p["W2"]), N_H, N_H, _ptr(self.W2b), _ptr(self.W2t),
+                                              e.stream), "mlp_to_bf16")
+
+    def _gemm(self, epi, A, B, M, N, K, C=None, bias=None, mask=None, Y=None, Yt=None):
+        e = self.eng
+        L.check(self._lib().edgpu_gemm_bf16_epi(epi, _ptr(A), _ptr(B), M, N, K, _ptr(C) if C is not None else None,
+                                                _ptr(bias) if bias is not None else None,
+                                                _ptr(mask) if mask is not None else None,
+                                                _ptr(Y) if Y is not None else None,
+                                                _ptr(Yt) if Yt is not None else None, _ptr(e.status), e.stream),
+                "gemm_bf16_epi")
+
+    def inputs(self, states, transposed=False):
+        """BF16 occupation matrix X [B, N_IN] (and X^T) of padded states [B, WORDS]."""
+        B = states.shape[0]
+        dev = self.eng.device
+        X = torch.empty((B, N_IN), dtype=torch.bfloat16, device=dev)
+        Xt = torch.empty((N_IN, B), dtype=torch.bfloat16, device=dev) if transposed else None
+        L.check(self._lib().edgpu_mlp_bits(_ptr(states), states.shape[1], B, N_IN, _ptr(X),
+                                           _ptr(Xt) if Xt is not None else None, self.eng.stream), "mlp_bits")
+        return X, Xt
+
+    def forward(self, X, keep=False):
+        B = X.shape[0]
+        dev = self.eng.device
+        H1 = torch.empty((B, N_H), dtype=torch.bfloat16, device=dev)
+        H2 = torch.empty((B, N_H), dtype=torch.bfloat16, device=dev)
+        H1t = torch.empty((N_H, B), dtype=torch.bfloat16, device=dev) if keep else None
+        H2t = torch.empty((N_H, B), dtype=torch.bfloat16, device=dev) if keep else None
+        self._gemm(1, X, self.W1b, B, N_H, N_IN, bias=self.p["b1"], Y=H1, Yt=H1t)
+        self._gemm(1, H1, self.W2b, B, N_H, N_H, bias=self.p["b2"], Y=H2, Yt=H2t)
+        y = torch.empty(B, dtype=torch.float32, device=dev)
+        L.check(self._lib().edgpu_mlp_head(_ptr(H2), _ptr(self.p["w3"]), _ptr(self.p["b3"]), B, N_H, _ptr(y),
+                                           self.eng.stream), "mlp_head")
+        return y, (H1, H1t, H2, H2t)
+
+    def gradients(self, X, Xt, target):
+        """Mean-squared-error loss (device scalar) and gradients into self.g."""
+        B = X.shape[0]
+        dev = self.eng.device
+        lib, s = self._lib(), self.eng.stream
+        y, (H1, H1t, H2, H2t) = self.forward(X, keep=True)
+        dy = torch.empty(B, dtype=torch.float32, device=dev)
+        dH2 = torch.empty((B, N_H), dtype=torch.bfloat16, device=dev)
+        dH2t = torch.empty((N_H, B), dtype=torch.bfloat16, device=dev)
+        L.check(lib.edgpu_mlp_head_backward(_ptr(H2), _ptr(y), _ptr(target), _ptr(self.p["w3"]), B, N_H, _ptr(dy),
+                                            _ptr(dH2), _ptr(dH2t), s), "mlp_head_backward")
+        L.check(lib.edgpu_mlp_row_dot(_ptr(H2t), N_H, B, _ptr(dy), _ptr(self.g["w3"]), s), "row_dot")
+        self.g["b3"].copy_(dy.sum().view(1))
+        self._gemm(0, dH2t, H1t, N_H, N_H, B, C=self.g["W2"])
+        L.check(lib.edgpu_mlp_row_dot(_ptr(dH2t), N_H, B, None, _ptr(self.g["b2"]), s), "row_dot")
+        dH1 = torch.empty((B, N_H), dtype=torch.bfloat16, device=dev)
+        dH1t = torch.empty((N_H, B), dtype=torch.bfloat16, device=dev)
+        self._gemm(2, dH2, self.W2t, B, N_H, N_H, mask=H1, Y=dH1, Yt=dH1t)
+        self._gemm(0, dH1t, Xt, N_H, N_IN, B, C=self.g["W1"])
+        L.check(lib.edgpu_mlp_row_dot(_ptr(dH1t), N_H, B, None, _ptr(self.g["b1"]), s), "row_dot")
+        return ((y - target) ** 2).mean()
+
+    def adam_step(self, beta1=0.9, beta2=0.999, eps=1e-8):
+        self.t += 1
+        lr_t = self.lr * math.sqrt(1.0 - beta2 ** self.t) / (1.0 - beta1 ** self.t)
+        L.check(self._lib().edgpu_mlp_adam(_ptr(self.P), _ptr(self.G), _ptr(self.m), _ptr(self.v), self.P.numel(),
+                                           lr_t, beta1, beta2, eps, self.eng.stream), "mlp_adam")
+        self.refresh()
+
+    # -- training and inference ----------------------------------------------------------
+    def train(self, states, log_w, epochs=4, batch=4096, seed=0, log=None):
+        """Fit log10 weights ``log_w`` [N] of padded states [N, WORDS] by Adam on shuffled batches."""
+        batch = max(ROWS, (batch // ROWS) * ROWS)
+        n = states.shape[0]
+        gen = torch.Generator(device=self.eng.device)
+        gen.manual_seed(int(seed))
+        losses = []
+        for ep in range(epochs):
+            perm = torch.randperm(n, device=self.eng.device, generator=gen)
+            for b0 in range(0, n - batch + 1, batch):
+                idx = perm[b0: b0 + batch]
+                X, Xt = self.inputs(states[idx].contiguous(), transposed=True)
+                loss = self.gradients(X, Xt, log_w[idx].contiguous())
+                self.adam_step()
+                losses.append(loss)
+            if log is not None:
+                log.append(float(torch.stack(losses[-max(1, n // batch):]).mean().item()))
+        self.eng.read_status("mlp training")
+        return losses
+
+    def predict(self, states):
+        """Predicted log10 weights of padded states [N, WORDS] (any N)."""
+        n = states.shape[0]
+        nb = ((n + ROWS - 1) // ROWS) * ROWS
+        if nb != n:
+            pad = torch.zeros((nb - n, states.shape[1]), dtype=states.dtype, device=states.device)
+            states = torch.cat([states, pad], 0)
+        X, _ = self.inputs(states.contiguous())
+        y, _ = self.forward(X)
+        self.eng.read_status("mlp inference")
+        return y[:n]
+
+
+def ground_state_samples(eng, models, k_start=120):
+    """(padded states [N, WORDS], log10 weights [N] float32) of the ground states of ``models``
+    from plain exact diagonalisation (one ragged launch per convergence round)."""
+    from .ensemble import ModelSectors, ensemble_ground_states
+
+    secs = [ModelSectors(eng, m) for m in models]
+    _, psis = ensemble_ground_states(eng, secs, 1, k_start=k_start, slaterWeightMin=0.0)
+    st, lw = [], []
+    for ps in psis:
+        s, a = ps[0]
+        st.append(pad_words(s))
+        w2 = (a[:, 0] ** 2 + a[:, 1] ** 2).clamp_min(FLOOR)
+        lw.append(torch.log10(w2).to(torch.float32))
+    return torch.cat(st), torch.cat(lw)
+
+
+def pruned_ground_state(eng, model, keep, ranking):
+    """Ground-state energy on the ``keep`` fraction of the model's basis ranked by
+    ``ranking`` ("net", "diagonal" or "random"), against the full basis.
+
+    ``ranking`` may also be a BasisNet (ranks by its prediction).  Returns a dict with the
+    full and pruned energies, the error (eV, >= 0 by the variational principle) and sizes."""
+    from .finite import _device_hamiltonian, _device_op, _SortedBasis, eig_lowest, get_basis
+
+    n = model.n_spin_orbitals
+    dop = _device_op(model.hOp, eng)
+    sb = _SortedBasis(eng, list(get_basis(*model.basis_args())), n)
+    csr = _device_hamiltonian(eng, dop, sb)
+    e_full, _ = eig_lowest(eng, csr, 1)
+    N = sb.sorted.shape[0]
+    m = max(1, int(round(keep * N)))
+    if isinstance(ranking, BasisNet):
+        score = ranking.predict(pad_words(sb.sorted))
+    elif ranking == "diagonal":
+        rows = torch.repeat_interleave(torch.arange(N, device=eng.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
+        diag = torch.zeros(N, dtype=torch.float64, device=eng.device)
+        on = rows == csr.col.to(torch.int64)
+        vals = csr.val_r if csr.val_r is not None else csr.val_c[:, 0]
+        diag[rows[on]] = vals[on]
+        score = -diag
+    elif ranking == "random":
+        gen = torch.Generator(device=eng.device)
+        gen.manual_seed(0)
+        score = torch.rand(N, device=eng.device, generator=gen)
+    else:
+        raise ValueError("ranking must be a BasisNet, 'diagonal' or 'random'")
+    top = torch.sort(torch.topk(score.to(torch.float64), m).indices).values
+    sub = sb.sorted[top].contiguous()
+    csr_p = eng.build_csr(sub, dop, None)
+    e_p, _ = eig_lowest(eng, csr_p, 1)
+    return dict(e_full=float(e_full[0]), e_pruned=float(e_p[0]), error=float(e_p[0] - e_full[0]), n_full=int(N),
+                n_pruned=int(m), nnz_full=int(csr.nnz), nnz_pruned=int(csr_p.nnz))

@@ -319,6 +319,33 @@ int edgpu_lanczos_reorth_ragged(const edgpu_csr* h, const edgpu_ragged* rg, cons
  */
 int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev, void* stream);
 
+/*
+ * Basis-pruning network (input bits -> 256 -> 256 -> 1, BF16 operands, FP32 accumulation);
+ * no counterpart in upstream impurityModel.  The GEMM with a fused epilogue:
+ *   epi 0: C = acc (float32 [M][N]);
+ *   epi 1: Y = relu(acc + bias[col]) as BF16 [M][N], and Yt = Y^T [N][M] when not NULL;
+ *   epi 2: Y = acc where mask[row][col] > 0 else 0 (BF16 mask [M][N]), Y and Yt as epi 1.
+ * Shapes as edgpu_gemm_bf16.
+ */
+int edgpu_gemm_bf16_epi(int epi, const void* A, const void* B, int M, int N, int K, float* C, const float* bias,
+                        const void* mask, void* Y, void* Yt, int32_t* status_dev, void* stream);
+/* X[b][i] = occupation of spin-orbital i of states[b] (W words, bit 63 - i%64 of word i/64),
+ * BF16 [B][n_in]; Xt = X^T [n_in][B] when not NULL. */
+int edgpu_mlp_bits(const uint64_t* states, int W, int64_t B, int n_in, void* X, void* Xt, void* stream);
+/* y[b] = sum_j H[b][j] w3[j] + b3[0] (H BF16 [B][n_h]). */
+int edgpu_mlp_head(const void* H, const float* w3, const float* b3, int64_t B, int n_h, float* y, void* stream);
+/* Mean-squared-error head backward: dy = 2 (y - target) / B, dH = dy w3 masked by H > 0
+ * (BF16 [B][n_h] and its transpose dHt). */
+int edgpu_mlp_head_backward(const void* H, const float* y, const float* target, const float* w3, int64_t B, int n_h,
+                            float* dy, void* dH, void* dHt, void* stream);
+/* out[r] = sum_c M[r][c] v[c] (v NULL: plain row sums) for BF16 M [rows][cols]. */
+int edgpu_mlp_row_dot(const void* M, int rows, int64_t cols, const float* v, float* out, void* stream);
+/* Adam step on a flat FP32 vector; lr_t is the bias-corrected step size. */
+int edgpu_mlp_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr_t, float beta1, float beta2,
+                   float eps, void* stream);
+/* BF16 copy Wb of a row-major FP32 [rows][cols] matrix and/or of its transpose Wt. */
+int edgpu_mlp_to_bf16(const float* Wf, int rows, int cols, void* Wb, void* Wt, void* stream);
+
 /* Ritz vectors of a ragged batch: X[r][q] = sum_{k < k_len[r]} S[r][k][q] V_r[k] for q < Q
  * (S real [n_runs][K][Q]); X packed complex128 at offset Q * run_vec0[r]. */
 int edgpu_combine_ragged(const double* V, const edgpu_ragged* rg, const int64_t* run_V0, const int32_t* k_len,
