@@ -348,6 +348,60 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     }
 
 
+def pruning_setup(eng, n_train=1000, n_held=200, keeps=(0.5, 0.75), epochs=10):
+    """The basis-pruning network: trained on the ground-state weights of 1000 seeded models
+    (seeds 1000-1999, 10-50 bath spin-orbitals), judged on 200 held-out models (seeds
+    2000-2199; even seeds 50, odd seeds 100 bath spin-orbitals) by the ground-state energy on
+    the best-ranked fraction of each basis, against the full basis and against keeping the
+    lowest diagonal energies (the ranking without the network)."""
+    import torch
+
+    from impuritymodel_gb300 import models, pruning
+
+    train = [models.random_model(s, 1 + s % 5) for s in range(1000, 1000 + n_train)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, lw = pruning.ground_state_samples(eng, train)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net = pruning.BasisNet(eng, seed=0, lr=2e-3)
+    log = []
+    n0 = eng.lib.edgpu_launch_count()
+    net.train(st, lw, epochs=epochs, batch=4096, log=log)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    steps = net.t
+    flop_fwd = 2.0 * (pruning.N_IN * pruning.N_H + pruning.N_H * pruning.N_H + pruning.N_H)
+    rows = {"net": {}, "lowest_diagonal": {}}
+    split = {}
+    for s in range(2000, 2000 + n_held):
+        levels = 5 if s % 2 == 0 else 10
+        res, full = pruning.evaluate_pruning(eng, models.random_model(s, levels), keeps,
+                                             {"net": net, "lowest_diagonal": "diagonal"})
+        key = "%d_bath" % (10 * levels)
+        split.setdefault(key, [0, full["n"]])[0] += 1
+        for name in rows:
+            for k in keeps:
+                rows[name].setdefault((key, k), []).append(res[name][k]["error"])
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    held = {}
+    for name, d in rows.items():
+        for (key, k), errs in d.items():
+            e = np.asarray(errs)
+            held.setdefault(key, {}).setdefault("keep_%g" % k, {})[name] = {
+                "median_error_eV": float(np.median(e)), "max_error_eV": float(e.max()),
+                "within_1e-4_eV": int(np.sum(e <= 1e-4))}
+    return net, {
+        "train_models": n_train, "train_samples": int(st.shape[0]), "target": "log10 |<s|psi_0>|^2",
+        "sample_gen_s": round(t1 - t0, 3), "epochs": epochs, "adam_steps": int(steps), "batch": 4096,
+        "train_s": round(t2 - t1, 3), "train_launches": int(eng.lib.edgpu_launch_count() - n0),
+        "train_loss_first_last": [round(log[0], 4), round(log[-1], 4)],
+        "train_tflops": round(3.0 * flop_fwd * steps * 4096 / (t2 - t1) / 1e12, 3),
+        "held_out": {k: {"models": v[0], "rows": v[1]} for k, v in split.items()}, "held_out_errors": held,
+        "eval_s": round(t3 - t2, 3)}
+
+
 def batched_configs(eng, n_models=256):
     """The batched workloads: an ensemble of seeded models (10-50 bath spin-orbitals) solved
     for their 3 lowest eigenstates + XAS as ragged batches, and the RIXS map of the 26-orbital
@@ -487,8 +541,9 @@ def run_gpu(args):
         a = {"runs": len(cp["live"]), "sector": int(cp["csr"].n),
              "plain_ensemble_vs_exact_rel_l1": [round(x, 6) for x in ens]}
         for name in forms:
-            a[name + "_vs_exact_rel_l1"] = rel_l1_t(run_level(caps[name][idx]), ex)
-            a[name + "_vs_plain_rel_l1"] = rel_l1_t(run_level(caps[name][idx]), run_level(cp))
+            g = run_level(caps[name][idx])
+            a[name + "_vs_exact_rel_l1"] = rel_l1_t(g, ex)
+            a[name + "_vs_plain_rel_l1"] = rel_l1_t(g, run_level(cp))
         acc[kind] = a
     del caps, caps_e
     # equal error: a form may not be farther from the exact resolvent than the worst
@@ -496,6 +551,7 @@ def run_gpu(args):
     ok = {name: all(a[name + "_vs_exact_rel_l1"] <= max([a["plain_fp64_vs_exact_rel_l1"]] +
                                                          a["plain_ensemble_vs_exact_rel_l1"]) + MIXED_L1_TOL
                     for a in acc.values()) for name in forms}
+
     # time every form; the headline is the fastest form that keeps the error
     form_times = {}
     outs = {}
@@ -559,6 +615,7 @@ def run_gpu(args):
         traffic = traffic_from_profile(roof)
         roof["traffic"] = traffic
     batched = batched_configs(eng) if (rank == 0 and not args.skip_batched) else None
+    prune_info = pruning_setup(eng)[1] if (rank == 0 and not args.skip_batched) else None
     cpu = cpu_baseline(args.cpu_sample_seconds) if (rank == 0 and not args.skip_cpu) else None
     if rank == 0:
         line = {
@@ -590,6 +647,7 @@ def run_gpu(args):
             "pipeline_kernel": pipeline_kernel_stats(timing),
             "cpu_baseline": cpu,
             "batched": batched,
+            "basis_pruning": prune_info,
         }
         print(json.dumps(line))
     if world > 1:

@@ -176,55 +176,93 @@ class BasisNet:
         return y[:n]
 
 
-def ground_state_samples(eng, models, k_start=120):
-    """(padded states [N, WORDS], log10 weights [N] float32) of the ground states of ``models``
-    from plain exact diagonalisation (one ragged launch per convergence round)."""
+def ground_state_samples(eng, models, n_states=1, k_start=120):
+    """(padded states [N, WORDS], log10 weights [N] float32) of the basis states of ``models``
+    from plain exact diagonalisation (one ragged launch per convergence round).  The weight of
+    a state is its largest ``|<s|psi_q>|^2`` over the ``n_states`` lowest eigenstates."""
     from .ensemble import ModelSectors, ensemble_ground_states
 
     secs = [ModelSectors(eng, m) for m in models]
-    _, psis = ensemble_ground_states(eng, secs, 1, k_start=k_start, slaterWeightMin=0.0)
+    _, psis = ensemble_ground_states(eng, secs, n_states, k_start=k_start, slaterWeightMin=0.0)
     st, lw = [], []
     for ps in psis:
-        s, a = ps[0]
+        s = ps[0][0]
+        w2 = None
+        for _, a in ps:  # every eigenvector holds the whole sorted basis (no truncation)
+            q = a[:, 0] ** 2 + a[:, 1] ** 2
+            w2 = q if w2 is None else torch.maximum(w2, q)
         st.append(pad_words(s))
-        w2 = (a[:, 0] ** 2 + a[:, 1] ** 2).clamp_min(FLOOR)
-        lw.append(torch.log10(w2).to(torch.float32))
+        lw.append(torch.log10(w2.clamp_min(FLOOR)).to(torch.float32))
     return torch.cat(st), torch.cat(lw)
 
 
-def pruned_ground_state(eng, model, keep, ranking):
-    """Ground-state energy on the ``keep`` fraction of the model's basis ranked by
-    ``ranking`` ("net", "diagonal" or "random"), against the full basis.
+def prune_basis(n_spin_orbitals, basis, net, keep):
+    """The ``keep`` fraction of ``basis`` (upstream ``bytes`` states) with the highest
+    predicted weights, in the caller's order; pass it to ``finite.eigensystem`` as the basis."""
+    from .finite import _SortedBasis
 
-    ``ranking`` may also be a BasisNet (ranks by its prediction).  Returns a dict with the
-    full and pruned energies, the error (eV, >= 0 by the variational principle) and sizes."""
+    eng = net.eng
+    basis = list(basis)
+    sb = _SortedBasis(eng, basis, int(n_spin_orbitals))
+    m = max(1, int(round(keep * len(basis))))
+    score = net.predict(pad_words(sb.given))
+    top = torch.sort(torch.topk(score.to(torch.float64), m).indices).values.cpu().numpy()
+    return [basis[i] for i in top]
+
+
+def _scores(eng, sb, csr, ranking):
+    N = sb.sorted.shape[0]
+    if isinstance(ranking, BasisNet):
+        return ranking.predict(pad_words(sb.sorted)).to(torch.float64)
+    if ranking == "diagonal":
+        rows = torch.repeat_interleave(torch.arange(N, device=eng.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
+        diag = torch.zeros(N, dtype=torch.float64, device=eng.device)
+        on = rows == csr.col.to(torch.int64)
+        vals = csr.val_r if csr.val_r is not None else csr.val_c[:, 0]
+        diag[rows[on]] = vals[on]
+        return -diag
+    if ranking == "random":
+        gen = torch.Generator(device=eng.device)
+        gen.manual_seed(0)
+        return torch.rand(N, device=eng.device, generator=gen, dtype=torch.float64)
+    raise ValueError("ranking must be a BasisNet, 'diagonal' or 'random'")
+
+
+def evaluate_pruning(eng, model, keeps, rankings, n_states=1):
+    """Lowest ``n_states`` energies on the best-ranked ``keep`` fraction of the model's basis for
+    every keep in ``keeps`` and every ranking in ``rankings`` ({name: BasisNet | "diagonal" |
+    "random"}; "diagonal" keeps the lowest diagonal energies, the ranking without a network),
+    against the full basis (the fallback and the judge).
+
+    Returns {name: {keep: dict(error (eV, largest over the states, >= 0 by the variational
+    principle), n_pruned, nnz_pruned)}} and the full-basis record."""
     from .finite import _device_hamiltonian, _device_op, _SortedBasis, eig_lowest, get_basis
 
     n = model.n_spin_orbitals
     dop = _device_op(model.hOp, eng)
     sb = _SortedBasis(eng, list(get_basis(*model.basis_args())), n)
     csr = _device_hamiltonian(eng, dop, sb)
-    e_full, _ = eig_lowest(eng, csr, 1)
+    e_full, _ = eig_lowest(eng, csr, n_states)
     N = sb.sorted.shape[0]
-    m = max(1, int(round(keep * N)))
-    if isinstance(ranking, BasisNet):
-        score = ranking.predict(pad_words(sb.sorted))
-    elif ranking == "diagonal":
-        rows = torch.repeat_interleave(torch.arange(N, device=eng.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
-        diag = torch.zeros(N, dtype=torch.float64, device=eng.device)
-        on = rows == csr.col.to(torch.int64)
-        vals = csr.val_r if csr.val_r is not None else csr.val_c[:, 0]
-        diag[rows[on]] = vals[on]
-        score = -diag
-    elif ranking == "random":
-        gen = torch.Generator(device=eng.device)
-        gen.manual_seed(0)
-        score = torch.rand(N, device=eng.device, generator=gen)
-    else:
-        raise ValueError("ranking must be a BasisNet, 'diagonal' or 'random'")
-    top = torch.sort(torch.topk(score.to(torch.float64), m).indices).values
-    sub = sb.sorted[top].contiguous()
-    csr_p = eng.build_csr(sub, dop, None)
-    e_p, _ = eig_lowest(eng, csr_p, 1)
-    return dict(e_full=float(e_full[0]), e_pruned=float(e_p[0]), error=float(e_p[0] - e_full[0]), n_full=int(N),
-                n_pruned=int(m), nnz_full=int(csr.nnz), nnz_pruned=int(csr_p.nnz))
+    out = {}
+    for name, ranking in rankings.items():
+        score = _scores(eng, sb, csr, ranking)
+        out[name] = {}
+        for keep in keeps:
+            m = max(1, int(round(keep * N)))
+            top = torch.sort(torch.topk(score, m).indices).values
+            csr_p = eng.build_csr(sb.sorted[top].contiguous(), dop, None)
+            e_p, _ = eig_lowest(eng, csr_p, n_states)
+            q = min(len(e_full), len(e_p))
+            out[name][keep] = dict(error=float(np.max(np.asarray(e_p[:q]) - np.asarray(e_full[:q]))), n_pruned=int(m),
+                                   nnz_pruned=int(csr_p.nnz))
+    full = dict(e=[float(x) for x in e_full], n=int(N), nnz=int(csr.nnz))
+    return out, full
+
+
+def pruned_ground_state(eng, model, keep, ranking, n_states=1):
+    """``evaluate_pruning`` for one keep fraction and one ranking; returns a flat dict."""
+    res, full = evaluate_pruning(eng, model, [keep], {"r": ranking}, n_states)
+    r = res["r"][keep]
+    return dict(error=r["error"], n_full=full["n"], n_pruned=r["n_pruned"], nnz_full=full["nnz"],
+                nnz_pruned=r["nnz_pruned"], e_full=full["e"])

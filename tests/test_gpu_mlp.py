@@ -94,3 +94,11 @@ def test_trained_network_prunes_better_than_random(eng):
     r_rand = pruning.pruned_ground_state(eng, held, 0.5, "random")
     assert r_net["error"] >= -1e-9 and r_net["error"] <= 1e-4, r_net
     assert r_net["error"] < r_diag["error"] and r_net["error"] < r_rand["error"], (r_net, r_diag, r_rand)
+    # the drop-in path: pruned bytes basis through finite.eigensystem
+    from impuritymodel_gb300 import finite
+
+    basis = finite.get_basis(*held.basis_args())
+    kept = pruning.prune_basis(held.n_spin_orbitals, basis, net, 0.5)
+    assert len(kept) == r_net["n_pruned"] and set(kept) <= set(basis)
+    es, _ = finite.eigensystem(held.n_spin_orbitals, held.hOp, kept, 1)
+    assert abs(es[0] - (r_net["e_full"][0] + r_net["error"])) < 1e-9
