@@ -570,3 +570,23 @@ def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", 
         for vi in range(len(es))
     ]
     return np.asarray(es), psis
+
+# 3d-shell observables under upstream's names (finite.py:121-174, 843-1298)
+from .observables import (  # noqa: E402,F401
+    applyLminus3d,
+    applyLplus3d,
+    applyLz3d,
+    applySminus3d,
+    applySplus3d,
+    applySz3d,
+    getDensityMatrix,
+    getDensityMatrixCubic,
+    getEgT2gOccupation,
+    getLsqr3d,
+    getLz3d,
+    getSsqr3d,
+    getSz3d,
+    getTraceDensityMatrix,
+    printExpValues,
+    printThermalExpValues,
+)

@@ -346,6 +346,17 @@ int edgpu_mlp_adam(float* p, const float* g, float* m, float* v, int64_t n, floa
 /* BF16 copy Wb of a row-major FP32 [rows][cols] matrix and/or of its transpose Wt. */
 int edgpu_mlp_to_bf16(const float* Wf, int rows, int cols, void* Wb, void* Wt, void* stream);
 
+/*
+ * One-body density matrices of R states: out[r][p] = <psi_r| T_p |psi_r> (complex128) for P
+ * packed two-operator terms T_p (edgpu_terms ops encoding, e.g. c_j^dagger c_i).  State r is
+ * states[run_off[r] .. run_off[r+1]) (n_words words each, SORTED within the state) with
+ * complex128 amplitudes.  Replaces the per-pair loops of upstream getDensityMatrix
+ * (impurityModel/ed/finite.py:967-1012); the occupation observables of finite.py:843-1112 are
+ * linear in its result.  R <= 65535.
+ */
+int edgpu_density_matrix(int n_words, const uint64_t* states, const double* amps, const int64_t* run_off, int R,
+                         const uint64_t* pair_ops, int P, double* out, void* stream);
+
 /* Ritz vectors of a ragged batch: X[r][q] = sum_{k < k_len[r]} S[r][k][q] V_r[k] for q < Q
  * (S real [n_runs][K][Q]); X packed complex128 at offset Q * run_vec0[r]. */
 int edgpu_combine_ragged(const double* V, const edgpu_ragged* rg, const int64_t* run_V0, const int32_t* k_len,

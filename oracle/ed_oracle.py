@@ -734,3 +734,163 @@ def get_rixs_map(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, d
                         n_spin_orbitals, e, psi3, hOp, wLoss, delta2, krylovSize, slaterWeightMin, restrictions,
                         memo=memo_gnd, exact=exact, perturb=perturb)
     return gs
+
+
+# ---------------------------------------------------------------------------------------
+# 3d-shell observables (impurityModel/ed/finite.py:843-1298)
+# ---------------------------------------------------------------------------------------
+
+
+def _n_spin_orbitals(nBaths):
+    return sum(2 * (2 * l + 1) + nb for l, nb in nBaths.items())
+
+
+def spherical_to_cubic_d():
+    """``finite.get_spherical_2_cubic_matrix(l=2)`` (finite.py:220-268): column j is cubic
+    harmonic j (two eg, then three t2g) in spherical harmonics m = -2..2."""
+    u = np.zeros((5, 5), dtype=complex)
+    r = 1 / np.sqrt(2)
+    u[2, 0] = 1
+    u[0, 1] = u[4, 1] = r
+    u[1, 2] = u[3, 2] = -1j * r
+    u[1, 3], u[3, 3] = r, -r
+    u[0, 4], u[4, 4] = 1j * r, -1j * r
+    return u
+
+
+def _hop(n, psi, i_create, j_annihilate):
+    """c_i^dagger c_j psi without pruning (upstream ``c(n, i, a(n, j, psi))``)."""
+    return apply_op(n, {((i_create, "c"), (j_annihilate, "a")): 1.0}, psi, slaterWeightMin=0.0)
+
+
+def _inner(a, b):
+    return sum(np.conj(a[s]) * v for s, v in b.items() if s in a)
+
+
+def density_matrix(nBaths, psi, l=2):
+    """``finite.getDensityMatrix`` (finite.py:967-1012): entry ((l,si,mi),(l,sj,mj)) =
+    <psi| c_j^dagger c_i |psi>, nonzero entries only, loop order si, sj, mi, mj."""
+    n = _n_spin_orbitals(nBaths)
+    out = {}
+    for si in range(2):
+        for sj in range(2):
+            for mi in range(-l, l + 1):
+                for mj in range(-l, l + 1):
+                    i = _c2i(nBaths, (l, si, mi))
+                    j = _c2i(nBaths, (l, sj, mj))
+                    v = _inner(psi, _hop(n, psi, j, i))
+                    if v != 0:
+                        out[((l, si, mi), (l, sj, mj))] = v
+    return out
+
+
+def density_matrix_cubic(nBaths, psi):
+    """``finite.getDensityMatrixCubic`` (finite.py:1015-1060): n_cub = u^dagger n_sph u per
+    spin block, keys ((si, i), (sj, j))."""
+    nsph = density_matrix(nBaths, psi)
+    u = spherical_to_cubic_d()
+    out = {}
+    for i in range(5):
+        for j in range(5):
+            for si in range(2):
+                for sj in range(2):
+                    for k, mk in enumerate(range(-2, 3)):
+                        for m, mm in enumerate(range(-2, 3)):
+                            e = ((2, si, mm), (2, sj, mk))
+                            if e in nsph:
+                                t = np.conj(u[m, i]) * nsph[e] * u[k, j]
+                                if t != 0:
+                                    out[((si, i), (sj, j))] = out.get(((si, i), (sj, j)), 0) + t
+    return out
+
+
+def eg_t2g_occupation(nBaths, psi):
+    """``finite.getEgT2gOccupation`` (finite.py:1063-1112): [eg_dn, eg_up, t2g_dn, t2g_up]."""
+    n = _n_spin_orbitals(nBaths)
+    u = spherical_to_cubic_d()
+    occ = [0j, 0j, 0j, 0j]
+    for i in range(5):
+        for j, mj in enumerate(range(-2, 3)):
+            for k, mk in enumerate(range(-2, 3)):
+                for s in range(2):
+                    jj = _c2i(nBaths, (2, s, mj))
+                    kk = _c2i(nBaths, (2, s, mk))
+                    v = u[j, i] * np.conj(u[k, i]) * _inner(psi, _hop(n, psi, jj, kk))
+                    occ[(0 if i < 2 else 2) + s] += v
+    return [o.real if abs(o.imag) < 1e-12 else o for o in occ]
+
+
+def trace_density_matrix(nBaths, psi, l=2):
+    """``finite.getTraceDensityMatrix`` (finite.py:937-964): sum over states of |amp|^2 times
+    the number of occupied l-shell spin-orbitals."""
+    n = _n_spin_orbitals(nBaths)
+    idx = [_c2i(nBaths, (l, s, m)) for s in range(2) for m in range(-l, l + 1)]
+    return sum(abs(a) ** 2 * sum(1 for i in idx if i in bytes_to_tuple(st, n)) for st, a in psi.items())
+
+
+def lz3d(nBaths, psi):
+    """``finite.getLz3d`` (finite.py:843-866)."""
+    n = _n_spin_orbitals(nBaths)
+    idx = {_c2i(nBaths, (2, s, m)): m for s in range(2) for m in range(-2, 3)}
+    return sum(sum(idx[i] for i in bytes_to_tuple(st, n) if i in idx) * abs(a) ** 2 for st, a in psi.items())
+
+
+def sz3d(nBaths, psi):
+    """``finite.getSz3d`` (finite.py:869-892)."""
+    n = _n_spin_orbitals(nBaths)
+    idx = {_c2i(nBaths, (2, s, m)): (0.5 if s == 1 else -0.5) for s in range(2) for m in range(-2, 3)}
+    return sum(sum(idx[i] for i in bytes_to_tuple(st, n) if i in idx) * abs(a) ** 2 for st, a in psi.items())
+
+
+def one_body_op_3d(nBaths, kind):
+    """The operator dicts of ``finite.applySz3d / applyLz3d / applySplus3d / applyLplus3d /
+    applySminus3d / applyLminus3d`` (finite.py:1115-1298), terms in upstream's loop order."""
+    c = lambda s, m: _c2i(nBaths, (2, s, m))  # noqa: E731
+    op = {}
+    if kind == "Sz":
+        for s in range(2):
+            for m in range(-2, 3):
+                op[((c(s, m), "c"), (c(s, m), "a"))] = 0.5 if s == 1 else -0.5
+    elif kind == "Lz":
+        for s in range(2):
+            for m in range(-2, 3):
+                op[((c(s, m), "c"), (c(s, m), "a"))] = float(m)
+    elif kind == "S+":
+        for m in range(-2, 3):
+            op[((c(1, m), "c"), (c(0, m), "a"))] = 1.0
+    elif kind == "S-":
+        for m in range(-2, 3):
+            op[((c(0, m), "c"), (c(1, m), "a"))] = 1.0
+    elif kind == "L+":
+        for s in range(2):
+            for m in range(-2, 2):
+                op[((c(s, m + 1), "c"), (c(s, m), "a"))] = sqrt((2 - m) * (2 + m + 1))
+    elif kind == "L-":
+        for s in range(2):
+            for m in range(-1, 3):
+                op[((c(s, m - 1), "c"), (c(s, m), "a"))] = sqrt((2 + m) * (2 - m + 1))
+    else:
+        raise ValueError(kind)
+    return op
+
+
+def apply_one_body_3d(nBaths, psi, kind):
+    """Upstream's applyX3d: sum over the terms of ``coefficient * c_i^dagger c_j psi``."""
+    n = _n_spin_orbitals(nBaths)
+    out = {}
+    for key, coef in one_body_op_3d(nBaths, kind).items():
+        for s, v in apply_op(n, {key: 1.0}, psi, slaterWeightMin=0.0).items():
+            out[s] = out.get(s, 0) + coef * v
+    return out
+
+
+def lsqr3d(nBaths, psi):
+    """``finite.getLsqr3d`` (finite.py:916-934): |Lz psi|^2 + (|L+ psi|^2 + |L- psi|^2) / 2."""
+    f = lambda k: norm2(apply_one_body_3d(nBaths, psi, k))  # noqa: E731
+    return float(np.real(f("Lz") + 0.5 * (f("L+") + f("L-"))))
+
+
+def ssqr3d(nBaths, psi):
+    """``finite.getSsqr3d`` (finite.py:895-913)."""
+    f = lambda k: norm2(apply_one_body_3d(nBaths, psi, k))  # noqa: E731
+    return float(np.real(f("Sz") + 0.5 * (f("S+") + f("S-"))))

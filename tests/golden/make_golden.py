@@ -205,5 +205,47 @@ def main():
     print("nio done %.1fs" % (time.time() - t0))
 
 
+def observables():
+    """Upstream's 3d observables (finite.py:843-1298) on the stored eigenstates of the 26- and
+    66-spin-orbital models: density matrices (spherical, cubic), N(3d), eg/t2g occupations,
+    Lz, Sz, L^2, S^2, and the S/L ladder- and z-operator results on the lowest state."""
+    finite, spectra, psr, create, remove = refenv.load()
+    from tests.golden.fixtures import decode_psi, load
+
+    out = {}
+    for tag, cfg, fname in (("c1", "config1", "config1.npz"), ("c2", "config2", "config2.npz")):
+        mod = M.make_model(cfg)
+        z = load(fname)
+        n = int(z["n_spin_orbitals"])
+        nb = mod.nBaths
+        k = 0
+        while ("eig%d" % k + "_states") in z.files:
+            k += 1
+        psis = [decode_psi(z, "eig%d" % i, n) for i in range(k)]
+        dm = np.zeros((k, 10, 10), dtype=complex)
+        dmc = np.zeros((k, 10, 10), dtype=complex)
+        vals = np.zeros((k, 9))
+        for i, psi in enumerate(psis):
+            for ((l, si, mi), (l2, sj, mj)), v in finite.getDensityMatrix(nb, psi).items():
+                dm[i, si * 5 + mi + 2, sj * 5 + mj + 2] = v
+            for ((si, ii), (sj, jj)), v in finite.getDensityMatrixCubic(nb, psi).items():
+                dmc[i, si * 5 + ii, sj * 5 + jj] = v
+            occ = finite.getEgT2gOccupation(nb, psi)
+            vals[i] = [finite.getTraceDensityMatrix(nb, psi), *np.real(occ), finite.getLz3d(nb, psi),
+                       finite.getSz3d(nb, psi), finite.getLsqr3d(nb, psi), finite.getSsqr3d(nb, psi)]
+        out[tag + "_n_states"] = k
+        out[tag + "_dm"] = dm
+        out[tag + "_dm_cubic"] = dmc
+        out[tag + "_values"] = vals
+        for name in ("applySz3d", "applyLz3d", "applySplus3d", "applyLplus3d", "applySminus3d", "applyLminus3d"):
+            out.update(encode_psi(tag + "_" + name, getattr(finite, name)(nb, psis[0]), n))
+    np.savez_compressed(os.path.join(HERE, "observables.npz"), **out)
+    print("observables done")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["observables"]:
+        observables()
+    else:
+        main()
+        observables()

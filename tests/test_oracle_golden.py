@@ -204,3 +204,37 @@ def test_nio_shipped_xas_dat():
     dat = z["xas_dat"]
     assert np.abs(dat[:, 0] - w).max() < 1e-4
     assert np.abs(a.sum(axis=0) - dat[:, 1]).max() < 1.5e-4  # "%8.4f" columns
+
+
+def _dense(d, key):
+    out = np.zeros((10, 10), dtype=complex)
+    for k, v in d.items():
+        out[key(k)] = v
+    return out
+
+
+@pytest.mark.parametrize("tag,cfg,fname", [("c1", "config1", "config1.npz")])
+def test_observables_match_upstream(tag, cfg, fname):
+    """3d observables (finite.py:843-1298) on upstream's eigenstates against upstream's own
+    values (golden fixture observables.npz), 1e-12."""
+    z = load("observables.npz")
+    zc = load(fname)
+    mod = M.make_model(cfg)
+    n = int(zc["n_spin_orbitals"])
+    nb = mod.nBaths
+    for i in range(int(z[tag + "_n_states"])):
+        psi = decode_psi(zc, "eig%d" % i, n)
+        dm = _dense(O.density_matrix(nb, psi), lambda k: (k[0][1] * 5 + k[0][2] + 2, k[1][1] * 5 + k[1][2] + 2))
+        assert np.abs(dm - z[tag + "_dm"][i]).max() < 1e-12
+        dmc = _dense(O.density_matrix_cubic(nb, psi), lambda k: (k[0][0] * 5 + k[0][1], k[1][0] * 5 + k[1][1]))
+        assert np.abs(dmc - z[tag + "_dm_cubic"][i]).max() < 1e-12
+        vals = [O.trace_density_matrix(nb, psi), *np.real(O.eg_t2g_occupation(nb, psi)), O.lz3d(nb, psi),
+                O.sz3d(nb, psi), O.lsqr3d(nb, psi), O.ssqr3d(nb, psi)]
+        assert np.abs(np.array(vals) - z[tag + "_values"][i]).max() < 1e-11
+    psi0 = decode_psi(zc, "eig0", n)
+    for kind, name in (("Sz", "applySz3d"), ("Lz", "applyLz3d"), ("S+", "applySplus3d"), ("L+", "applyLplus3d"),
+                       ("S-", "applySminus3d"), ("L-", "applyLminus3d")):
+        ref = decode_psi(z, tag + "_" + name, n)
+        got = O.apply_one_body_3d(nb, psi0, kind)
+        keys = set(ref) | set(got)
+        assert max(abs(ref.get(s, 0) - got.get(s, 0)) for s in keys) < 1e-13
