@@ -561,3 +561,90 @@ def _transfer_matrix(eng, tdop, restr, core_basis):
     csr = CsrMatrix(rp, col[p].to(torch.int32).contiguous(), val_c=out_v[p].contiguous(), ncols=core_basis.shape[0])
     del w
     return _TransferMatrix(outs, csr)
+
+
+# ---------------------------------------------------------------------------------------
+# Output formats and the spectra driver (upstream spectra.py:36-293)
+# ---------------------------------------------------------------------------------------
+
+
+class NpzStore:
+    """Dataset store with the ``create_dataset(name, data=...)`` call of an h5py file, written
+    as one ``.npz`` on ``close()`` (same dataset names and shapes as upstream's spectra.h5;
+    h5py itself works as well when it is installed)."""
+
+    def __init__(self, filename):
+        self.filename = filename
+        self.data = {}
+
+    def create_dataset(self, name, data):
+        self.data[name] = np.asarray(data)
+        return self.data[name]
+
+    def close(self):
+        np.savez_compressed(self.filename, **self.data)
+
+
+def save_spectra_dat(filename, w, a):
+    """Upstream's text spectra (spectra.py:152-162): columns energy, sum over transition
+    operators, then each operator's thermally averaged spectrum; ``%8.4f``, same header."""
+    a = np.asarray(a)
+    tmp = [np.asarray(w), np.sum(a, axis=0)]
+    for i in range(a.shape[0]):
+        tmp.append(a[i, :])
+    np.savetxt(filename, np.array(tmp).T, fmt="%8.4f", header="E  sum  T1  T2  T3 ...")
+
+
+def save_rixs_bin(filename, wIn, wLoss, a):
+    """Upstream's RIXS.bin (spectra.py:276-285): float32 [n_wLoss + 1, n_wIn + 1], element
+    [0, 0] = n_wIn, first row wIn, first column wLoss, the rest the thermally averaged map
+    summed over in- and out-polarisations, transposed to [wLoss, wIn]."""
+    a_sum = np.sum(np.asarray(a), axis=(0, 1))
+    tmp = np.zeros((len(wLoss) + 1, len(wIn) + 1), dtype=np.float32)
+    tmp[0, 0] = len(wIn)
+    tmp[0, 1:] = wIn
+    tmp[1:, 0] = wLoss
+    tmp[1:, 1:] = a_sum.T
+    tmp.tofile(filename)
+
+
+def simulate_spectra(es, psis, hOp, T, w, delta, epsilons, wLoss, deltaNIXS, qsNIXS, liNIXS, ljNIXS, RiNIXS,
+                     RjNIXS, radialMesh, wIn, deltaRIXS, epsilonsRIXSin, epsilonsRIXSout, restrictions, h5f, nBaths,
+                     out_dir=".", precision=0):
+    """PS+IPS, XPS, NIXS, XAS and RIXS spectra with upstream's outputs (spectra.py:36-293):
+    datasets PS/PSthermal, XPS/XPSthermal, NIXS/NIXSthermal, XAS/XASthermal, RIXS/RIXSthermal
+    in ``h5f`` (an h5py file or NpzStore), text files PS.dat, XPS.dat, NIXS.dat, XAS.dat and
+    RIXS.bin in ``out_dir``.  Every spectrum family is one batched device computation."""
+    import os
+
+    from .models import dipole_ops, daggered_dipole_ops, inverse_photoemission_ops, photoemission_ops
+
+    n = sum(2 * (2 * ang + 1) + nb for ang, nb in nBaths.items())
+    es = np.asarray(es)
+    path = lambda f: os.path.join(out_dir, f)  # noqa: E731
+
+    def store(name, gs, mesh, fname):
+        a = thermal_average(es[: gs.shape[0]], -gs.imag, T=T)
+        h5f.create_dataset(name, data=-gs.imag)
+        h5f.create_dataset(name + "thermal", data=a)
+        save_spectra_dat(path(fname), mesh, a)
+
+    gs_ips = getSpectra(n, hOp, inverse_photoemission_ops(nBaths, l=2), psis, es, w, delta, restrictions,
+                        precision=precision)
+    gs_ps = -getSpectra(n, hOp, photoemission_ops(nBaths, l=2), psis, es, -w, -delta, restrictions,
+                        precision=precision)
+    store("PS", gs_ps + gs_ips, w, "PS.dat")
+    gs = -getSpectra(n, hOp, photoemission_ops(nBaths, l=1), psis, es, -w, -delta, restrictions,
+                     precision=precision)
+    store("XPS", gs, w, "XPS.dat")
+    gs = getSpectra(n, hOp, getNIXSOperators(nBaths, qsNIXS, liNIXS, ljNIXS, RiNIXS, RjNIXS, radialMesh), psis, es,
+                    wLoss, deltaNIXS, restrictions, precision=precision)
+    store("NIXS", gs, wLoss, "NIXS.dat")
+    gs = getSpectra(n, hOp, dipole_ops(nBaths, epsilons), psis, es, w, delta, restrictions, precision=precision)
+    store("XAS", gs, w, "XAS.dat")
+    gs = getRIXSmap(n, hOp, dipole_ops(nBaths, epsilonsRIXSin), daggered_dipole_ops(nBaths, epsilonsRIXSout), psis,
+                    es, wIn, wLoss, delta, deltaRIXS, restrictions, precision=precision)
+    a = thermal_average(es[: gs.shape[0]], -gs.imag, T=T)
+    h5f.create_dataset("RIXS", data=-gs.imag)
+    h5f.create_dataset("RIXSthermal", data=a)
+    save_rixs_bin(path("RIXS.bin"), wIn, wLoss, a)

@@ -86,3 +86,17 @@ def decode_restrictions(z, prefix):
 
 def load(name):
     return np.load(os.path.join(HERE, name), allow_pickle=False)
+
+
+def simulate_inputs():
+    """Inputs of the small spectra-driver case (26-orbital model, short meshes) shared by the
+    fixture generator and the GPU test of simulate_spectra."""
+    from impuritymodel_gb300 import models as M
+
+    mod = M.make_model("config1")
+    r, R = M.hydrogenic_3d_radial()
+    eps = [np.array(v, dtype=float) for v in ((1, 0, 0), (0, 1, 0), (0, 0, 1))]
+    qs = [1.0 * np.array([1, 1, 1]) / np.sqrt(3), 2.0 * np.array([1, 1, 1]) / np.sqrt(3)]
+    return dict(mod=mod, T=300.0, w=np.linspace(-25, 25, 400), delta=0.2, epsilons=eps,
+                wLoss=np.linspace(-2, 12, 200), deltaNIXS=0.1, qsNIXS=qs, liNIXS=2, ljNIXS=2, RiNIXS=R, RjNIXS=R,
+                radialMesh=r, wIn=np.linspace(-5, 10, 3), deltaRIXS=0.05, epsilonsRIXSin=eps, epsilonsRIXSout=eps)

@@ -243,9 +243,52 @@ def observables():
     print("observables done")
 
 
+def simulate():
+    """Upstream's spectra driver simulate_spectra (spectra.py:36-293) on the stored
+    eigenstates of the 26-orbital model: every dataset and output file it writes."""
+    import contextlib
+    import tempfile
+
+    finite, spectra, psr, create, remove = refenv.load()
+    import h5py  # the in-memory stand-in of _standins/
+
+    from tests.golden.fixtures import decode_psi, load
+
+    z = load("config1.npz")
+    n = int(z["n_spin_orbitals"])
+    psis = [decode_psi(z, "eig%d" % i, n) for i in range(len(z["es"]))]
+    from tests.golden.fixtures import simulate_inputs
+
+    a = simulate_inputs()
+    mod = a.pop("mod")
+    h5f = h5py.File("spectra.h5", "w")
+    out = {}
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)
+        try:
+            with contextlib.redirect_stdout(io.StringIO()):
+                spectra.simulate_spectra(z["es"], psis, mod.hOp, a["T"], a["w"], a["delta"], a["epsilons"], a["wLoss"],
+                                         a["deltaNIXS"], a["qsNIXS"], a["liNIXS"], a["ljNIXS"], a["RiNIXS"],
+                                         a["RjNIXS"], a["radialMesh"], a["wIn"], a["deltaRIXS"], a["epsilonsRIXSin"],
+                                         a["epsilonsRIXSout"], mod.restrictions, h5f, mod.nBaths)
+            for f in ("PS.dat", "XPS.dat", "NIXS.dat", "XAS.dat", "RIXS.bin"):
+                with open(f, "rb") as fh:
+                    out["file_" + f.replace(".", "_")] = np.frombuffer(fh.read(), dtype=np.uint8)
+        finally:
+            os.chdir(cwd)
+    for k, v in h5f.data.items():
+        out["ds_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "simulate_config1.npz"), **out)
+    print("simulate done")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["observables"]:
         observables()
+    elif sys.argv[1:] == ["simulate"]:
+        simulate()
     else:
         main()
         observables()
+        simulate()
