@@ -283,8 +283,29 @@ def simulate():
     print("simulate done")
 
 
+def nio_cli():
+    """Upstream's shipped NiO 50-bath run (scripts/run_Ni_NiO_Xbath.sh 50: get_spectra.py with
+    --nBaths 0 50 --nValBaths 0 50, other flags at their defaults): its inputs (the h0 operator
+    read with the restricted unpickler, the Ni 3d radial orbital) and its output files."""
+    root = refenv.REFERENCE_ROOT
+    with open(os.path.join(root, "h0/h0_NiO_50bath.pickle"), "rb") as fh:
+        h0 = _SafeUnpickler(fh).load()
+    keys = [repr(k) for k in h0.keys()]
+    vals = np.array([complex(v) for v in h0.values()])
+    radial = np.loadtxt(os.path.join(root, "radialOrbitals/Ni3d.dat"))
+    ref = os.path.join(root, "impurityModel/test/referenceOutput/Ni_NiO_50bath")
+    out = dict(h0_keys=np.array(keys), h0_vals=vals, radial=radial)
+    for f in ("PS.dat", "XPS.dat", "NIXS.dat", "XAS.dat", "RIXS.bin"):
+        with open(os.path.join(ref, f), "rb") as fh:
+            out["file_" + f.replace(".", "_")] = np.frombuffer(fh.read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "nio50_cli.npz"), **out)
+    print("nio cli done: %d h0 terms" % len(keys))
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["observables"]:
+    if sys.argv[1:] == ["nio_cli"]:
+        nio_cli()
+    elif sys.argv[1:] == ["observables"]:
         observables()
     elif sys.argv[1:] == ["simulate"]:
         simulate()
@@ -292,3 +313,4 @@ if __name__ == "__main__":
         main()
         observables()
         simulate()
+        nio_cli()
