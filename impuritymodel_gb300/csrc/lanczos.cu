@@ -968,6 +968,7 @@ extern "C" int edgpu_cfrac(const double* alpha, const double* beta, const int32_
 namespace edgpu {
 
 constexpr int kSmallThreads = 512;
+constexpr int kSmallBatch = 8;  // CSR entries loaded together per row
 
 // Deterministic block sum (fixed thread -> partial mapping and fixed tree).
 __device__ __forceinline__ double block_sum(double v, double* red) {
@@ -1127,10 +1128,39 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
   return df_fast_two_sum(p, e);
 }
 
-// Upstream's Lanczos recurrence in df64 for a real H (values as hi/lo float pairs); alpha
-// and beta are reduced in FP64 from df64 per-thread partials.  Vectors are float4
-// (re.hi, re.lo, im.hi, im.lo) in shared memory, one CTA per run.
-__global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const dfl s = df_two_sum(a.hi, b.hi);
+  return df_fast_two_sum(s.hi, __fadd_rn(__fadd_rn(s.lo, a.lo), b.lo));
+}
+
+// Deterministic double-float block sum on the FP32 pipe (fixed shuffle tree, then warp 0 over
+// the per-warp partials), broadcast to every thread.  red holds 33 values.
+__device__ __forceinline__ dfl df_block_sum(dfl v, dfl* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_add(v, {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    dfl t = lane < nw ? red[lane] : dfl{0.f, 0.f};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      t = df_add(t, {__shfl_down_sync(0xffffffffu, t.hi, o), __shfl_down_sync(0xffffffffu, t.lo, o)});
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// Upstream's Lanczos recurrence in df64 for a real H (values as hi/lo float pairs), one CTA
+// per run, vectors float4 (re.hi, re.lo, im.hi, im.lo) in shared memory.  alpha and beta are
+// reduced in double-float as well (GB300 retires FP64 at 1/64 of the FP32 rate, so even the
+// reductions' FP64 adds would dominate); one thread forms beta = sqrt(.) and 1/beta in FP64
+// per step and writes the FP64 outputs.
+__global__ void __launch_bounds__(kSmallThreads, 2) lanczos_small_df_kernel(
     int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv, int R,
     const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
     double* __restrict__ beta, int32_t* status) {
@@ -1138,9 +1168,11 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
   float4* A = reinterpret_cast<float4*>(sm);
   float4* B = A + n;
   float4* Cv = B + n;
-  double* red = reinterpret_cast<double*>(Cv + n);
+  dfl* red = reinterpret_cast<dfl*>(Cv + n);             // [33] reduction partials, [33] scalars
+  int32_t* srp = reinterpret_cast<int32_t*>(red + 68);  // row pointers, cached once
   const int tid = threadIdx.x, bs = blockDim.x;
   const dfl zero = {0.f, 0.f};
+  for (int64_t i = tid; i <= n; i += bs) srp[i] = (int32_t)rp[i];
   for (int r = blockIdx.x; r < R; r += gridDim.x) {
     const int km = k_max[r];
     if (km <= 0) continue;
@@ -1154,28 +1186,42 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
     float4* x = A;
     float4* p = B;
     float4* y = Cv;
-    double bprev = 0.0;
+    dfl bprev = zero;
     for (int j = 0; j < km; ++j) {
       dfl acc = zero;
       for (int64_t i = tid; i < n; i += bs) {
         dfl yr = zero, yi = zero;
-        const int64_t e1 = rp[i + 1];
-        for (int64_t e = rp[i]; e < e1; ++e) {
-          const float2 hh = hv[e];
-          const dfl h = {hh.x, hh.y};
-          const float4 xv = x[col[e]];
-          yr = df_fma(yr, h, {xv.x, xv.y});
-          yi = df_fma(yi, h, {xv.z, xv.w});
+        const int e1 = srp[i + 1];
+        // the row's CSR entries in batches of kSmallBatch independent loads (one L2 round
+        // trip per batch instead of one per entry), then the same sums in entry order
+        for (int e = srp[i]; e < e1; e += kSmallBatch) {
+          int c[kSmallBatch];
+          float2 hh[kSmallBatch];
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            const bool ok = e + u < e1;
+            c[u] = ok ? __ldg(col + e + u) : 0;
+            hh[u] = ok ? __ldg(hv + e + u) : make_float2(0.f, 0.f);
+          }
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            if (e + u < e1) {
+              const dfl h = {hh[u].x, hh[u].y};
+              const float4 xv = x[c[u]];
+              yr = df_fma(yr, h, {xv.x, xv.y});
+              yi = df_fma(yi, h, {xv.z, xv.w});
+            }
+          }
         }
         y[i] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
         const float4 xi = x[i];
         acc = df_fma(acc, yr, {xi.x, xi.y});
         acc = df_fma(acc, yi, {xi.z, xi.w});
       }
-      const double a = block_sum(df_val(acc), red);
-      if (tid == 0) alpha[(int64_t)r * K + j] = a;
+      const dfl a = df_block_sum(acc, red);
+      if (tid == 0) alpha[(int64_t)r * K + j] = df_val(a);
       if (j + 1 == km) break;
-      const dfl na = df_split(-a), nb = df_split(-bprev);
+      const dfl na = {-a.hi, -a.lo}, nb = {-bprev.hi, -bprev.lo};
       acc = zero;
       for (int64_t i = tid; i < n; i += bs) {
         const float4 w = y[i], xi = x[i], pi = p[i];
@@ -1185,22 +1231,26 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
         acc = df_fma(acc, wr, wr);
         acc = df_fma(acc, wi, wi);
       }
-      const double b = sqrt(block_sum(df_val(acc), red));
+      const dfl b2 = df_block_sum(acc, red);
       if (tid == 0) {
+        const double b = sqrt(df_val(b2));
         beta[(int64_t)r * K + j] = b;
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+        red[33] = df_split(b);
+        red[34] = df_split(b > 0.0 ? 1.0 / b : 0.0);
       }
-      const dfl ib = df_split(b > 0.0 ? 1.0 / b : 0.0);
+      __syncthreads();
+      const dfl ib = red[34];
       for (int64_t i = tid; i < n; i += bs) {
         const float4 w = y[i];
         const dfl vr = df_mul({w.x, w.y}, ib), vi = df_mul({w.z, w.w}, ib);
         p[i] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);  // v_{j-1}'s buffer becomes v_{j+1}
       }
+      bprev = red[33];
       __syncthreads();
       float4* t = p;
       p = x;
       x = t;
-      bprev = b;
     }
     __syncthreads();
   }
@@ -1208,7 +1258,8 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_df_kernel(
 
 size_t small_smem_bytes(int64_t n, int precision) {
   const size_t v = precision == 1 ? sizeof(float2) : sizeof(double2);  // df64 rows are float4
-  return 3 * v * (size_t)n + 34 * sizeof(double) + 16;
+  const size_t rows = precision == 3 ? sizeof(int32_t) * (size_t)(n + 1) : 0;  // cached row pointers
+  return 3 * v * (size_t)n + 68 * sizeof(double) + rows + 16;
 }
 
 bool small_fits(int64_t n, int precision) { return small_smem_bytes(n, precision) <= 200 * 1024; }
