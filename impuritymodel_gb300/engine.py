@@ -398,6 +398,66 @@ class Engine:
             out.append((ukeys[b[r]:b[r + 1], 1:].contiguous(), sums[b[r]:b[r + 1]].contiguous()))
         return out
 
+    def apply_vectors_multi(self, run_states, run_amps, dops, restr, weight_min):
+        """``[op][run] -> (states, amps)``: every operator of ``dops`` applied to every run.
+
+        The same results, bit for bit, as one ``apply_vectors`` call per operator, with one
+        scan, one sort and one unique over all (operator, run) pairs instead of one each per
+        operator (the count and fill passes still run per operator)."""
+        runs, n_ops = len(run_states), len(dops)
+        w = run_states[0].shape[1] if runs else 1
+        empty = (torch.empty((0, w), dtype=torch.int64, device=self.device),
+                 torch.empty((0, 2), dtype=torch.float64, device=self.device))
+        if runs == 0 or n_ops == 0:
+            return [[] for _ in range(n_ops)] if runs == 0 else []
+        sizes = [int(x.shape[0]) for x in run_states]
+        n = sum(sizes)
+        if n == 0:
+            return [[empty] * runs for _ in range(n_ops)]
+        states = torch.cat(run_states, 0).contiguous()
+        amps = torch.cat(run_amps, 0).contiguous()
+        rp = C.byref(restr) if restr is not None else None
+        counts = torch.zeros(n_ops * n, dtype=torch.int64, device=self.device)
+        for o, dop in enumerate(dops):
+            if dop.n_terms:
+                L.check(self.lib.edgpu_apply_vector(w, _ptr(states), None, n, C.byref(dop.terms), rp, None,
+                                                    _ptr(counts[o * n:]), None, None, self.stream),
+                        "apply_vector(count)")
+        offsets = self.scan(counts)
+        total = int(offsets[-1].item())
+        if total == 0:
+            return [[empty] * runs for _ in range(n_ops)]
+        out_s = torch.empty((total, w), dtype=torch.int64, device=self.device)
+        out_v = torch.empty((total, 2), dtype=torch.float64, device=self.device)
+        for o, dop in enumerate(dops):
+            if dop.n_terms:
+                L.check(self.lib.edgpu_apply_vector(w, _ptr(states), _ptr(amps), n, C.byref(dop.terms), rp,
+                                                    _ptr(offsets[o * n:]), None, _ptr(out_s), _ptr(out_v),
+                                                    self.stream), "apply_vector(fill)")
+        run_of_input = torch.repeat_interleave(torch.arange(runs, device=self.device),
+                                               torch.tensor(sizes, device=self.device))
+        group = (torch.arange(n_ops, device=self.device).view(-1, 1) * runs + run_of_input.view(1, -1)).reshape(-1)
+        group_of_emit = torch.repeat_interleave(group, offsets[1:] - offsets[:-1])
+        keys = torch.cat([group_of_emit.view(-1, 1), out_s], 1).contiguous()
+        payload = torch.arange(total, dtype=torch.int32, device=self.device)
+        self.sort_states(keys, payload)
+        ukeys, first, sums = self.unique_sorted(keys, payload, out_v)
+        a2 = torch.hypot(sums[:, 0], sums[:, 1]) ** 2
+        keep = a2 >= weight_min
+        ukeys, first, sums = ukeys[keep], first[keep], sums[keep]
+        order = torch.argsort(first.to(torch.int64))  # dict insertion order within each group
+        ukeys, sums = ukeys[order], sums[order]
+        bounds = torch.searchsorted(ukeys[:, 0].contiguous(),
+                                    torch.arange(n_ops * runs + 1, device=self.device)).cpu().tolist()
+        out = []
+        for o in range(n_ops):
+            row = []
+            for r in range(runs):
+                g = o * runs + r
+                row.append((ukeys[bounds[g]:bounds[g + 1], 1:].contiguous(), sums[bounds[g]:bounds[g + 1]].contiguous()))
+            out.append(row)
+        return out
+
     # -- sectors --------------------------------------------------------------------------
     def expand(self, basis0, dop, restr, weight_min=1e-12):
         """Closure of ``basis0`` under the operator (upstream expand_basis, finite.py:1696-1803).

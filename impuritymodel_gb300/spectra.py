@@ -300,8 +300,8 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
     ne = len(es)
     w = np.asarray(w, dtype=np.float64)
     run_states, run_amps, e_runs = [], [], []
-    for tdop in t_dops:
-        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], tdop, restr, slaterWeightMin)
+    for outs in eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], t_dops, restr,
+                                        slaterWeightMin):
         for i, (s_, a_) in enumerate(outs):
             run_states.append(s_)
             run_amps.append(a_)
@@ -413,8 +413,8 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
         return gs
     # 1. core-hole states psi1 = T_in psi
     psi1 = {}
-    for t_in, tdop in enumerate(tin_dops):
-        outs = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], tdop, restr, slaterWeightMin)
+    for t_in, outs in enumerate(eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], tin_dops,
+                                                        restr, slaterWeightMin)):
         for ie, o in enumerate(outs):
             psi1[(t_in, ie)] = o
     nonempty = [v[0] for v in psi1.values() if v[0].shape[0]]

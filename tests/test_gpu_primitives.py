@@ -115,3 +115,22 @@ def test_reorth_fused_matches_per_step_kernels(eng, config, k_cap):
     th1 = scipy.linalg.eigh_tridiagonal(a1, b1[:-1], eigvals_only=True)[:5]
     th0 = scipy.linalg.eigh_tridiagonal(a0, b0[:-1], eigvals_only=True)[:5]
     assert np.abs(th1 - th0).max() < 1e-10
+
+
+def test_apply_vectors_multi_equals_per_operator_calls(eng):
+    """All operators at once (one scan/sort/unique) give bit for bit the per-operator results."""
+    from impuritymodel_gb300 import finite
+
+    mod = M.make_model("config1")
+    n = mod.n_spin_orbitals
+    es, psi_t = finite.eigensystem_device(eng, finite._device_op(mod.hOp, eng),
+                                          finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n), 3)
+    from impuritymodel_gb300.engine import make_restrictions
+
+    restr = make_restrictions(mod.restrictions, n)
+    dops = [finite._device_op(t, eng) for t in mod.xas_ops() + mod.ps_ops()[:2]]
+    multi = eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], dops, restr, 1e-7)
+    for o, dop in enumerate(dops):
+        single = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], dop, restr, 1e-7)
+        for (s1, a1), (s2, a2) in zip(single, multi[o]):
+            assert torch.equal(s1, s2) and torch.equal(a1, a2)
