@@ -169,6 +169,9 @@ class CsrMatrix:
         return 16 if self.val_c is not None else 8
 
 
+COMPONENTS_KERNEL_MAX_ROWS = 1 << 16  # single-CTA label propagation of edgpu_components
+
+
 class Engine:
     """One engine per CUDA device.  Holds the library handle, a status word and a workspace."""
 
@@ -495,6 +498,10 @@ class Engine:
     def components(self, csr):
         """Connected-component label (smallest member index) of every sector state."""
         n = csr.n
+        if 0 < n <= COMPONENTS_KERNEL_MAX_ROWS:
+            labels = torch.empty(n, dtype=torch.int64, device=self.device)
+            L.check(self.lib.edgpu_components(C.byref(csr.struct()), _ptr(labels), None, self.stream), "components")
+            return labels
         labels = torch.arange(n, dtype=torch.int64, device=self.device)
         if csr.nnz == 0:
             return labels

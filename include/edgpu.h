@@ -357,6 +357,15 @@ int edgpu_mlp_to_bf16(const float* Wf, int rows, int cols, void* Wb, void* Wt, v
 int edgpu_density_matrix(int n_words, const uint64_t* states, const double* amps, const int64_t* run_off, int R,
                          const uint64_t* pair_ops, int P, double* out, void* stream);
 
+/*
+ * Connected components of a sector's (symmetric) sparsity pattern: label[i] = smallest state
+ * index of i's component, for n <= 65536 in one launch (one CTA iterating minimum-label
+ * propagation with pointer jumping on chip until a round changes nothing; *rounds receives
+ * the number of rounds when not NULL).  Gives the dimension of each Green's-function run's
+ * basis closure, upstream's Krylov-size cap (impurityModel/ed/spectra.py:646-676).
+ */
+int edgpu_components(const edgpu_csr* h, int64_t* label, int32_t* rounds, void* stream);
+
 /* Ritz vectors of a ragged batch: X[r][q] = sum_{k < k_len[r]} S[r][k][q] V_r[k] for q < Q
  * (S real [n_runs][K][Q]); X packed complex128 at offset Q * run_vec0[r]. */
 int edgpu_combine_ragged(const double* V, const edgpu_ragged* rg, const int64_t* run_V0, const int32_t* k_len,

@@ -134,3 +134,28 @@ def test_apply_vectors_multi_equals_per_operator_calls(eng):
         single = eng.apply_vectors([p[0] for p in psi_t], [p[1] for p in psi_t], dop, restr, 1e-7)
         for (s1, a1), (s2, a2) in zip(single, multi[o]):
             assert torch.equal(s1, s2) and torch.equal(a1, a2)
+
+
+def test_components_kernel_equals_label_propagation(eng):
+    """One-launch component labels equal scipy's connected components (smallest member index
+    as label) on the XAS sector of the 26-orbital model."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+
+    from impuritymodel_gb300 import finite, spectra
+    from impuritymodel_gb300.engine import make_restrictions
+
+    mod = M.make_model("config1")
+    n = mod.n_spin_orbitals
+    dop = finite._device_op(mod.hOp, eng)
+    restr = make_restrictions(mod.restrictions, n)
+    es, psi_t = finite.eigensystem_device(eng, dop, finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n), 3)
+    outs = eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t],
+                                   [finite._device_op(t, eng) for t in mod.xas_ops()], restr, 1e-7)
+    sec = spectra.Sector(eng, dop, restr, torch.cat([s for row in outs for s, _ in row]))
+    csr = sec.csr
+    lab = eng.components(csr).cpu().numpy()
+    H = sp.csr_matrix((np.ones(csr.nnz), csr.col.cpu().numpy(), csr.row_ptr.cpu().numpy()), shape=(csr.n, csr.n))
+    nc, cc = connected_components(H, directed=False)
+    ref = np.array([np.nonzero(cc == cc[i])[0].min() for i in range(csr.n)])
+    assert np.array_equal(lab, ref)
