@@ -527,13 +527,14 @@ def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMi
     es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3))
     vec_given = torch.empty_like(X)
     vec_given[:, sb.perm] = X
-    psis = []
-    for vi in range(len(es)):
-        v = vec_given[vi]
-        keep = (v.real ** 2 + v.imag ** 2) >= slaterWeightMin
-        idx = torch.nonzero(keep).flatten()
-        amps = torch.view_as_real(v[idx]).contiguous()
-        psis.append((sb.given[idx].contiguous(), amps))
+    k = len(es)
+    keep = (vec_given[:k].real ** 2 + vec_given[:k].imag ** 2) >= slaterWeightMin
+    vi, idx = torch.nonzero(keep, as_tuple=True)  # grouped by eigenvector, states in caller order
+    bounds = torch.searchsorted(vi.contiguous(), torch.arange(k + 1, device=vi.device)).cpu().tolist()
+    amps_all = torch.view_as_real(vec_given[vi, idx]).contiguous()
+    states_all = sb.given[idx]
+    psis = [(states_all[bounds[q]:bounds[q + 1]].contiguous(), amps_all[bounds[q]:bounds[q + 1]].contiguous())
+            for q in range(k)]
     return np.asarray(es), psis
 
 

@@ -85,20 +85,28 @@ class Sector:
         self._sizes = None
 
     def components(self, eng):
+        """Component label of every state (its smallest member) and the size of each component
+        stored at its label's index (0 elsewhere); no host synchronisation."""
         if self._labels is None:
             labels = eng.components(self.csr)
-            uniq, inv = torch.unique(labels, return_inverse=True)
-            self._labels = inv
-            self._sizes = torch.bincount(inv, minlength=uniq.numel())
+            sizes = torch.zeros(self.n, dtype=torch.int64, device=eng.device)
+            sizes.index_add_(0, labels, torch.ones_like(labels))
+            self._labels, self._sizes = labels, sizes
         return self._labels, self._sizes
 
     def run_dims(self, eng, rows, run_of_row, runs):
-        """Closure dimension of each run's support (upstream len(basis_index) per getGreen)."""
+        """Closure dimension of each run's support (upstream len(basis_index) per getGreen):
+        the summed sizes of the distinct components its start states touch."""
         labels, sizes = self.components(eng)
-        nc = sizes.numel()
-        pair = torch.unique(run_of_row * nc + labels[rows])
+        n = self.n
+        comp = labels[rows]
+        if runs * n <= (1 << 26):
+            touched = torch.zeros((runs, n), dtype=torch.bool, device=eng.device)
+            touched[run_of_row, comp] = True
+            return (touched.to(torch.int64) * sizes.view(1, -1)).sum(1)
+        pair = torch.unique(run_of_row * n + comp)
         dims = torch.zeros(runs, dtype=torch.int64, device=eng.device)
-        dims.index_add_(0, pair // nc, sizes[pair % nc])
+        dims.index_add_(0, pair // n, sizes[pair % n])
         return dims
 
 
@@ -154,8 +162,7 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
         sector = Sector(eng, dop, restr, states[n2[run_of_row] > 0], precision)
     _mark(stages, "green:sector")
     rows = eng.lookup(sector.basis, states)
-    if bool((rows < 0).any()):
-        raise RuntimeError("start state outside the sector basis")
+    missing = (rows < 0).any()  # checked with the run dimensions below (one synchronisation)
     # live runs renumbered 0..L-1
     remap = torch.full((runs,), -1, dtype=torch.int64, device=eng.device)
     live_t = torch.from_numpy(live).to(eng.device)
@@ -170,7 +177,7 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
     else:
         scale_h = np.ones(runs) if scales is None else np.asarray(scales, dtype=np.float64)
     v0 = torch.zeros((sector.n, live.size), dtype=torch.complex128, device=eng.device)
-    v0.index_put_((rows[sel], lr[sel]), vals[sel], accumulate=True)
+    v0.index_put_((rows[sel].clamp_min(0), lr[sel]), vals[sel], accumulate=True)
     if perturb is not None:
         # verification only: relative start-vector perturbation (eps, seed) to measure how
         # much the unreorthogonalised recurrence amplifies rounding-level differences
@@ -179,8 +186,11 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
         gen.manual_seed(int(seed))
         v0 = v0 * (1.0 + eps * torch.randn(v0.shape, dtype=torch.float64, device=eng.device, generator=gen))
     _mark(stages, "green:v0")
-    dims = sector.run_dims(eng, rows[sel], lr[sel], int(live.size))
-    k_h = np.minimum(dims.cpu().numpy(), int(krylovSize)).astype(np.int32)
+    dims = sector.run_dims(eng, rows[sel].clamp_min(0), lr[sel], int(live.size))
+    dims_h = torch.cat([dims, missing.view(1).to(torch.int64)]).cpu().numpy()
+    if dims_h[-1]:
+        raise RuntimeError("start state outside the sector basis")
+    k_h = np.minimum(dims_h[:-1], int(krylovSize)).astype(np.int32)
     _mark(stages, "green:run_dims")
     return GreenSetup(runs, live, sector, v0, k_h, scale_h)
 
