@@ -535,8 +535,9 @@ class Engine:
         n, r = v0.shape
         if n != csr.n or csr.ncols != csr.n:
             raise ValueError("lanczos: square matrix of size %d required for vectors of size %d" % (csr.n, n))
-        kmax = torch.as_tensor(k_max, dtype=torch.int32).to(self.device)
-        K = int(kmax.max().item())
+        k_h = np.asarray(k_max.cpu() if torch.is_tensor(k_max) else k_max, dtype=np.int32)
+        kmax = torch.from_numpy(k_h).to(self.device)
+        K = int(k_h.max())
         alpha = torch.zeros((r, K), dtype=torch.float64, device=self.device)
         beta = torch.zeros((r, K), dtype=torch.float64, device=self.device)
         if precision == 1:
@@ -630,18 +631,20 @@ class Engine:
                                                   _ptr(torch.view_as_real(V)), _ptr(torch.view_as_real(w)),
                                                   _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
                     "lanczos_reorth")
-            st = int(self.status.item())
+            # one device-to-host read per chunk: status, alpha and beta together
+            host = torch.cat([self.status.to(torch.float64), alpha[:j1], beta[:j1]]).cpu().numpy()
+            st = int(host[0])
+            ah, bh = host[1:1 + j1], host[1 + j1:]
             if st == L.EDGPU_ERR_BREAKDOWN:
                 # invariant subspace: the Krylov space is exact at the first zero beta
-                bh = beta[:j1].cpu().numpy()
                 kb = int(np.argmax(bh == 0.0)) + 1
-                return V[:kb], alpha[:kb].cpu().numpy(), bh[:kb]
+                return V[:kb], ah[:kb], bh[:kb]
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "lanczos_reorth")
             j = j1
-            if stop is not None and stop(alpha[:j].cpu().numpy(), beta[:j].cpu().numpy(), j):
+            if stop is not None and stop(ah, bh, j):
                 break
-        return V[:j], alpha[:j].cpu().numpy(), beta[:j].cpu().numpy()
+        return V[:j], ah[:j], bh[:j]
 
     def shifted_solve(self, csr, Y, zs, tol, k_cap):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).
