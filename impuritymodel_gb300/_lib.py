@@ -105,6 +105,7 @@ SIGNATURES = {
     "edgpu_set_reorth_fused": (None, [_I]),
     "edgpu_shifted_solve_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_shifted_solve": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
+    "edgpu_shifted_solve_df": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_combine": (_I, [_P, _I, _I64, _P, _I, _P, _P]),
     "edgpu_lanczos_ragged_smem": (_SZ, [_I64]),
     "edgpu_lanczos_ragged": (_I, [C.POINTER(CSR), C.c_void_p, _P, _P, _I, _P, _P, _P, _P]),

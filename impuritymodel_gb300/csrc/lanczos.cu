@@ -8,6 +8,7 @@
 // Vectors of a batch are stored [n][R] (run index fastest) so that the R threads of one
 // row read the row's CSR entries once (broadcast) and gather x[col][0..R) contiguously.
 // All reductions are deterministic: per-block partials in fixed order, summed in fixed order.
+#include <algorithm>
 #include <atomic>
 #include <vector>
 
@@ -1155,28 +1156,100 @@ __device__ __forceinline__ dfl df_block_sum(dfl v, dfl* red) {
   return red[32];
 }
 
-// Upstream's Lanczos recurrence in df64 for a real H (values as hi/lo float pairs), one CTA
-// per run, vectors float4 (re.hi, re.lo, im.hi, im.lo) in shared memory.  alpha and beta are
-// reduced in double-float as well (GB300 retires FP64 at 1/64 of the FP32 rate, so even the
-// reductions' FP64 adds would dominate); one thread forms beta = sqrt(.) and 1/beta in FP64
-// per step and writes the FP64 outputs.
-__global__ void __launch_bounds__(kSmallThreads, 2) lanczos_small_df_kernel(
+// The same sum with two barriers instead of three, over NW warps: consecutive sums must
+// alternate between two partial buffers of 33 entries, so that a sum never overwrites the
+// partials that a slower thread may still be reading from the previous one (every thread
+// reads the previous result before it reaches the next sum's first barrier).
+constexpr int kDfRed = 80;  // two 40-entry partial buffers
+template <int NW>
+__device__ __forceinline__ dfl df_block_sum2(dfl v, dfl* buf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_add(v, {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+  if (lane == 0) buf[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    dfl t = lane < NW ? buf[lane] : dfl{0.f, 0.f};
+#pragma unroll
+    for (int o = NW / 2; o > 0; o >>= 1)
+      t = df_add(t, {__shfl_down_sync(0xffffffffu, t.hi, o), __shfl_down_sync(0xffffffffu, t.lo, o)});
+    if (lane == 0) buf[32] = t;
+  }
+  __syncthreads();
+  return buf[32];
+}
+
+// Double-float running sum s + c with the compensation c left unnormalised until the end:
+// two-sum keeps the high parts exact, and the FP32 sum of the (small) low parts costs a
+// relative 2^-48 per term like a full double-float add, for 12 instructions per multiply-add
+// instead of 15.
+struct dacc {
+  float s, c;
+};
+
+// a += h * (xh + xl)
+__device__ __forceinline__ void dacc_fma(dacc& a, dfl h, float xh, float xl) {
+  const float p = __fmul_rn(h.hi, xh);
+  float pe = fmaf(h.hi, xh, -p);
+  pe = fmaf(h.hi, xl, pe);
+  pe = fmaf(h.lo, xh, pe);
+  const dfl t = df_two_sum(a.s, p);
+  a.s = t.hi;
+  a.c = __fadd_rn(a.c, __fadd_rn(t.lo, pe));
+}
+
+__device__ __forceinline__ dfl dacc_val(dacc a) { return df_two_sum(a.s, a.c); }
+
+// sqrt(a) for a > 0: FP32 square root s, then one Newton correction (a - s^2) / (2 s) with
+// s^2 formed exactly by the FMA two-product (Dekker's double-length square root).
+__device__ __forceinline__ dfl df_sqrt(dfl a) {
+  if (!(a.hi > 0.f)) return {a.hi == 0.f ? 0.f : __fsqrt_rn(a.hi), 0.f};
+  const float s = __fsqrt_rn(a.hi);
+  const float p = __fmul_rn(s, s);
+  const float pe = fmaf(s, s, -p);
+  const float r = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo), __fadd_rn(s, s));
+  return df_fast_two_sum(s, r);
+}
+
+// 1 / b for b != 0: FP32 reciprocal r, then one Newton step r + r (1 - b r) with the
+// residual 1 - b r formed from the exact product b.hi * r.
+__device__ __forceinline__ dfl df_rcp(dfl b) {
+  const float r = __fdiv_rn(1.f, b.hi);
+  const float p = __fmul_rn(b.hi, r);
+  const float pe = fmaf(b.hi, r, -p);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.f, p), pe), __fmul_rn(b.lo, r));
+  return df_fast_two_sum(r, __fmul_rn(r, e));
+}
+
+// The double-float recurrence with two vectors per run instead of three: the H v_j pass
+// reads x = v_j anywhere but p = v_{j-1} only at its own rows, so it overwrites p in place
+// with H v_j - beta_{j-1} v_{j-1} while summing alpha_j = v_j . H v_j from the same row
+// values; the second pass subtracts alpha_j v_j, the third normalises, and the buffers swap.
+// (The subtractions run in the order (H v - beta p) - alpha v instead of upstream's
+// (H v - alpha v) - beta p, a difference at the 2^-48 rounding level.)  Two vectors of
+// 16 bytes per row leave room for three or four CTAs per SM.  Every thread forms beta and
+// 1/beta itself from the broadcast sum (double-float square root and reciprocal, a few
+// FP32 instructions), so no barrier publishes them; the last thread, which has the fewest
+// rows, converts alpha and beta to FP64 for the outputs.
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv, int R,
     const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
     double* __restrict__ beta, int32_t* status) {
   extern __shared__ __align__(16) unsigned char sm[];
   float4* A = reinterpret_cast<float4*>(sm);
   float4* B = A + n;
-  float4* Cv = B + n;
-  dfl* red = reinterpret_cast<dfl*>(Cv + n);             // [33] reduction partials, [33] scalars
-  int32_t* srp = reinterpret_cast<int32_t*>(red + 68);  // row pointers, cached once
-  const int tid = threadIdx.x, bs = blockDim.x;
+  dfl* red = reinterpret_cast<dfl*>(B + n);                // two reduction buffers
+  int32_t* srp = reinterpret_cast<int32_t*>(red + kDfRed);  // row pointers, cached once
+  constexpr int NW = THREADS / 32;
+  const int tid = threadIdx.x;
   const dfl zero = {0.f, 0.f};
-  for (int64_t i = tid; i <= n; i += bs) srp[i] = (int32_t)rp[i];
+  for (int64_t i = tid; i <= n; i += THREADS) srp[i] = (int32_t)rp[i];
   for (int r = blockIdx.x; r < R; r += gridDim.x) {
     const int km = k_max[r];
     if (km <= 0) continue;
-    for (int64_t i = tid; i < n; i += bs) {
+    for (int64_t i = tid; i < n; i += THREADS) {
       const double2 v = v0[i * R + r];
       const dfl re = df_split(v.x), im = df_split(v.y);
       A[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
@@ -1185,15 +1258,13 @@ __global__ void __launch_bounds__(kSmallThreads, 2) lanczos_small_df_kernel(
     __syncthreads();
     float4* x = A;
     float4* p = B;
-    float4* y = Cv;
     dfl bprev = zero;
     for (int j = 0; j < km; ++j) {
-      dfl acc = zero;
-      for (int64_t i = tid; i < n; i += bs) {
-        dfl yr = zero, yi = zero;
+      const dfl nb = {-bprev.hi, -bprev.lo};
+      dacc acc = {0.f, 0.f};
+      for (int64_t i = tid; i < n; i += THREADS) {
+        dacc yr = {0.f, 0.f}, yi = {0.f, 0.f};
         const int e1 = srp[i + 1];
-        // the row's CSR entries in batches of kSmallBatch independent loads (one L2 round
-        // trip per batch instead of one per entry), then the same sums in entry order
         for (int e = srp[i]; e < e1; e += kSmallBatch) {
           int c[kSmallBatch];
           float2 hh[kSmallBatch];
@@ -1208,45 +1279,43 @@ __global__ void __launch_bounds__(kSmallThreads, 2) lanczos_small_df_kernel(
             if (e + u < e1) {
               const dfl h = {hh[u].x, hh[u].y};
               const float4 xv = x[c[u]];
-              yr = df_fma(yr, h, {xv.x, xv.y});
-              yi = df_fma(yi, h, {xv.z, xv.w});
+              dacc_fma(yr, h, xv.x, xv.y);
+              dacc_fma(yi, h, xv.z, xv.w);
             }
           }
         }
-        y[i] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
-        const float4 xi = x[i];
-        acc = df_fma(acc, yr, {xi.x, xi.y});
-        acc = df_fma(acc, yi, {xi.z, xi.w});
+        const dfl hr = dacc_val(yr), hi = dacc_val(yi);
+        const float4 xi = x[i], pi = p[i];
+        dacc_fma(acc, hr, xi.x, xi.y);
+        dacc_fma(acc, hi, xi.z, xi.w);
+        const dfl wr = df_fma(hr, nb, {pi.x, pi.y}), wi = df_fma(hi, nb, {pi.z, pi.w});
+        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
       }
-      const dfl a = df_block_sum(acc, red);
-      if (tid == 0) alpha[(int64_t)r * K + j] = df_val(a);
+      const dfl a = df_block_sum2<NW>(dacc_val(acc), red);
+      if (tid == THREADS - 1) alpha[(int64_t)r * K + j] = df_val(a);
       if (j + 1 == km) break;
-      const dfl na = {-a.hi, -a.lo}, nb = {-bprev.hi, -bprev.lo};
-      acc = zero;
-      for (int64_t i = tid; i < n; i += bs) {
-        const float4 w = y[i], xi = x[i], pi = p[i];
-        const dfl wr = df_fma(df_fma({w.x, w.y}, na, {xi.x, xi.y}), nb, {pi.x, pi.y});
-        const dfl wi = df_fma(df_fma({w.z, w.w}, na, {xi.z, xi.w}), nb, {pi.z, pi.w});
-        y[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
-        acc = df_fma(acc, wr, wr);
-        acc = df_fma(acc, wi, wi);
+      const dfl na = {-a.hi, -a.lo};
+      acc = {0.f, 0.f};
+      for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 w = p[i], xi = x[i];
+        const dfl wr = df_fma({w.x, w.y}, na, {xi.x, xi.y});
+        const dfl wi = df_fma({w.z, w.w}, na, {xi.z, xi.w});
+        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+        dacc_fma(acc, wr, wr.hi, wr.lo);
+        dacc_fma(acc, wi, wi.hi, wi.lo);
       }
-      const dfl b2 = df_block_sum(acc, red);
-      if (tid == 0) {
-        const double b = sqrt(df_val(b2));
+      bprev = df_sqrt(df_block_sum2<NW>(dacc_val(acc), red + 40));
+      const dfl ib = bprev.hi > 0.f ? df_rcp(bprev) : zero;
+      if (tid == THREADS - 1) {
+        const double b = df_val(bprev);
         beta[(int64_t)r * K + j] = b;
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
-        red[33] = df_split(b);
-        red[34] = df_split(b > 0.0 ? 1.0 / b : 0.0);
       }
-      __syncthreads();
-      const dfl ib = red[34];
-      for (int64_t i = tid; i < n; i += bs) {
-        const float4 w = y[i];
+      for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 w = p[i];
         const dfl vr = df_mul({w.x, w.y}, ib), vi = df_mul({w.z, w.w}, ib);
-        p[i] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);  // v_{j-1}'s buffer becomes v_{j+1}
+        p[i] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
       }
-      bprev = red[33];
       __syncthreads();
       float4* t = p;
       p = x;
@@ -1257,9 +1326,11 @@ __global__ void __launch_bounds__(kSmallThreads, 2) lanczos_small_df_kernel(
 }
 
 size_t small_smem_bytes(int64_t n, int precision) {
-  const size_t v = precision == 1 ? sizeof(float2) : sizeof(double2);  // df64 rows are float4
-  const size_t rows = precision == 3 ? sizeof(int32_t) * (size_t)(n + 1) : 0;  // cached row pointers
-  return 3 * v * (size_t)n + 68 * sizeof(double) + rows + 16;
+  // df64: two float4 vectors and the cached row pointers; otherwise three vectors
+  if (precision == 3)
+    return 2 * sizeof(float4) * (size_t)n + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(n + 1) + 16;
+  const size_t v = precision == 1 ? sizeof(float2) : sizeof(double2);
+  return 3 * v * (size_t)n + 68 * sizeof(double) + 16;
 }
 
 bool small_fits(int64_t n, int precision) { return small_smem_bytes(n, precision) <= 200 * 1024; }
@@ -1281,19 +1352,29 @@ int launch_small(const edgpu_csr* h, const T* vals, const double* v0, int R, con
   return check_launch();
 }
 
+// 256-thread CTAs when three or more fit on an SM (measured on the 1770-row RIXS final-state
+// sector with 750 runs: 256 x 3-4 per SM 6.9 ms against 7.4 ms for 512 x 2), else 512.
 int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
                     double* beta, int32_t* status, cudaStream_t s) {
   const size_t smem = small_smem_bytes(h->n, 3);
-  cudaFuncSetAttribute(lanczos_small_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto k256 = lanczos_small_df_kernel<256, 4>;
+  auto k512 = lanczos_small_df_kernel<512, 2>;
+  cudaFuncSetAttribute(k256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_small_df_kernel, kSmallThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k256, 256, smem);
+  int threads = 256;
+  auto kern = k256;
+  if (per_sm < 3) {
+    cudaFuncSetAttribute(k512, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k512, 512, smem);
+    threads = 512;
+    kern = k512;
+  }
   if (per_sm < 1) per_sm = 1;
   int grid = grid_cap() * per_sm;
   if (grid > R) grid = R;
-  lanczos_small_df_kernel<<<grid, kSmallThreads, smem, s>>>(h->n, h->row_ptr, h->col,
-                                                            reinterpret_cast<const float2*>(h->val_df), R,
-                                                            reinterpret_cast<const double2*>(v0), k_max, K, alpha,
-                                                            beta, status);
+  kern<<<grid, threads, smem, s>>>(h->n, h->row_ptr, h->col, reinterpret_cast<const float2*>(h->val_df), R,
+                                   reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta, status);
   note_launch();
   return check_launch();
 }
@@ -1438,69 +1519,271 @@ __global__ void __launch_bounds__(kSmallThreads) shifted_small_kernel(
   }
 }
 
-// coef[r][z][k] = ynorm_r * ((z - T_m)^{-1} e_1)_k by the Thomas algorithm; thread per (r, z).
-// (z - T) has diagonal z - a_k and off-diagonals -b_k.  scratch holds the forward-sweep ratios.
-__global__ void shifted_coef_kernel(const double* alpha, const double* beta, const int32_t* m_arr,
-                                    const double* ynorm, const double2* zs, int n_rhs, int nz, int k_cap,
-                                    double2* coef, double2* scratch) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_rhs * nz) return;
-  const int r = t / nz;
-  const int m = m_arr[r];
-  double2* x = coef + (size_t)t * k_cap;
-  double2* cp = scratch + (size_t)t * k_cap;
-  if (m <= 0) {
-    for (int k = 0; k < k_cap; ++k) x[k] = make_double2(0.0, 0.0);
-    return;
-  }
-  const double2 z = zs[t];
-  const double* a = alpha + (size_t)r * k_cap;
-  const double* b = beta + (size_t)r * k_cap;
-  double2 cprev = make_double2(0.0, 0.0), dprev = make_double2(0.0, 0.0);
-  for (int k = 0; k < m; ++k) {
-    double2 den = make_double2(z.x - a[k], z.y);
-    double2 rk = make_double2(1.0, 0.0);
-    if (k > 0) {
-      den.x += b[k - 1] * cprev.x;
-      den.y += b[k - 1] * cprev.y;
-      rk = make_double2(b[k - 1] * dprev.x, b[k - 1] * dprev.y);
+// The same shifted solves in double-float arithmetic for a real H (values as hi/lo float
+// pairs), two vectors per right-hand side as in lanczos_small_df_kernel, each v_j written
+// to V[rhs][j] as float4 (re.hi, re.lo, im.hi, im.lo).  The residual estimate only decides
+// when to stop, so its LU recurrence runs in FP32 (the pivots keep Im d_k >= Im z > 0, so
+// it cannot break down); every thread forms beta and 1/beta from the broadcast sum, and the
+// barrier that pools the per-shift verdicts is the only one beyond the two sums.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) shifted_small_df_kernel(
+    int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv,
+    int n_rhs, const double2* __restrict__ Y, const double2* __restrict__ zs, int nz, int k_cap, float tol,
+    float4* __restrict__ V, double* __restrict__ alpha, double* __restrict__ beta, int32_t* __restrict__ m_out,
+    double* __restrict__ ynorm_out, int32_t* status) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  float4* A = reinterpret_cast<float4*>(sm);
+  float4* B = A + n;
+  dfl* red = reinterpret_cast<dfl*>(B + n);
+  int32_t* srp = reinterpret_cast<int32_t*>(red + kDfRed);
+  constexpr int NW = THREADS / 32;
+  const int tid = threadIdx.x;
+  const dfl zero = {0.f, 0.f};
+  for (int64_t i = tid; i <= n; i += THREADS) srp[i] = (int32_t)rp[i];
+  for (int r = blockIdx.x; r < n_rhs; r += gridDim.x) {
+    float4* Vr = V + (size_t)r * k_cap * n;
+    const double2* y = Y + (size_t)r * n;
+    dacc acc = {0.f, 0.f};
+    for (int64_t i = tid; i < n; i += THREADS) {
+      const double2 v = y[i];
+      const dfl re = df_split(v.x), im = df_split(v.y);
+      A[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      dacc_fma(acc, re, re.hi, re.lo);
+      dacc_fma(acc, im, im.hi, im.lo);
     }
-    const double dd = den.x * den.x + den.y * den.y;
-    const double2 inv = make_double2(den.x / dd, -den.y / dd);
-    const double bk = (k + 1 < m) ? b[k] : 0.0;
-    cprev = make_double2(-bk * inv.x, -bk * inv.y);
-    dprev = make_double2(rk.x * inv.x - rk.y * inv.y, rk.x * inv.y + rk.y * inv.x);
-    cp[k] = cprev;
-    x[k] = dprev;
+    const dfl yn = df_sqrt(df_block_sum2<NW>(dacc_val(acc), red));
+    if (tid == THREADS - 1) ynorm_out[r] = df_val(yn);
+    if (!(yn.hi > 0.f)) {
+      if (tid == 0) m_out[r] = 0;
+      __syncthreads();
+      continue;
+    }
+    const dfl iyn = df_rcp(yn);
+    for (int64_t i = tid; i < n; i += THREADS) {
+      const float4 w = A[i];
+      const dfl vr = df_mul({w.x, w.y}, iyn), vi = df_mul({w.z, w.w}, iyn);
+      const float4 v = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
+      A[i] = v;
+      B[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      Vr[i] = v;
+    }
+    __syncthreads();
+    float4* x = A;
+    float4* p = B;
+    float2 z = make_float2(0.f, 0.f), d = make_float2(1.f, 0.f), q = make_float2(1.f, 0.f);
+    if (tid < nz) {
+      const double2 zd = zs[(size_t)r * nz + tid];
+      z = make_float2((float)zd.x, (float)zd.y);
+    }
+    dfl bprev = zero;
+    int m = k_cap;
+    for (int j = 0; j < k_cap; ++j) {
+      const dfl nb = {-bprev.hi, -bprev.lo};
+      acc = {0.f, 0.f};
+      for (int64_t i = tid; i < n; i += THREADS) {
+        dacc yr = {0.f, 0.f}, yi = {0.f, 0.f};
+        const int e1 = srp[i + 1];
+        for (int e = srp[i]; e < e1; e += kSmallBatch) {
+          int c[kSmallBatch];
+          float2 hh[kSmallBatch];
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            const bool ok = e + u < e1;
+            c[u] = ok ? __ldg(col + e + u) : 0;
+            hh[u] = ok ? __ldg(hv + e + u) : make_float2(0.f, 0.f);
+          }
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            if (e + u < e1) {
+              const dfl h = {hh[u].x, hh[u].y};
+              const float4 xv = x[c[u]];
+              dacc_fma(yr, h, xv.x, xv.y);
+              dacc_fma(yi, h, xv.z, xv.w);
+            }
+          }
+        }
+        const dfl hr = dacc_val(yr), hi = dacc_val(yi);
+        const float4 xi = x[i], pi = p[i];
+        dacc_fma(acc, hr, xi.x, xi.y);
+        dacc_fma(acc, hi, xi.z, xi.w);
+        const dfl wr = df_fma(hr, nb, {pi.x, pi.y}), wi = df_fma(hi, nb, {pi.z, pi.w});
+        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+      }
+      const dfl a = df_block_sum2<NW>(dacc_val(acc), red);
+      if (tid == THREADS - 1) alpha[(size_t)r * k_cap + j] = df_val(a);
+      const dfl na = {-a.hi, -a.lo};
+      acc = {0.f, 0.f};
+      for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 w = p[i], xi = x[i];
+        const dfl wr = df_fma({w.x, w.y}, na, {xi.x, xi.y});
+        const dfl wi = df_fma({w.z, w.w}, na, {xi.z, xi.w});
+        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+        dacc_fma(acc, wr, wr.hi, wr.lo);
+        dacc_fma(acc, wi, wi.hi, wi.lo);
+      }
+      const dfl b = df_sqrt(df_block_sum2<NW>(dacc_val(acc), red + 40));
+      if (tid == THREADS - 1) beta[(size_t)r * k_cap + j] = df_val(b);
+      bool ok = true;
+      if (tid < nz) {
+        const float af = a.hi, bp = bprev.hi;
+        float2 dn = make_float2(z.x - af, z.y);
+        if (j > 0) {
+          const float rd = __fdiv_rn(bp * bp, d.x * d.x + d.y * d.y);
+          dn.x -= rd * d.x;
+          dn.y += rd * d.y;
+        }
+        const float2 qn = make_float2(j > 0 ? q.x * bp : 1.f, j > 0 ? q.y * bp : 0.f);
+        const float rr = __fdiv_rn(1.f, dn.x * dn.x + dn.y * dn.y);
+        q = make_float2((qn.x * dn.x + qn.y * dn.y) * rr, (qn.y * dn.x - qn.x * dn.y) * rr);
+        d = dn;
+        ok = b.hi * sqrtf(q.x * q.x + q.y * q.y) <= tol;
+      }
+      const bool conv = __syncthreads_and(ok);
+      if (conv || !(b.hi > 0.f) || j + 1 == k_cap) {
+        m = j + 1;
+        if (tid == 0) {
+          if (!(b.hi >= 0.f))
+            atomicExch(status, (int32_t)EDGPU_ERR_NAN);
+          else if (!conv && b.hi > 0.f)
+            atomicExch(status, (int32_t)EDGPU_ERR_NOCONV);
+        }
+        break;
+      }
+      const dfl ib = df_rcp(b);
+      float4* vn = Vr + (size_t)(j + 1) * n;
+      for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 w = p[i];
+        const dfl vr = df_mul({w.x, w.y}, ib), vi = df_mul({w.z, w.w}, ib);
+        const float4 v = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
+        p[i] = v;
+        vn[i] = v;
+      }
+      __syncthreads();
+      float4* t = p;
+      p = x;
+      x = t;
+      bprev = b;
+    }
+    if (tid == 0) m_out[r] = m;
+    __syncthreads();
   }
-  for (int k = m - 2; k >= 0; --k) {
-    const double2 c = cp[k], xn = x[k + 1];
-    x[k] = make_double2(x[k].x - (c.x * xn.x - c.y * xn.y), x[k].y - (c.x * xn.y + c.y * xn.x));
-  }
-  const double yn = ynorm[r];
-  for (int k = 0; k < m; ++k) x[k] = make_double2(yn * x[k].x, yn * x[k].y);
-  for (int k = m; k < k_cap; ++k) x[k] = make_double2(0.0, 0.0);
 }
 
-// X[r][z][i] = sum_k coef[r][z][k] V[r][k][i]
+// coef[r][k][z] = ynorm_r * ((z - T_m)^{-1} e_1)_k by the Thomas algorithm: block per
+// right-hand side with its alpha and beta staged in shared memory, thread per shift (one
+// FP64 reciprocal per step).  (z - T) has diagonal z - a_k and off-diagonals -b_k; the
+// forward-sweep ratios and the solution go through scratch laid out [r][k][z], so a warp's
+// accesses are contiguous.  DF writes the coefficients as double-float pairs (float4).
+template <bool DF>
+__global__ void shifted_coef_kernel(const double* __restrict__ alpha, const double* __restrict__ beta,
+                                    const int32_t* __restrict__ m_arr, const double* __restrict__ ynorm,
+                                    const double2* __restrict__ zs, int nz, int k_cap, double2* __restrict__ coef,
+                                    float4* __restrict__ coef_df, double2* __restrict__ cp,
+                                    double2* __restrict__ xs) {
+  extern __shared__ double ab[];
+  const int r = blockIdx.x;
+  const int m = m_arr[r];
+  double* a = ab;
+  double* b = ab + k_cap;
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    a[k] = alpha[(size_t)r * k_cap + k];
+    b[k] = beta[(size_t)r * k_cap + k];
+  }
+  __syncthreads();
+  if (m <= 0) return;
+  const double yn = ynorm[r];
+  const size_t base = (size_t)r * k_cap * nz;
+  for (int zi = threadIdx.x; zi < nz; zi += blockDim.x) {
+    const double2 z = zs[(size_t)r * nz + zi];
+    double2 cprev = make_double2(0.0, 0.0), dprev = make_double2(0.0, 0.0);
+    for (int k = 0; k < m; ++k) {
+      double2 den = make_double2(z.x - a[k], z.y);
+      double2 rk = make_double2(1.0, 0.0);
+      if (k > 0) {
+        den.x += b[k - 1] * cprev.x;
+        den.y += b[k - 1] * cprev.y;
+        rk = make_double2(b[k - 1] * dprev.x, b[k - 1] * dprev.y);
+      }
+      const double rdd = 1.0 / (den.x * den.x + den.y * den.y);
+      const double2 inv = make_double2(den.x * rdd, -den.y * rdd);
+      const double bk = (k + 1 < m) ? b[k] : 0.0;
+      cprev = make_double2(-bk * inv.x, -bk * inv.y);
+      dprev = make_double2(rk.x * inv.x - rk.y * inv.y, rk.x * inv.y + rk.y * inv.x);
+      cp[base + (size_t)k * nz + zi] = cprev;
+      xs[base + (size_t)k * nz + zi] = dprev;
+    }
+    double2 xn = dprev;
+    for (int k = m - 1; k >= 0; --k) {
+      double2 xk = xs[base + (size_t)k * nz + zi];
+      if (k + 1 < m) {
+        const double2 c = cp[base + (size_t)k * nz + zi];
+        xk = make_double2(xk.x - (c.x * xn.x - c.y * xn.y), xk.y - (c.x * xn.y + c.y * xn.x));
+      }
+      xn = xk;
+      const double2 o = make_double2(yn * xk.x, yn * xk.y);
+      if (DF) {
+        const dfl re = df_split(o.x), im = df_split(o.y);
+        coef_df[base + (size_t)k * nz + zi] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      } else {
+        coef[base + (size_t)k * nz + zi] = o;
+      }
+    }
+  }
+}
+
+// X[r][z][i] = sum_k coef[r][k][z] V[r][k][i] (FP64)
 __global__ void combine_batched_kernel(const double2* __restrict__ V, const double2* __restrict__ coef,
                                        const int32_t* __restrict__ m_arr, int64_t n, int nz, int k_cap,
                                        double2* __restrict__ X) {
   const int r = blockIdx.z;
   const int zi = blockIdx.y;
   const int m = m_arr[r];
-  const double2* c = coef + ((size_t)r * nz + zi) * k_cap;
+  const double2* c = coef + (size_t)r * k_cap * nz + zi;
   const double2* Vr = V + (size_t)r * k_cap * n;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double xr = 0.0, xi = 0.0;
 #pragma unroll 8
     for (int k = 0; k < m; ++k) {
-      const double2 ck = c[k];
+      const double2 ck = c[(size_t)k * nz];
       const double2 v = Vr[(size_t)k * n + i];
       xr += ck.x * v.x - ck.y * v.y;
       xi += ck.x * v.y + ck.y * v.x;
     }
     X[((size_t)r * nz + zi) * n + i] = make_double2(xr, xi);
+  }
+}
+
+// The same in double-float: thread per row i, kCombineZ shifts per thread (V[k][i] read once
+// for all of them), sums in double-float, FP64 only for the output.
+constexpr int kCombineZ = 8;
+__global__ void __launch_bounds__(128) combine_df_kernel(const float4* __restrict__ V, const float4* __restrict__ coef,
+                                                         const int32_t* __restrict__ m_arr, int64_t n, int nz,
+                                                         int k_cap, double2* __restrict__ X) {
+  const int r = blockIdx.z;
+  const int z0 = blockIdx.y * kCombineZ;
+  const int m = m_arr[r];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const float4* c = coef + (size_t)r * k_cap * nz;
+  const float4* Vr = V + (size_t)r * k_cap * n;
+  dacc xr[kCombineZ], xi[kCombineZ];
+#pragma unroll
+  for (int u = 0; u < kCombineZ; ++u) xr[u] = xi[u] = {0.f, 0.f};
+  if (i < n) {
+    for (int k = 0; k < m; ++k) {
+      const float4 v = Vr[(size_t)k * n + i];
+#pragma unroll
+      for (int u = 0; u < kCombineZ; ++u) {
+        const float4 ck = z0 + u < nz ? __ldg(c + (size_t)k * nz + z0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const dfl cr = {ck.x, ck.y}, ci = {ck.z, ck.w}, nci = {-ck.z, -ck.w};
+        dacc_fma(xr[u], cr, v.x, v.y);
+        dacc_fma(xr[u], nci, v.z, v.w);
+        dacc_fma(xi[u], cr, v.z, v.w);
+        dacc_fma(xi[u], ci, v.x, v.y);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kCombineZ; ++u)
+      if (z0 + u < nz) X[((size_t)r * nz + z0 + u) * n + i] = make_double2(df_val(dacc_val(xr[u])), df_val(dacc_val(xi[u])));
   }
 }
 
@@ -1511,21 +1794,26 @@ extern "C" size_t edgpu_shifted_solve_workspace(int64_t n, int n_rhs, int nz, in
   b += sizeof(double2) * (size_t)n_rhs * k_cap * n + 256;       // V
   b += 2 * sizeof(double) * (size_t)n_rhs * k_cap + 512;        // alpha, beta
   b += sizeof(int32_t) * (size_t)n_rhs + sizeof(double) * n_rhs + 512;
-  b += 2 * sizeof(double2) * (size_t)n_rhs * nz * k_cap + 256;  // coefficients + forward-sweep scratch
+  b += 3 * sizeof(double2) * (size_t)n_rhs * nz * k_cap + 768;  // coefficients + Thomas scratch
   return b + 1024;
 }
 
-extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
-                                   double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
-                                   size_t workspace_bytes, void* stream) {
+namespace {
+
+int shifted_solve_impl(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap, double tol,
+                       double* X, int32_t* m_out, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                       cudaStream_t s, bool df) {
+  using namespace edgpu;
   if (!h || !Y || !zs || !X || !m_out || !status_dev || n_rhs < 1 || nz < 1 || k_cap < 1 || h->n < 1)
     return EDGPU_ERR_ARG;
   if (nz > kSmallThreads) return EDGPU_ERR_ARG;
+  if (df && (!h->val_df || h->val_c)) return EDGPU_ERR_ARG;
   if (workspace_bytes < edgpu_shifted_solve_workspace(h->n, n_rhs, nz, k_cap)) return EDGPU_ERR_WORKSPACE;
   const int64_t n = h->n;
-  const size_t smem = 3 * sizeof(double2) * (size_t)n + 34 * sizeof(double) + 16;
+  const size_t smem = df ? small_smem_bytes(n, 3) : 3 * sizeof(double2) * (size_t)n + 34 * sizeof(double) + 16;
   if (smem > 200 * 1024) return EDGPU_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
+  const size_t coef_smem = 2 * sizeof(double) * (size_t)k_cap;
+  if (coef_smem > 200 * 1024) return EDGPU_ERR_ARG;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
   size_t off = 0;
   auto carve = [&](size_t bytes) {
@@ -1533,44 +1821,79 @@ extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rh
     off += (bytes + 255) & ~(size_t)255;
     return p;
   };
-  double2* V = reinterpret_cast<double2*>(carve(sizeof(double2) * (size_t)n_rhs * k_cap * n));
+  void* V = carve(sizeof(double2) * (size_t)n_rhs * k_cap * n);
   double* alpha = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs * k_cap));
   double* beta = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs * k_cap));
   double* yn = reinterpret_cast<double*>(carve(sizeof(double) * (size_t)n_rhs));
-  double* coef = reinterpret_cast<double*>(carve(2 * sizeof(double2) * (size_t)n_rhs * nz * k_cap));
+  const size_t cbytes = sizeof(double2) * (size_t)n_rhs * nz * k_cap;
+  void* coef = carve(cbytes);
+  double2* cp = reinterpret_cast<double2*>(carve(cbytes));
+  double2* xs = reinterpret_cast<double2*>(carve(cbytes));
   if (off > workspace_bytes) return EDGPU_ERR_WORKSPACE;
   const double2* Yc = reinterpret_cast<const double2*>(Y);
   const double2* zc = reinterpret_cast<const double2*>(zs);
   int per_sm = 0;
-  if (h->val_c) {
-    cudaFuncSetAttribute(shifted_small_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shifted_small_kernel<true>, kSmallThreads, smem);
+  if (df) {
+    auto kern = shifted_small_df_kernel<kSmallThreads>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSmallThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    const int grid = std::min(grid_cap() * per_sm, n_rhs);
+    kern<<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, reinterpret_cast<const float2*>(h->val_df), n_rhs,
+                                           Yc, zc, nz, k_cap, (float)tol, reinterpret_cast<float4*>(V), alpha, beta,
+                                           m_out, yn, status_dev);
   } else {
-    cudaFuncSetAttribute(shifted_small_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shifted_small_kernel<false>, kSmallThreads, smem);
+    auto kern = h->val_c ? shifted_small_kernel<true> : shifted_small_kernel<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSmallThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    const int grid = std::min(grid_cap() * per_sm, n_rhs);
+    kern<<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, h->val_c ? h->val_c : h->val_r, n_rhs, Yc, zc, nz,
+                                           k_cap, tol, reinterpret_cast<double2*>(V), alpha, beta, m_out, yn,
+                                           status_dev);
   }
-  if (per_sm < 1) per_sm = 1;
-  int grid = grid_cap() * per_sm;
-  if (grid > n_rhs) grid = n_rhs;
-  if (h->val_c)
-    shifted_small_kernel<true><<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, h->val_c, n_rhs, Yc, zc, nz,
-                                                                 k_cap, tol, V, alpha, beta, m_out, yn, status_dev);
-  else
-    shifted_small_kernel<false><<<grid, kSmallThreads, smem, s>>>(n, h->row_ptr, h->col, h->val_r, n_rhs, Yc, zc, nz,
-                                                                  k_cap, tol, V, alpha, beta, m_out, yn, status_dev);
   note_launch();
   int rc = check_launch();
   if (rc) return rc;
-  const int tot = n_rhs * nz;
-  shifted_coef_kernel<<<(tot + 127) / 128, 128, 0, s>>>(alpha, beta, m_out, yn, zc, n_rhs, nz, k_cap,
-                                                        reinterpret_cast<double2*>(coef),
-                                                        reinterpret_cast<double2*>(coef) + (size_t)tot * k_cap);
+  const int cthreads = nz < 128 ? ((nz + 31) / 32) * 32 : 128;
+  if (df) {
+    cudaFuncSetAttribute(shifted_coef_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)coef_smem);
+    shifted_coef_kernel<true><<<n_rhs, cthreads, coef_smem, s>>>(alpha, beta, m_out, yn, zc, nz, k_cap, nullptr,
+                                                                 reinterpret_cast<float4*>(coef), cp, xs);
+  } else {
+    cudaFuncSetAttribute(shifted_coef_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)coef_smem);
+    shifted_coef_kernel<false><<<n_rhs, cthreads, coef_smem, s>>>(alpha, beta, m_out, yn, zc, nz, k_cap,
+                                                                  reinterpret_cast<double2*>(coef), nullptr, cp, xs);
+  }
   note_launch();
-  dim3 g3((unsigned)((n + 255) / 256 > 16 ? 16 : (n + 255) / 256), nz, n_rhs);
-  combine_batched_kernel<<<g3, 256, 0, s>>>(V, reinterpret_cast<const double2*>(coef), m_out, n, nz, k_cap,
-                                            reinterpret_cast<double2*>(X));
+  if (df) {
+    dim3 g3((unsigned)((n + 127) / 128), (unsigned)((nz + kCombineZ - 1) / kCombineZ), (unsigned)n_rhs);
+    combine_df_kernel<<<g3, 128, 0, s>>>(reinterpret_cast<const float4*>(V), reinterpret_cast<const float4*>(coef), m_out,
+                                         n, nz, k_cap, reinterpret_cast<double2*>(X));
+  } else {
+    dim3 g3((unsigned)((n + 255) / 256 > 16 ? 16 : (n + 255) / 256), nz, n_rhs);
+    combine_batched_kernel<<<g3, 256, 0, s>>>(reinterpret_cast<const double2*>(V),
+                                              reinterpret_cast<const double2*>(coef), m_out, n, nz, k_cap,
+                                              reinterpret_cast<double2*>(X));
+  }
   note_launch();
   return check_launch();
+}
+
+}  // namespace
+
+extern "C" int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
+                                   double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  return shifted_solve_impl(h, Y, n_rhs, zs, nz, k_cap, tol, X, m_out, status_dev, workspace, workspace_bytes,
+                            (cudaStream_t)stream, false);
+}
+
+extern "C" int edgpu_shifted_solve_df(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz,
+                                      int k_cap, double tol, double* X, int32_t* m_out, int32_t* status_dev,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  return shifted_solve_impl(h, Y, n_rhs, zs, nz, k_cap, tol, X, m_out, status_dev, workspace, workspace_bytes,
+                            (cudaStream_t)stream, true);
 }
 
 // =======================================================================================

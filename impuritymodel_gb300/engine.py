@@ -646,25 +646,29 @@ class Engine:
                 break
         return V[:j], ah[:j], bh[:j]
 
-    def shifted_solve(self, csr, Y, zs, tol, k_cap):
+    def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).
 
-        Returns (X [R, nz, N] complex128, krylov sizes [R]) or None when the sector or the
-        shift count exceeds the single-CTA kernel's limits."""
+        ``precision=3`` runs the Krylov recurrence in double-float arithmetic when H is real
+        (complex H stays FP64).  Returns (X [R, nz, N] complex128, krylov sizes [R]) or None
+        when the sector or the shift count exceeds the single-CTA kernel's limits."""
         r, n = Y.shape
         nz = zs.shape[1]
         k_cap = int(k_cap)
-        if nz > 512 or 48 * n + 300 > 200 * 1024:
+        if nz > 512 or 48 * n + 300 > 200 * 1024 or 16 * k_cap > 200 * 1024:
             return None
+        df = precision == 3 and csr.val_c is None and csr.val_r is not None
+        if df:
+            csr.double_float()
+        solve = self.lib.edgpu_shifted_solve_df if df else self.lib.edgpu_shifted_solve
         zt = torch.as_tensor(np.ascontiguousarray(zs, dtype=np.complex128)).to(self.device)
         X = torch.empty((r, nz, n), dtype=torch.complex128, device=self.device)
         m = torch.empty(r, dtype=torch.int32, device=self.device)
         ws, wsn = self.workspace(self.lib.edgpu_shifted_solve_workspace(n, r, nz, k_cap))
         self.reset_status()
-        L.check(self.lib.edgpu_shifted_solve(C.byref(csr.struct()), _ptr(torch.view_as_real(Y.contiguous())), r,
-                                             _ptr(torch.view_as_real(zt)), nz, k_cap, float(tol),
-                                             _ptr(torch.view_as_real(X)), _ptr(m), _ptr(self.status), ws, wsn,
-                                             self.stream), "shifted_solve")
+        L.check(solve(C.byref(csr.struct()), _ptr(torch.view_as_real(Y.contiguous())), r, _ptr(torch.view_as_real(zt)),
+                      nz, k_cap, float(tol), _ptr(torch.view_as_real(X)), _ptr(m), _ptr(self.status), ws, wsn,
+                      self.stream), "shifted_solve")
         st = int(self.status.item())
         if st == L.EDGPU_ERR_NOCONV:
             # upstream only prints when BiCGSTAB misses its tolerance (spectra.py:963-971)

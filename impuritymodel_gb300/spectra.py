@@ -453,7 +453,7 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     # without reorthogonalisation the recurrence may need a few times the sector dimension
     k_solve = min(6 * core.n + 50, max_krylov)
     if batched:
-        solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve)
+        solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve, precision)
     else:
         solved = None
         blocks = []

@@ -270,6 +270,17 @@ size_t edgpu_shifted_solve_workspace(int64_t n, int n_rhs, int nz, int k_cap);
 int edgpu_shifted_solve(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
                         double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
                         size_t workspace_bytes, void* stream);
+/*
+ * The same solves with the Krylov recurrence in double-float arithmetic (float hi/lo pairs,
+ * about 48 significand bits, on the FP32 pipe) for a real H with its val_df copy set; the
+ * residual estimate that decides when to stop runs in FP32, the tridiagonal solves in FP64
+ * and the assembly of X in double-float.  Same arguments, workspace and outputs.
+ * EDGPU_ERR_ARG for a complex H or without val_df.  No counterpart in upstream
+ * impurityModel (an arithmetic form of the solves above).
+ */
+int edgpu_shifted_solve_df(const edgpu_csr* h, const double* Y, int n_rhs, const double* zs, int nz, int k_cap,
+                           double tol, double* X, int32_t* m_out, int32_t* status_dev, void* workspace,
+                           size_t workspace_bytes, void* stream);
 
 /* X[m][n] = sum_k C[k][m] V[k][n] (complex128): Ritz vectors / shifted-solve solutions. */
 int edgpu_combine(const double* V, int K, int64_t n, const double* C, int M, double* X, void* stream);
