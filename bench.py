@@ -166,6 +166,13 @@ class Pipeline:
         es, psi_t = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"])
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psi_t = es[:ne], psi_t[:ne]
+        if capture is None and perturb is None and timing is None and batched:
+            # XAS on a side stream while the RIXS pipeline runs on the current one
+            g_xas, g_rixs = spectra.xas_rixs_device(
+                self.eng, self.dop, self.restr, self.xas_dops, self.xas_dops, self.out_dops, psi_t, es, self.w,
+                W["xas"]["delta"], self.w_in, self.w_loss, W["rixs"]["delta_in"], W["rixs"]["delta_loss"],
+                W["krylov"], W["slater_weight_min"], precision)
+            return es, g_xas, g_rixs
         g_xas = spectra.spectra_device(self.eng, self.dop, self.restr, self.xas_dops, psi_t, es, self.w,
                                        W["xas"]["delta"], W["krylov"], W["slater_weight_min"], precision,
                                        capture=capture, perturb=perturb, batched=batched)
@@ -580,9 +587,10 @@ def run_gpu(args):
         torch.distributed.barrier()
     clocks.start()
     n0 = lib.edgpu_launch_count()
-    best_times, best_out = time_steps(lambda: pipe.step(best_prec, timing), args.steps, 0, flush_buf)
+    best_times, best_out = time_steps(lambda: pipe.step(best_prec), args.steps, 0, flush_buf)
     launches = lib.edgpu_launch_count() - n0
     clk = clocks.stop()
+    pipe.step(best_prec, timing)  # kernel times of the Lanczos calls (untimed step)
     es_p = plain_out[0]
     es_b = best_out[0]
     err = {"gs_energy_max_abs_eV": float(np.abs(es_b - es_p).max()), "vs_exact": acc, "forms_pass": ok,

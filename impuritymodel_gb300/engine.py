@@ -171,32 +171,64 @@ class CsrMatrix:
 
 COMPONENTS_KERNEL_MAX_ROWS = 1 << 16  # single-CTA label propagation of edgpu_components
 
+# raw handle of the current stream without building a torch Stream object (about 10 us less
+# per library call); the public accessor is the fallback
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
 
 class Engine:
-    """One engine per CUDA device.  Holds the library handle, a status word and a workspace."""
+    """One engine per CUDA device.  Holds the library handle and, per CUDA stream that issues
+    work, a status word and a workspace (so that pipelines on different streams never share
+    either)."""
 
     def __init__(self, device=None):
         if not torch.cuda.is_available():
             raise RuntimeError("impuritymodel_gb300 needs a CUDA device (there is no CPU fallback)")
         self.lib = L.load()
         self.device = torch.device(device if device is not None else "cuda")
-        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
-        self._ws = torch.empty(1 << 20, dtype=torch.uint8, device=self.device)
+        self._dev_index = self.device.index if self.device.index is not None else torch.cuda.current_device()
+        self._lanes = {}
+        self._side = []
         self.scratch_entries = 256
         # bytes moved across the host<->device boundary by the drop-in API (inputs/results)
         self.h2d_bytes = 0
         self.d2h_bytes = 0
 
     # -- plumbing -------------------------------------------------------------------------
+    def _stream_handle(self):
+        if _raw_stream is not None:
+            return _raw_stream(self._dev_index)
+        return torch.cuda.current_stream(self.device).cuda_stream
+
     @property
     def stream(self):
-        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        return C.c_void_p(self._stream_handle())
+
+    def _lane(self):
+        h = self._stream_handle()
+        lane = self._lanes.get(h)
+        if lane is None:
+            lane = self._lanes[h] = [torch.zeros(1, dtype=torch.int32, device=self.device),
+                                     torch.empty(1 << 20, dtype=torch.uint8, device=self.device)]
+        return lane
+
+    @property
+    def status(self):
+        """Device status word of the current stream (edgpu_* error codes)."""
+        return self._lane()[0]
+
+    def side_stream(self, k=0):
+        """The k-th high-priority side stream of this engine (created on first use)."""
+        while len(self._side) <= k:
+            self._side.append(torch.cuda.Stream(self.device, priority=-1))
+        return self._side[k]
 
     def workspace(self, nbytes):
         nbytes = int(nbytes)
-        if self._ws.numel() < nbytes:
-            self._ws = torch.empty(max(nbytes, 2 * self._ws.numel()), dtype=torch.uint8, device=self.device)
-        return C.c_void_p(self._ws.data_ptr()), C.c_size_t(self._ws.numel())
+        lane = self._lane()
+        if lane[1].numel() < nbytes:
+            lane[1] = torch.empty(max(nbytes, 2 * lane[1].numel()), dtype=torch.uint8, device=self.device)
+        return C.c_void_p(lane[1].data_ptr()), C.c_size_t(lane[1].numel())
 
     def reset_status(self):
         self.status.zero_()
@@ -530,8 +562,11 @@ class Engine:
         return dims
 
     # -- Krylov ---------------------------------------------------------------------------
-    def lanczos(self, csr, v0, k_max, precision=0, timing=None):
-        """Batched Lanczos on R start vectors v0 [N, R] complex128 (normalised)."""
+    def lanczos(self, csr, v0, k_max, precision=0, timing=None, check=True):
+        """Batched Lanczos on R start vectors v0 [N, R] complex128 (normalised).
+
+        ``check=False`` only enqueues the work: the caller reads the status later on the same
+        stream (``read_status``) before it relies on alpha and beta."""
         n, r = v0.shape
         if n != csr.n or csr.ncols != csr.n:
             raise ValueError("lanczos: square matrix of size %d required for vectors of size %d" % (csr.n, n))
@@ -562,7 +597,8 @@ class Engine:
             sb = (4 if precision == 1 else 8) * (2 if csr.val_c is not None else 1)
             timing.append(dict(n=csr.n, nnz=csr.nnz, R=r, K=K, precision=precision, spmm_ms=ms[0], axpy_ms=ms[1],
                                normalize_ms=ms[2], spmm_launches=K, vec_bytes=vb, val_bytes=sb))
-        self.read_status("lanczos")
+        if check:
+            self.read_status("lanczos")
         if precision == 1 and csr.mixed_shift:
             alpha += csr.mixed_shift  # Lanczos ran on H - shift*I
         return alpha, beta

@@ -195,6 +195,48 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
     return GreenSetup(runs, live, sector, v0, k_h, scale_h)
 
 
+def _drive(steps):
+    """Run a pipeline step generator to completion and return its value."""
+    while True:
+        try:
+            next(steps)
+        except StopIteration as done:
+            return done.value
+
+
+def run_concurrently(eng, jobs):
+    """Run pipeline step generators side by side on one GPU and return their values.
+
+    Job 0 runs on the current stream, job k > 0 on the engine's k-th high-priority side
+    stream, which first waits for the work already queued on the current stream (the jobs'
+    inputs).  A job yields right after it enqueues a long GPU operation whose result it needs
+    next; the host then advances the next job, whose launches and synchronisations stay on
+    its own stream, instead of idling until the long operation ends.  The current stream
+    waits for every side stream before this returns, and the returned device tensors are
+    marked as used on it.
+    """
+    main = torch.cuda.current_stream(eng.device)
+    streams = [main] + [eng.side_stream(k) for k in range(len(jobs) - 1)]
+    for s in streams[1:]:
+        s.wait_stream(main)
+    results = [None] * len(jobs)
+    pending = list(range(len(jobs)))
+    while pending:
+        for k in list(pending):
+            with torch.cuda.stream(streams[k]):
+                try:
+                    next(jobs[k])
+                except StopIteration as done:
+                    results[k] = done.value
+                    pending.remove(k)
+    for s in streams[1:]:
+        main.wait_stream(s)
+    for k, r in enumerate(results):
+        if k and torch.is_tensor(r):
+            r.record_stream(main)
+    return results
+
+
 def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
                 sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
                 perturb=None, stages=None):
@@ -203,6 +245,15 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
     Arguments as :func:`green_setup`; ``e_runs[r]`` is the energy added to the frequency of
     run r.  Returns g [R, n_omega] complex128 (device).
     """
+    return _drive(_green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize,
+                                     precision, sector, return_coeffs, normalize, scales, timing, capture, perturb,
+                                     stages))
+
+
+def _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
+                       sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
+                       perturb=None, stages=None):
+    """green_batch as a step generator: yields once, after the Lanczos launch."""
     omega = np.asarray(omega, dtype=np.float64)
     st = green_setup(eng, dop, restr, run_states, run_amps, krylovSize, precision, sector, normalize, scales,
                      perturb, stages)
@@ -212,7 +263,9 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
         return (g, None) if return_coeffs else g
     live, k_h = st.live, st.k
     alpha, beta = eng.lanczos(st.sector.csr, st.v0, k_h, precision=precision if precision in (1, 3) else 0,
-                              timing=timing)
+                              timing=timing, check=False)
+    yield
+    eng.read_status("lanczos")
     _mark(stages, "green:lanczos")
     e_live = np.asarray(e_runs, dtype=np.float64)[live]
     live_t = torch.from_numpy(live).to(eng.device)
@@ -307,6 +360,13 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
     ``batched=False`` runs upstream's call structure (one Green's function at a time).
     Returns g [n_states, n_ops, n_w] complex128 on the device.
     """
+    return _drive(spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision,
+                                capture, perturb, batched))
+
+
+def spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7, precision=0,
+                  capture=None, perturb=None, batched=True):
+    """spectra_device as a step generator for :func:`run_concurrently`."""
     ne = len(es)
     w = np.asarray(w, dtype=np.float64)
     run_states, run_amps, e_runs = [], [], []
@@ -317,8 +377,8 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
             run_amps.append(a_)
             e_runs.append(es[i])
     if batched:
-        g = green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision,
-                        capture=capture, perturb=perturb)
+        g = yield from _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize,
+                                          precision, capture=capture, perturb=perturb)
     else:
         g = green_runs_one_by_one(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision)
     return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
@@ -414,6 +474,16 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
 
     ``batched=False`` runs upstream's call structure: one shifted solve per incoming energy
     and one final-state Green's function per (incoming energy, outgoing channel)."""
+    return _drive(rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize,
+                             slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov, timing, capture,
+                             perturb, stages, batched))
+
+
+def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
+               slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
+               timing=None, capture=None, perturb=None, stages=None, batched=True):
+    """rixs_device as a step generator for :func:`run_concurrently` (yields after the launch
+    of the final-state Lanczos)."""
     _mark(stages, "start")
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
@@ -516,9 +586,9 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
     # runs getGreen on the normalised-then-pruned psi3 and scales by the squared norm taken
     # before the second pruning (spectra.py:1097-1124).
     if batched:
-        g = green_batch(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
-                        normalize=False, scales=scales, timing=timing, capture=capture, perturb=perturb,
-                        stages=stages)
+        g = yield from _green_batch_steps(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
+                                          normalize=False, scales=scales, timing=timing, capture=capture,
+                                          perturb=perturb, stages=stages)
     else:
         g = green_runs_one_by_one(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
                                   normalize=False, scales=scales)
@@ -529,6 +599,21 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
         gs[:, :, k] = gs[:, :, k0]
     _mark(stages, "rixs:assemble")
     return gs
+
+
+def xas_rixs_device(eng, dop, restr, xas_dops, tin_dops, tout_dops, psi_t, es, w, delta, wIns, wLoss, delta1, delta2,
+                    krylovSize=150, slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True,
+                    max_krylov=2000):
+    """XAS (:func:`spectra_device`) and the RIXS map (:func:`rixs_device`) of the same
+    eigenstates, computed side by side: the RIXS pipeline on the current stream, the XAS one
+    on a side stream, so the XAS host work (operator application, sector build) runs while
+    the RIXS final-state Lanczos occupies the GPU.  Same results as the two calls one after
+    the other.  Returns (g_xas [n_states, n_ops, n_w], g_rixs) on the device."""
+    g_rixs, g_xas = run_concurrently(eng, [
+        rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize,
+                   slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov),
+        spectra_steps(eng, dop, restr, xas_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision)])
+    return g_xas, g_rixs
 
 
 class _TransferMatrix:
