@@ -163,7 +163,8 @@ class Pipeline:
         from impuritymodel_gb300 import finite, spectra
 
         W = WORKLOAD
-        es, psi_t = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"])
+        es, psi_t = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"],
+                                              precision=3 if precision == 3 else 0)
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psi_t = es[:ne], psi_t[:ne]
         if capture is None and perturb is None and timing is None and batched:

@@ -171,6 +171,13 @@ class CsrMatrix:
 
 COMPONENTS_KERNEL_MAX_ROWS = 1 << 16  # single-CTA label propagation of edgpu_components
 
+
+def _df_to_c128(v):
+    """complex128-sized buffer holding double-float elements (re.hi, re.lo, im.hi, im.lo as
+    float32) -> the complex128 values."""
+    f = torch.view_as_real(v).contiguous().view(torch.float32).view(*v.shape, 4).to(torch.float64)
+    return torch.complex(f[..., 0] + f[..., 1], f[..., 2] + f[..., 3])
+
 # raw handle of the current stream without building a torch Stream object (about 10 us less
 # per library call); the public accessor is the fallback
 _raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
@@ -641,18 +648,24 @@ class Engine:
                                      _ptr(e_t), _ptr(sc), _ptr(torch.view_as_real(g)), self.stream), "cfrac")
         return g
 
-    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16):
+    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16, precision=0):
         """Lanczos with full reorthogonalisation from v0 (normalised, [N] complex128).
 
         ``stop(alpha, beta, j)`` (host arrays of length j) returns True when converged.
         Returns (V [K, N], alpha [K], beta [K]) with K the number of steps taken;
         ``beta[:K-1]`` is the tridiagonal's off-diagonal and ``beta[K-1]`` the coupling to
-        the next Krylov vector (0 when the space is exhausted).
+        the next Krylov vector (0 when the space is exhausted).  ``precision=3`` runs the
+        recurrence in double-float arithmetic (real H up to 65536 rows; otherwise FP64); V is
+        returned in complex128 either way.
         """
         n = csr.n
         if csr.ncols != n or v0.numel() != n:
             raise ValueError("krylov_reorth: square matrix and start vector of matching size required")
         k_cap = int(min(k_cap, n))
+        df = precision == 3 and csr.val_c is None and csr.val_r is not None and n <= (1 << 16)
+        if df:
+            csr.double_float()
+        launch = self.lib.edgpu_lanczos_reorth_df if df else self.lib.edgpu_lanczos_reorth
         V = torch.zeros((k_cap, n), dtype=torch.complex128, device=self.device)
         w = torch.zeros(n, dtype=torch.complex128, device=self.device)
         alpha = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
@@ -663,10 +676,9 @@ class Engine:
         while j < k_cap:
             j1 = min(k_cap, j + chunk)
             self.reset_status()
-            L.check(self.lib.edgpu_lanczos_reorth(C.byref(csr.struct()), _ptr(v0r), j, j1, k_cap,
-                                                  _ptr(torch.view_as_real(V)), _ptr(torch.view_as_real(w)),
-                                                  _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
-                    "lanczos_reorth")
+            L.check(launch(C.byref(csr.struct()), _ptr(v0r), j, j1, k_cap, _ptr(torch.view_as_real(V)),
+                           _ptr(torch.view_as_real(w)), _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn,
+                           self.stream), "lanczos_reorth")
             # one device-to-host read per chunk: status, alpha and beta together
             host = torch.cat([self.status.to(torch.float64), alpha[:j1], beta[:j1]]).cpu().numpy()
             st = int(host[0])
@@ -674,13 +686,13 @@ class Engine:
             if st == L.EDGPU_ERR_BREAKDOWN:
                 # invariant subspace: the Krylov space is exact at the first zero beta
                 kb = int(np.argmax(bh == 0.0)) + 1
-                return V[:kb], ah[:kb], bh[:kb]
+                return (_df_to_c128(V[:kb]) if df else V[:kb]), ah[:kb], bh[:kb]
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "lanczos_reorth")
             j = j1
             if stop is not None and stop(ah, bh, j):
                 break
-        return V[:j], ah[:j], bh[:j]
+        return (_df_to_c128(V[:j]) if df else V[:j]), ah[:j], bh[:j]
 
     def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).

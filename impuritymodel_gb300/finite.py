@@ -468,8 +468,9 @@ def get_tridiagonal_krylov_vectors(h, psi0, krylovSize, h_local=False, mode="spa
     return alpha[0, :k].cpu().numpy(), beta[0, : k - 1].cpu().numpy()
 
 
-def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
-    """Lowest ``k`` eigenpairs by Lanczos with full reorthogonalisation (FP64 on the GPU).
+def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
+    """Lowest ``k`` eigenpairs by Lanczos with full reorthogonalisation (FP64 on the GPU;
+    double-float arithmetic for a real H with ``precision=3``).
 
     Ritz values come from the Krylov tridiagonal matrix on the host each chunk; iteration
     stops when every wanted residual ``beta_j |s_{j,i}|`` is below
@@ -502,7 +503,7 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
         return bool(np.all(res <= tol_rel * np.maximum(1.0, np.abs(th[:k]))))
 
     while True:
-        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32)
+        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32, precision=precision)
         kk = len(a)
         th, s, res = residuals(a, bfull, kk)
         exact = kk >= n or (kk < k_cap and bfull[kk - 1] == 0.0)
@@ -517,14 +518,15 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0):
     return th[:kw], X
 
 
-def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7):
-    """Device form of :func:`eigensystem` on a :class:`_SortedBasis`.
+def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7, precision=0):
+    """Device form of :func:`eigensystem` on a :class:`_SortedBasis` (``precision=3``: the
+    Lanczos recurrence in double-float arithmetic when H is real).
 
     Returns (energies [k] host array, list of (states [m, W], amps [m, 2]) device tensors in
     caller basis order keeping ``|amp|^2 >= slaterWeightMin``).
     """
     csr = _device_hamiltonian(eng, dop, sb)
-    es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3))
+    es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3), precision=precision)
     vec_given = torch.empty_like(X)
     vec_given[:, sb.perm] = X
     k = len(es)

@@ -253,6 +253,20 @@ size_t edgpu_lanczos_reorth_workspace(int64_t n, int K_cap);
 int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
                          double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                          void* stream);
+/*
+ * The same reorthogonalised Lanczos in double-float arithmetic (float hi/lo pairs, about 48
+ * significand bits, on the FP32 pipe) for a real H with its val_df copy set and n <= 65536,
+ * as one cooperative launch per call.  V and w hold double-float elements (re.hi, re.lo,
+ * im.hi, im.lo as floats; 16 bytes like complex128); v0 is complex128; alpha and beta FP64.
+ * V[j] is written by step j itself (v_{j+1} = w / beta_j is formed by the next call's first
+ * step), so after steps j0 .. j1-1 V holds v_0 .. v_{j1-1} and w the unnormalised
+ * remainder.  Same workspace as edgpu_lanczos_reorth.  EDGPU_ERR_ARG for a complex H, a
+ * missing val_df, n > 65536 or a device without cooperative launch.  No counterpart in
+ * upstream impurityModel (an arithmetic form of the call above).
+ */
+int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
+                            double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                            void* stream);
 /* Process-wide switch (default 1): 0 sends every edgpu_lanczos_reorth call to the
  * per-step kernels (both paths compute the same recurrence; used to test one against the
  * other).  No counterpart in upstream impurityModel. */
