@@ -672,15 +672,30 @@ class Engine:
         beta = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
         ws, wsn = self.workspace(self.lib.edgpu_lanczos_reorth_workspace(n, k_cap))
         v0r = torch.view_as_real(v0.contiguous())
-        j = 0
-        while j < k_cap:
-            j1 = min(k_cap, j + chunk)
+        # one pinned device-to-host copy per chunk (status, alpha and beta together), read
+        # through an event, so the next chunk is already queued while the host tests this
+        # one (a chunk past convergence only writes beyond the returned steps)
+        host_t = torch.empty(1 + 2 * k_cap, dtype=torch.float64, pin_memory=True)
+
+        def enqueue(j0, j1):
             self.reset_status()
-            L.check(launch(C.byref(csr.struct()), _ptr(v0r), j, j1, k_cap, _ptr(torch.view_as_real(V)),
+            L.check(launch(C.byref(csr.struct()), _ptr(v0r), j0, j1, k_cap, _ptr(torch.view_as_real(V)),
                            _ptr(torch.view_as_real(w)), _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn,
                            self.stream), "lanczos_reorth")
-            # one device-to-host read per chunk: status, alpha and beta together
-            host = torch.cat([self.status.to(torch.float64), alpha[:j1], beta[:j1]]).cpu().numpy()
+            host_t[: 1 + 2 * j1].copy_(torch.cat([self.status.to(torch.float64), alpha[:j1], beta[:j1]]),
+                                       non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            return ev
+
+        j = 0
+        j1 = min(k_cap, chunk)
+        ev = enqueue(0, j1)
+        while True:
+            ev.synchronize()
+            host = host_t[: 1 + 2 * j1].numpy().copy()
+            jn = min(k_cap, j1 + chunk)
+            ev_next = enqueue(j1, jn) if jn > j1 else None  # speculative next chunk
             st = int(host[0])
             ah, bh = host[1:1 + j1], host[1 + j1:]
             if st == L.EDGPU_ERR_BREAKDOWN:
@@ -690,8 +705,9 @@ class Engine:
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "lanczos_reorth")
             j = j1
-            if stop is not None and stop(ah, bh, j):
+            if ev_next is None or (stop is not None and stop(ah, bh, j)):
                 break
+            j1, ev = jn, ev_next
         return (_df_to_c128(V[:j]) if df else V[:j]), ah[:j], bh[:j]
 
     def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0):

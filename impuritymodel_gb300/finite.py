@@ -486,9 +486,10 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
     v0 = v0 / torch.linalg.vector_norm(v0)
 
     def ritz(a, bfull):
+        # the lowest min(k, j) Ritz pairs only (all that the stop test and the result use)
         if len(a) == 1:
             return np.array(a, dtype=float), np.ones((1, 1))
-        return scipy.linalg.eigh_tridiagonal(a, bfull[: len(a) - 1])
+        return scipy.linalg.eigh_tridiagonal(a, bfull[: len(a) - 1], select="i", select_range=(0, min(k, len(a)) - 1))
 
     def residuals(a, bfull, j):
         th, s = ritz(a, bfull)
