@@ -516,9 +516,12 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     # (t_in, eigenstate) right-hand side
     keys = [k for k, (s1, _) in psi1.items() if s1.shape[0]]
     Y = torch.zeros((len(keys), core.n), dtype=torch.complex128, device=eng.device)
-    for r, key in enumerate(keys):
-        s1, a1 = psi1[key]
-        Y[r].index_put_((eng.lookup(core.basis, s1),), torch.complex(a1[:, 0], a1[:, 1]), accumulate=True)
+    # every right-hand side in one lookup and one scatter (each psi1 holds distinct states)
+    s_all = torch.cat([psi1[k][0] for k in keys], 0)
+    a_all = torch.cat([psi1[k][1] for k in keys], 0)
+    r_all = torch.repeat_interleave(torch.arange(len(keys), device=eng.device),
+                                    torch.tensor([int(psi1[k][0].shape[0]) for k in keys], device=eng.device))
+    Y.view(-1)[r_all * core.n + eng.lookup(core.basis, s_all)] = torch.complex(a_all[:, 0], a_all[:, 1])
     zs = np.array([wIns + 1j * delta1 + es[ie] for (_, ie) in keys])
     # without reorthogonalisation the recurrence may need a few times the sector dimension
     k_solve = min(6 * core.n + 50, max_krylov)
