@@ -158,6 +158,9 @@ class Pipeline:
         self.out_dops = [DeviceOp(t, eng.device) for t in m.rixs_out_ops()]
         self.sb = finite._SortedBasis(eng, list(self.basis), self.n)
         self.w, self.w_in, self.w_loss = meshes()
+        # the host operator dicts a caller of the dict API holds (built once, outside any step)
+        self.xas_ops_host = m.xas_ops()
+        self.out_ops_host = m.rixs_out_ops()
 
     def step(self, precision=0, timing=None, capture=None, perturb=None, batched=True):
         from impuritymodel_gb300 import finite, spectra
@@ -189,14 +192,14 @@ class Pipeline:
 
         W = WORKLOAD
         m = self.mod
-        es, psis = finite.eigensystem(self.n, m.hOp, self.basis, W["n_psi"])
+        es, psis = finite.eigensystem(self.n, m.hOp, self.basis, W["n_psi"], precision=precision)
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psis = es[:ne], psis[:ne]
-        g_xas = spectra.getSpectra(self.n, m.hOp, m.xas_ops(), psis, es, self.w, W["xas"]["delta"], m.restrictions,
-                                   W["krylov"], W["slater_weight_min"], precision=precision)
-        g_rixs = spectra.getRIXSmap(self.n, m.hOp, m.xas_ops(), m.rixs_out_ops(), psis, es, self.w_in, self.w_loss,
-                                    W["rixs"]["delta_in"], W["rixs"]["delta_loss"], m.restrictions, W["krylov"],
-                                    W["slater_weight_min"], precision=precision)
+        g_xas = spectra.getSpectra(self.n, m.hOp, self.xas_ops_host, psis, es, self.w, W["xas"]["delta"],
+                                   m.restrictions, W["krylov"], W["slater_weight_min"], precision=precision)
+        g_rixs = spectra.getRIXSmap(self.n, m.hOp, self.xas_ops_host, self.out_ops_host, psis, es, self.w_in,
+                                    self.w_loss, W["rixs"]["delta_in"], W["rixs"]["delta_loss"], m.restrictions,
+                                    W["krylov"], W["slater_weight_min"], precision=precision)
         return es, g_xas, g_rixs
 
 

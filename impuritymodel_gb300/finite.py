@@ -542,12 +542,13 @@ def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMi
 
 
 def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", eigenValueTol=1e-9,
-                slaterWeightMin=1e-7):
+                slaterWeightMin=1e-7, precision=0):
     """Lowest eigenpairs and eigenstates as dicts (upstream finite.py:58-118).
 
-    ``groundDiagMode='Lanczos'`` runs Lanczos with full reorthogonalisation on the GPU;
-    ``'full'`` diagonalises the dense matrix (upstream ``np.linalg.eigh``).  Eigenvectors
-    keep product states with ``|amp|^2 >= slaterWeightMin``.
+    ``groundDiagMode='Lanczos'`` runs Lanczos with full reorthogonalisation on the GPU
+    (``precision=3``: in double-float arithmetic when H is real; an addition to upstream's
+    signature); ``'full'`` diagonalises the dense matrix (upstream ``np.linalg.eigh``).
+    Eigenvectors keep product states with ``|amp|^2 >= slaterWeightMin``.
     """
     eng = get_engine()
     n = int(n_spin_orbitals)
@@ -561,7 +562,8 @@ def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", 
         es = es[:nPsiMax]
         vecs = vecs[:, :nPsiMax]
     elif groundDiagMode == "Lanczos":
-        es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3))
+        es, X = eig_lowest(eng, csr, nPsiMax, tol_rel=min(1e-12, eigenValueTol * 1e-3),
+                           precision=3 if precision == 3 else 0)
         # sorted position -> caller position
         vec_sorted = X.t().contiguous()
         vecs_t = torch.empty_like(vec_sorted)
