@@ -1,10 +1,13 @@
 // Operator application on packed product states (warp per input state).
 //
 // apply_columns: H|b> for single product states b (upstream finite.applyOp with {b: 1},
-//   impurityModel/ed/finite.py:1301-1511).  Terms that map a state onto itself ("diagonal"
-//   terms, flag bit 0) are accumulated in term order by warp shuffles; the few off-diagonal
-//   emissions go to a per-warp shared-memory buffer where equal output states are merged in
-//   term order.  This reproduces upstream's sequential dict sums bit for bit.
+//   impurityModel/ed/finite.py:1301-1511), warp per state.  Terms that map a state onto
+//   itself ("diagonal" terms, flag bit 0) are listed in term order and then summed by one lane
+//   per state, the eight states of a block sharing each FP64 warp instruction (GB300 issues
+//   an FP64 add in ~20 cycles per warp instruction whatever the number of active lanes, so a
+//   warp-wide sum of one state's hundreds of diagonal terms kept the FP64 pipe busy); the
+//   off-diagonal emissions go to a per-warp shared-memory buffer where equal output states
+//   are merged in term order.  This reproduces upstream's sequential dict sums bit for bit.
 // apply_vector: raw emissions of an operator on a weighted multi-state psi, in (state, term)
 //   order, for a later stable sort + segmented sum.
 #include "common.cuh"
@@ -34,6 +37,12 @@ struct ColParams {
   int32_t* status;
 };
 
+// -x by flipping the sign bit on the integer pipe (an FP64 negation would queue on GB300's
+// narrow FP64 pipe, ~64 cycles latency and ~20 cycles of issue per warp instruction)
+__device__ __forceinline__ double neg_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
 template <int W>
 __device__ __forceinline__ bool filter_pass(const ColParams& p, const uint64_t (&s)[W], int64_t& idx) {
   idx = -1;
@@ -55,6 +64,7 @@ __global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
   const uint64_t* sops = p.ops;
   const uint32_t* sflags = p.flags;
   size_t off = 0;
+  int cplx = 0;  // some coefficient has a nonzero imaginary part
   if (p.stage_terms) {
     double2* c = reinterpret_cast<double2*>(smem);
     uint64_t* o = reinterpret_cast<uint64_t*>(smem + 16 * (size_t)T);
@@ -63,76 +73,127 @@ __global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
       c[t] = p.coeff[t];
       o[t] = p.ops[t];
       f[t] = p.flags[t];
+      cplx |= c[t].y != 0.0;
     }
     scoeff = c;
     sops = o;
     sflags = f;
     off = (28 * (size_t)T + 15) & ~(size_t)15;
-    __syncthreads();
+  } else {
+    for (int t = threadIdx.x; t < T; t += blockDim.x) cplx |= p.coeff[t].y != 0.0;
   }
+  cplx = __syncthreads_or(cplx);
   const int cap = p.cap;
-  const size_t per_warp = (size_t)cap * (16 + 8 * W + 4);
+  const int nwords = (T + 31) >> 5;
+  const size_t per_warp = (((size_t)cap * (20 + 8 * W) + 8 * (size_t)nwords) + 15) & ~(size_t)15;
   unsigned char* wbase = smem + off + per_warp * warp;
   double2* wvals = reinterpret_cast<double2*>(wbase);
   uint64_t* wkeys = reinterpret_cast<uint64_t*>(wbase + 16 * (size_t)cap);
   int* wtidx = reinterpret_cast<int*>(wbase + (16 + 8 * W) * (size_t)cap);
+  // valid diagonal terms of the warp's state and their odd parities, one bit per term
+  uint32_t* wvalid = reinterpret_cast<uint32_t*>(wbase + (20 + 8 * W) * (size_t)cap);
+  uint32_t* wodd = wvalid + nwords;
+  __shared__ int nd_s[8];
+  __shared__ double2 dsum_s[8];
+  __shared__ int dfirst_s[8];
 
   const bool fill = p.offsets != nullptr;
-  for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += (int64_t)gridDim.x * wpb) {
+  // block-uniform loop: warp w of the block takes state jb + w
+  for (int64_t jb = (int64_t)blockIdx.x * wpb; jb < p.n_states; jb += (int64_t)gridDim.x * wpb) {
+    const int64_t j = jb + warp;
+    const bool active = j < p.n_states;
     uint64_t s0[W];
-    load_state<W>(p.states + j * W, s0);
-    double dre = 0.0, dim = 0.0;
-    int dfirst = -1;
+#pragma unroll
+    for (int q = 0; q < W; ++q) s0[q] = 0;
+    if (active) load_state<W>(p.states + j * W, s0);
     int m = 0;
-    for (int base = 0; base < T; base += 32) {
-      const int t = base + lane;
-      bool valid = false, isdiag = false;
-      double vre = 0.0, vim = 0.0;
-      uint64_t s[W];
-#pragma unroll
-      for (int q = 0; q < W; ++q) s[q] = s0[q];
-      if (t < T) {
+    if (active) {
+      for (int base = 0; base < T; base += 32) {
+        const int t = base + lane;
+        bool valid = false, isdiag = false;
         int par = 0;
-        valid = apply_term<W>(s, sops[t], par);
-        if (valid) {
-          double2 c = scoeff[t];
-          if (par & 1) {
-            c.x = -c.x;
-            c.y = -c.y;
-          }
-          vre = c.x;
-          vim = c.y;
-          isdiag = (sflags[t] & 1u) != 0;
-        }
-      }
-      unsigned bd = __ballot_sync(FULL, valid && isdiag);
-      const unsigned bo = __ballot_sync(FULL, valid && !isdiag);
-      while (bd) {
-        const int k = __ffs(bd) - 1;
-        bd &= bd - 1;
-        const double xr = __shfl_sync(FULL, vre, k);
-        const double xi = __shfl_sync(FULL, vim, k);
-        if (dfirst < 0) {
-          dre = xr;
-          dim = xi;
-          dfirst = base + k;
-        } else {
-          dre = __dadd_rn(dre, xr);
-          dim = __dadd_rn(dim, xi);
-        }
-      }
-      if (bo) {
-        const int pos = m + __popc(bo & ((1u << lane) - 1u));
-        if (valid && !isdiag && pos < cap) {
+        double vre = 0.0, vim = 0.0;
+        uint64_t s[W];
 #pragma unroll
-          for (int q = 0; q < W; ++q) wkeys[(size_t)pos * W + q] = s[q];
-          wvals[pos] = make_double2(vre, vim);
-          wtidx[pos] = t;
+        for (int q = 0; q < W; ++q) s[q] = s0[q];
+        if (t < T) {
+          valid = apply_term<W>(s, sops[t], par);
+          if (valid) {
+            isdiag = (sflags[t] & 1u) != 0;
+            if (!isdiag) {
+              double2 c = scoeff[t];
+              if (par & 1) {
+                c.x = neg_bits(c.x);
+                c.y = neg_bits(c.y);
+              }
+              vre = c.x;
+              vim = c.y;
+            }
+          }
         }
-        m += __popc(bo);
+        const unsigned bd = __ballot_sync(FULL, valid && isdiag);
+        const unsigned bp = __ballot_sync(FULL, valid && isdiag && (par & 1));
+        const unsigned bo = __ballot_sync(FULL, valid && !isdiag);
+        if (lane == 0) {
+          wvalid[base >> 5] = bd;
+          wodd[base >> 5] = bp;
+        }
+        if (bo) {
+          const int pos = m + __popc(bo & ((1u << lane) - 1u));
+          if (valid && !isdiag && pos < cap) {
+#pragma unroll
+            for (int q = 0; q < W; ++q) wkeys[(size_t)pos * W + q] = s[q];
+            wvals[pos] = make_double2(vre, vim);
+            wtidx[pos] = t;
+          }
+          m += __popc(bo);
+        }
       }
     }
+    if (lane == 0) nd_s[warp] = active ? 1 : 0;
     __syncwarp();
+    __syncthreads();
+    // Diagonal sums in term order, lane w of warp 0 for the state of warp w: the sequential
+    // FP64 adds of up to eight states share each warp instruction.
+    if (warp == 0 && lane < wpb) {
+      double re = 0.0, im = 0.0;
+      int first = -1;
+      if (nd_s[lane]) {
+        const uint32_t* V = reinterpret_cast<const uint32_t*>(smem + off + per_warp * lane + (20 + 8 * W) * (size_t)cap);
+        const uint32_t* O = V + nwords;
+        for (int q = 0; q < nwords; ++q) {
+          uint32_t bits = V[q];
+          const uint32_t odd = O[q];
+          while (bits) {
+            const int k = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int tq = (q << 5) + k;
+            double2 c = scoeff[tq];
+            if ((odd >> k) & 1u) {
+              c.x = neg_bits(c.x);
+              c.y = neg_bits(c.y);
+            }
+            if (first < 0) {
+              re = c.x;
+              im = c.y;
+              first = tq;
+            } else {
+              re = __dadd_rn(re, c.x);
+              // real operator: every imaginary part is a signed zero, and the sum of signed
+              // zeros is -0 only when all of them are -0 (IEEE round to nearest)
+              im = cplx ? __dadd_rn(im, c.y)
+                        : __longlong_as_double(__double_as_longlong(im) & __double_as_longlong(c.y));
+            }
+          }
+        }
+      }
+      dsum_s[lane] = make_double2(re, im);
+      dfirst_s[lane] = first;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const double dre = dsum_s[warp].x, dim = dsum_s[warp].y;
+    const int dfirst = dfirst_s[warp];
     if (m > cap) {
       if (lane == 0) {
         atomicExch(p.status, (int32_t)EDGPU_ERR_OVERFLOW);
@@ -190,7 +251,7 @@ __global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
         const int64_t o = obase + rank;
         if (p.out_states) store_state<W>(p.out_states + o * W, key);
         if (p.out_index) p.out_index[o] = idx;
-        if (p.out_vals) p.out_vals[o] = make_double2(sre, p.conj_vals ? -sim : sim);
+        if (p.out_vals) p.out_vals[o] = make_double2(sre, p.conj_vals ? neg_bits(sim) : sim);
       }
       kept += __popc(bk);
       dbefore += __popc(bb);
@@ -201,7 +262,7 @@ __global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
       const int64_t o = obase + dbefore;
       if (p.out_states) store_state<W>(p.out_states + o * W, s0);
       if (p.out_index) p.out_index[o] = didx;
-      if (p.out_vals) p.out_vals[o] = make_double2(dre, p.conj_vals ? -dim : dim);
+      if (p.out_vals) p.out_vals[o] = make_double2(dre, p.conj_vals ? neg_bits(dim) : dim);
     }
     __syncwarp();
   }
@@ -305,7 +366,8 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
   p.status = status_dev;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t term_bytes = (28 * (size_t)p.n_terms + 15) & ~(size_t)15;
-  const size_t per_warp = (size_t)p.cap * (16 + 8 * n_words + 4);
+  const size_t per_warp =
+      (((size_t)p.cap * (20 + 8 * (size_t)n_words) + 8 * (size_t)((p.n_terms + 31) / 32)) + 15) & ~(size_t)15;
   const size_t smem_max = 220 * 1024;
   int warps = 8;
   p.stage_terms = 1;
