@@ -655,7 +655,7 @@ class Engine:
                                      _ptr(e_t), _ptr(sc), _ptr(torch.view_as_real(g)), self.stream), "cfrac")
         return g
 
-    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16, precision=0):
+    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16, precision=0, remaining=None):
         """Lanczos with full reorthogonalisation from v0 (normalised, [N] complex128).
 
         ``stop(alpha, beta, j)`` (host arrays of length j) returns True when converged.
@@ -663,7 +663,9 @@ class Engine:
         ``beta[:K-1]`` is the tridiagonal's off-diagonal and ``beta[K-1]`` the coupling to
         the next Krylov vector (0 when the space is exhausted).  ``precision=3`` runs the
         recurrence in double-float arithmetic (real H up to 65536 rows; otherwise FP64); V is
-        returned in complex128 either way.
+        returned in complex128 either way.  ``remaining(j)`` (optional) estimates the steps
+        still needed after step j; the chunk queued ahead of each convergence test is then cut
+        to that estimate (at least 8 steps), so little work runs past convergence.
         """
         n = csr.n
         if csr.ncols != n or v0.numel() != n:
@@ -701,7 +703,12 @@ class Engine:
         while True:
             ev.synchronize()
             host = host_t[: 1 + 2 * j1].numpy().copy()
-            jn = min(k_cap, j1 + chunk)
+            size = chunk
+            if remaining is not None:
+                est = remaining(j1)
+                if est is not None:
+                    size = int(min(chunk, max(8, np.ceil(est) + 4)))
+            jn = min(k_cap, j1 + size)
             ev_next = enqueue(j1, jn) if jn > j1 else None  # speculative next chunk
             st = int(host[0])
             ah, bh = host[1:1 + j1], host[1 + j1:]

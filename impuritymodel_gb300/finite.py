@@ -497,14 +497,30 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
             return th, s, np.zeros(min(k, j))
         return th, s, np.abs(bfull[j - 1] * s[-1, : min(k, j)])
 
+    history = []  # (j, log of the worst residual / tolerance ratio) at each convergence test
+
     def stop(a, bfull, j):
         if j < k:
             return False
         th, _, res = residuals(a, bfull, j)
-        return bool(np.all(res <= tol_rel * np.maximum(1.0, np.abs(th[:k]))))
+        ratio = res / (tol_rel * np.maximum(1.0, np.abs(th[:k])))
+        history.append((j, float(np.log(max(ratio.max(), 1e-300)))))
+        return bool(np.all(ratio <= 1.0))
+
+    def remaining(j):
+        # steps still needed after step j, extrapolating the geometric residual decay of the
+        # last two tests (None until two tests exist or while the residual does not decay)
+        if len(history) < 2:
+            return None
+        (j1, r1), (j2, r2) = history[-2], history[-1]
+        slope = (r2 - r1) / max(j2 - j1, 1)
+        if not slope < 0.0:
+            return None
+        return j2 + (-r2 / slope) - j
 
     while True:
-        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32, precision=precision)
+        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32, precision=precision,
+                                        remaining=remaining)
         kk = len(a)
         th, s, res = residuals(a, bfull, kk)
         exact = kk >= n or (kk < k_cap and bfull[kk - 1] == 0.0)
