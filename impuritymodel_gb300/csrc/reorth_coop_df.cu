@@ -15,6 +15,11 @@
 //   D1  w -= V h on tiles of 16 rows x 64 k-classes (a warp: 16 rows x 2 k-classes).
 //   C2  h_k = <v_k, w>.
 //   D2  w -= V h, partials of |w|^2.
+// C1 and D1 also sum |w'|^2 and |w|^2; the second pass (C2, D2) runs only when the first one
+// removed more than half of |w'|^2 (Kahan's "twice is enough" test: after a pass that keeps
+// |w| >= |w'| / sqrt(2), w is orthogonal to V to working precision).  In a Lanczos step w'
+// is already orthogonal to V up to rounding, so the second pass is normally skipped and a
+// step takes three grid barriers.
 // Every block sums the per-block partials in one fixed order, so all blocks hold identical
 // alpha, beta and take identical branches; beta_j is formed after D2's barrier and v_{j+1} is
 // materialised by the next step's gather (also across chunk launches: w and beta persist).
@@ -74,7 +79,7 @@ __global__ void __launch_bounds__(kCoopDfThreads)
     lanczos_reorth_coop_df_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                                   const float2* __restrict__ hv, const double2* __restrict__ v0, int j0, int j1,
                                   int K_cap, float4* V, float4* w, float4* y, double* alpha, double* beta,
-                                  int32_t* status, dfl* pa, dfl* pn, float4* hc) {
+                                  int32_t* status, dfl* pa, dfl* pn, dfl* pw, float4* hc) {
   cg::grid_group grid = cg::this_grid();
   const int B = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -235,7 +240,17 @@ __global__ void __launch_bounds__(kCoopDfThreads)
     if (b == 0 && tid == 0) alpha[j] = df_val(a);
     if (j + 1 >= K_cap) break;  // identical in every block
     const dfl na = {-a.hi, -a.lo}, nb = {-bprev.hi, -bprev.lo};
-    for (int64_t i = gtid; i < n; i += gthreads) w[i] = three_term(y[i], vj[i], vjm1 ? vjm1 + i : nullptr, na, nb);
+    {
+      dacc nw = {0.f, 0.f};
+      for (int64_t i = gtid; i < n; i += gthreads) {
+        const float4 x = three_term(y[i], vj[i], vjm1 ? vjm1 + i : nullptr, na, nb);
+        w[i] = x;
+        dacc_fma(nw, {x.x, x.y}, x.x, x.y);
+        dacc_fma(nw, {x.z, x.w}, x.z, x.w);
+      }
+      const dfl s = df_block_sum2<kCoopDfWarps>(dacc_val(nw), red);  // |w'|^2 partial
+      if (tid == 0) pw[b] = s;
+    }
     const int m = j + 1;
     for (int k = b; k < m; k += B) {
       const float4* vk = V + (int64_t)k * n;
@@ -250,14 +265,31 @@ __global__ void __launch_bounds__(kCoopDfThreads)
         dot_acc(hr, hm, a2, w2);
       }
       if (i < n) dot_acc(hr, hm, vk[i], three_term(y[i], vj[i], vjm1 ? vjm1 + i : nullptr, na, nb));
-      const dfl sr = df_block_sum2<kCoopDfWarps>(dacc_val(hr), red);
-      const dfl si = df_block_sum2<kCoopDfWarps>(dacc_val(hm), red + 40);
+      const dfl sr = df_block_sum2<kCoopDfWarps>(dacc_val(hr), red + 40);
+      const dfl si = df_block_sum2<kCoopDfWarps>(dacc_val(hm), red);
       if (tid == 0) hc[k] = df4(sr, si);
     }
     grid.sync();
-    // ---- D1
-    project(m, false);
+    // ---- D1, with the partials of |w|^2 after the first pass
+    {
+      const dfl s = project(m, true);
+      if (tid == 0) pn[b] = s;
+    }
     grid.sync();
+    const dfl nw1 = coop_fixed_sum_df(pw, B, red + 40);
+    dfl nw2 = coop_fixed_sum_df(pn, B, red);
+    if (!(nw2.hi < 0.5f * nw1.hi)) {  // one pass was enough (identical in every block)
+      const dfl bt = df_sqrt(nw2);
+      if (b == 0 && tid == 0) {
+        const double bd = df_val(bt);
+        beta[j] = bd;
+        if (!(bd > 0.0)) atomicExch(status, (int32_t)(bd == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+      }
+      __syncthreads();  // the next step's first sum reuses the buffer of nw2
+      if (!(bt.hi > 0.f)) break;
+      bprev = bt;
+      continue;
+    }
     // ---- C2
     for (int k = b; k < m; k += B) {
       const float4* vk = V + (int64_t)k * n;
@@ -270,8 +302,8 @@ __global__ void __launch_bounds__(kCoopDfThreads)
         dot_acc(hr, hm, a2, x2);
       }
       if (i < n) dot_acc(hr, hm, vk[i], w[i]);
-      const dfl sr = df_block_sum2<kCoopDfWarps>(dacc_val(hr), red);
-      const dfl si = df_block_sum2<kCoopDfWarps>(dacc_val(hm), red + 40);
+      const dfl sr = df_block_sum2<kCoopDfWarps>(dacc_val(hr), red + 40);
+      const dfl si = df_block_sum2<kCoopDfWarps>(dacc_val(hm), red);
       if (tid == 0) hc[k] = df4(sr, si);
     }
     grid.sync();
@@ -304,7 +336,7 @@ extern "C" int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int
   if (j0 == 0 && !v0) return EDGPU_ERR_ARG;
   if (!h->val_df || h->val_c || h->n > kCoopDfMaxN) return EDGPU_ERR_ARG;
   const int64_t n = h->n;
-  const size_t need = sizeof(float4) * (size_t)n + 2 * sizeof(dfl) * kCoopDfMaxBlocks +
+  const size_t need = sizeof(float4) * (size_t)n + 3 * sizeof(dfl) * kCoopDfMaxBlocks +
                       sizeof(float4) * (size_t)(K_cap + 1) + 4 * 256;
   if (workspace_bytes < need) return EDGPU_ERR_WORKSPACE;
   if (j0 == j1) return EDGPU_OK;
@@ -335,6 +367,7 @@ extern "C" int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int
   float4* y = reinterpret_cast<float4*>(carve(sizeof(float4) * (size_t)n));
   dfl* pa = reinterpret_cast<dfl*>(carve(sizeof(dfl) * kCoopDfMaxBlocks));
   dfl* pn = reinterpret_cast<dfl*>(carve(sizeof(dfl) * kCoopDfMaxBlocks));
+  dfl* pw = reinterpret_cast<dfl*>(carve(sizeof(dfl) * kCoopDfMaxBlocks));
   float4* hc = reinterpret_cast<float4*>(carve(sizeof(float4) * (size_t)(K_cap + 1)));
   const int64_t* rp = h->row_ptr;
   const int32_t* col = h->col;
@@ -344,7 +377,7 @@ extern "C" int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int
   float4* w = reinterpret_cast<float4*>(wd);
   void* args[] = {(void*)&n, (void*)&rp, (void*)&col, (void*)&hv, (void*)&v0c, (void*)&j0, (void*)&j1, (void*)&K_cap,
                   (void*)&V, (void*)&w, (void*)&y, (void*)&alpha, (void*)&beta, (void*)&status_dev, (void*)&pa,
-                  (void*)&pn, (void*)&hc};
+                  (void*)&pn, (void*)&pw, (void*)&hc};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_reorth_coop_df_kernel, blocks, kCoopDfThreads,
                                                     args, kCacheBytes, (cudaStream_t)stream);
   note_launch();
