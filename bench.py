@@ -166,16 +166,19 @@ class Pipeline:
         from impuritymodel_gb300 import finite, spectra
 
         W = WORKLOAD
-        es, psi_t = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"],
-                                              precision=3 if precision == 3 else 0)
+        es, psi_t, h_gs = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"],
+                                                    precision=3 if precision == 3 else 0, with_hamiltonian=True)
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psi_t = es[:ne], psi_t[:ne]
+        # the ground-state sector serves the RIXS final states when it is closed
+        gs_sector = spectra.closed_sector(self.eng, self.dop, self.restr, self.sb.sorted, h_gs,
+                                          self.sb.words) if batched else None
         if capture is None and perturb is None and timing is None and batched:
             # XAS on a side stream while the RIXS pipeline runs on the current one
             g_xas, g_rixs = spectra.xas_rixs_device(
                 self.eng, self.dop, self.restr, self.xas_dops, self.xas_dops, self.out_dops, psi_t, es, self.w,
                 W["xas"]["delta"], self.w_in, self.w_loss, W["rixs"]["delta_in"], W["rixs"]["delta_loss"],
-                W["krylov"], W["slater_weight_min"], precision)
+                W["krylov"], W["slater_weight_min"], precision, final_sector=gs_sector)
             return es, g_xas, g_rixs
         g_xas = spectra.spectra_device(self.eng, self.dop, self.restr, self.xas_dops, psi_t, es, self.w,
                                        W["xas"]["delta"], W["krylov"], W["slater_weight_min"], precision,
@@ -183,7 +186,7 @@ class Pipeline:
         g_rixs = spectra.rixs_device(self.eng, self.dop, self.restr, self.xas_dops, self.out_dops, psi_t, es,
                                      self.w_in, self.w_loss, W["rixs"]["delta_in"], W["rixs"]["delta_loss"],
                                      W["krylov"], W["slater_weight_min"], precision, timing=timing,
-                                     capture=capture, perturb=perturb, batched=batched)
+                                     capture=capture, perturb=perturb, batched=batched, final_sector=gs_sector)
         return es, g_xas, g_rixs
 
     def e2e_step(self, precision=0):

@@ -535,9 +535,11 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
     return th[:kw], X
 
 
-def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7, precision=0):
+def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7, precision=0,
+                       with_hamiltonian=False):
     """Device form of :func:`eigensystem` on a :class:`_SortedBasis` (``precision=3``: the
-    Lanczos recurrence in double-float arithmetic when H is real).
+    Lanczos recurrence in double-float arithmetic when H is real).  ``with_hamiltonian=True``
+    also returns the sector Hamiltonian (CSR on ``sb.sorted``) as a third value.
 
     Returns (energies [k] host array, list of (states [m, W], amps [m, 2]) device tensors in
     caller basis order keeping ``|amp|^2 >= slaterWeightMin``).
@@ -554,6 +556,8 @@ def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMi
     states_all = sb.given[idx]
     psis = [(states_all[bounds[q]:bounds[q + 1]].contiguous(), amps_all[bounds[q]:bounds[q + 1]].contiguous())
             for q in range(k)]
+    if with_hamiltonian:
+        return np.asarray(es), psis, csr
     return np.asarray(es), psis
 
 

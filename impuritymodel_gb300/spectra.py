@@ -84,6 +84,15 @@ class Sector:
         self._labels = None
         self._sizes = None
 
+    @classmethod
+    def from_parts(cls, basis, csr):
+        """A sector from a sorted basis and its Hamiltonian built elsewhere."""
+        s = cls.__new__(cls)
+        s.basis, s.csr, s.n = basis, csr, basis.shape[0]
+        s._labels = None
+        s._sizes = None
+        return s
+
     def components(self, eng):
         """Component label of every state (its smallest member) and the size of each component
         stored at its label's index (0 elsewhere); no host synchronisation."""
@@ -110,6 +119,39 @@ class Sector:
         return dims
 
 
+def _popcount64(x):
+    """Bit counts of a uint64 array (SWAR, no numpy version requirement)."""
+    x = x.astype(np.uint64)
+    x = x - ((x >> np.uint64(1)) & np.uint64(0x5555555555555555))
+    x = (x & np.uint64(0x3333333333333333)) + ((x >> np.uint64(2)) & np.uint64(0x3333333333333333))
+    x = (x + (x >> np.uint64(4))) & np.uint64(0x0F0F0F0F0F0F0F0F)
+    return ((x * np.uint64(0x0101010101010101)) >> np.uint64(56)).astype(np.int64)
+
+
+def closed_sector(eng, dop, restr, basis_sorted, csr, words_host):
+    """The sector of ``basis_sorted`` (device, sorted) with its Hamiltonian ``csr`` when every
+    basis state satisfies the restrictions and H (restricted) maps the basis into itself; else
+    None.  Such a basis contains the closure of any of its states (upstream expand_basis,
+    finite.py:1696-1803) as a union of its connected components, with the same Hamiltonian
+    rows, so Green's-function runs that start inside it can use it instead of a fresh
+    expansion.  ``words_host``: the basis as host uint64 words (any order)."""
+    from . import _lib as L
+
+    if restr is not None:
+        w = np.asarray(words_host, dtype=np.uint64)
+        for k in range(int(restr.n)):
+            cnt = np.zeros(w.shape[0], dtype=np.int64)
+            for q in range(w.shape[1]):
+                cnt += _popcount64(w[:, q] & np.uint64(restr.mask[k][q] & 0xFFFFFFFFFFFFFFFF))
+            if np.any(cnt < int(restr.lo[k])) or np.any(cnt > int(restr.hi[k])):
+                return None
+    offsets, _, _, _ = eng.apply_columns(basis_sorted, dop, restr, 1e-12, basis=basis_sorted,
+                                         filt=L.FILTER_NOT_IN_BASIS)
+    if int(offsets[-1].item()) != 0:
+        return None
+    return Sector.from_parts(basis_sorted, csr)
+
+
 class GreenSetup:
     """Start vectors of a batch of Green's-function runs on one sector (see green_setup)."""
 
@@ -123,7 +165,7 @@ class GreenSetup:
 
 
 def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision=0, sector=None, normalize=True,
-                scales=None, perturb=None, stages=None):
+                scales=None, perturb=None, stages=None, sector_hint=None):
     """Sector, start vectors and Krylov sizes of a batch of Green's-function runs.
 
     ``run_states[r]`` [n_r, W] / ``run_amps[r]`` [n_r, 2] are the start states (lists), or
@@ -158,6 +200,9 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
     if live.size == 0:
         return None
     _mark(stages, "green:norms")
+    hinted = sector is None and sector_hint is not None
+    if hinted:
+        sector = sector_hint  # used when it holds every start state (checked below)
     if sector is None:
         sector = Sector(eng, dop, restr, states[n2[run_of_row] > 0], precision)
     _mark(stages, "green:sector")
@@ -188,6 +233,9 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
     _mark(stages, "green:v0")
     dims = sector.run_dims(eng, rows[sel].clamp_min(0), lr[sel], int(live.size))
     dims_h = torch.cat([dims, missing.view(1).to(torch.int64)]).cpu().numpy()
+    if dims_h[-1] and hinted:
+        return green_setup(eng, dop, restr, run_states, run_amps, krylovSize, precision, None, normalize, scales,
+                           perturb, stages)
     if dims_h[-1]:
         raise RuntimeError("start state outside the sector basis")
     k_h = np.minimum(dims_h[:-1], int(krylovSize)).astype(np.int32)
@@ -252,11 +300,11 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
 
 def _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
                        sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
-                       perturb=None, stages=None):
+                       perturb=None, stages=None, sector_hint=None):
     """green_batch as a step generator: yields once, after the Lanczos launch."""
     omega = np.asarray(omega, dtype=np.float64)
     st = green_setup(eng, dop, restr, run_states, run_amps, krylovSize, precision, sector, normalize, scales,
-                     perturb, stages)
+                     perturb, stages, sector_hint)
     runs = len(run_states) if run_amps is not None else run_states[3]
     g = torch.zeros((runs, len(omega)), dtype=torch.complex128, device=eng.device)
     if st is None:
@@ -469,21 +517,23 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
 
 def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                 slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-                timing=None, capture=None, perturb=None, stages=None, batched=True):
+                timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None):
     """Device form of :func:`getRIXSmap`; returns gs [nE, n_in, n_out, n_wIn, n_wLoss] (device).
 
     ``batched=False`` runs upstream's call structure: one shifted solve per incoming energy
     and one final-state Green's function per (incoming energy, outgoing channel)."""
     return _drive(rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize,
                              slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov, timing, capture,
-                             perturb, stages, batched))
+                             perturb, stages, batched, final_sector))
 
 
 def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-               timing=None, capture=None, perturb=None, stages=None, batched=True):
+               timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None):
     """rixs_device as a step generator for :func:`run_concurrently` (yields after the launch
-    of the final-state Lanczos)."""
+    of the final-state Lanczos).  ``final_sector``: a sector from :func:`closed_sector` (the
+    ground-state sector) used for the final states when it holds them all, instead of
+    expanding their closure."""
     _mark(stages, "start")
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
@@ -591,7 +641,7 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     if batched:
         g = yield from _green_batch_steps(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
                                           normalize=False, scales=scales, timing=timing, capture=capture,
-                                          perturb=perturb, stages=stages)
+                                          perturb=perturb, stages=stages, sector_hint=final_sector)
     else:
         g = green_runs_one_by_one(eng, dop, restr, packed, None, e_runs, wLoss, delta2, krylovSize, precision,
                                   normalize=False, scales=scales)
@@ -606,7 +656,7 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
 
 def xas_rixs_device(eng, dop, restr, xas_dops, tin_dops, tout_dops, psi_t, es, w, delta, wIns, wLoss, delta1, delta2,
                     krylovSize=150, slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True,
-                    max_krylov=2000):
+                    max_krylov=2000, final_sector=None):
     """XAS (:func:`spectra_device`) and the RIXS map (:func:`rixs_device`) of the same
     eigenstates, computed side by side: the RIXS pipeline on the current stream, the XAS one
     on a side stream, so the XAS host work (operator application, sector build) runs while
@@ -614,7 +664,7 @@ def xas_rixs_device(eng, dop, restr, xas_dops, tin_dops, tout_dops, psi_t, es, w
     the other.  Returns (g_xas [n_states, n_ops, n_w], g_rixs) on the device."""
     g_rixs, g_xas = run_concurrently(eng, [
         rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize,
-                   slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov),
+                   slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov, final_sector=final_sector),
         spectra_steps(eng, dop, restr, xas_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision)])
     return g_xas, g_rixs
 

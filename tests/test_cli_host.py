@@ -6,6 +6,7 @@ import ast
 import pickle
 from collections import OrderedDict
 
+import numpy as np
 import pytest
 
 from impuritymodel_gb300 import get_spectra as G
@@ -56,3 +57,13 @@ def test_restricted_unpickler_refuses_other_objects(tmp_path):
         pickle.dump({"x": pytest.approx}, fh)
     with pytest.raises(pickle.UnpicklingError):
         G.read_pickled_file(str(bad))
+
+
+def test_popcount64_matches_python():
+    """The SWAR bit count used to check restrictions on host words."""
+    from impuritymodel_gb300.spectra import _popcount64
+
+    rng = np.random.default_rng(3)
+    x = rng.integers(0, 2**63, size=500, dtype=np.int64).astype(np.uint64) * np.uint64(2) + np.uint64(1)
+    x[:3] = [0, np.uint64(0xFFFFFFFFFFFFFFFF), np.uint64(1) << np.uint64(63)]
+    assert np.array_equal(_popcount64(x), [bin(int(v)).count("1") for v in x])

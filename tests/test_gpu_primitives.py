@@ -226,3 +226,41 @@ def test_reorth_double_float_matches_fp64(eng, config):
     gram = V @ V.conj().t()
     err = (gram - torch.eye(V.shape[0], dtype=gram.dtype, device=gram.device)).abs().max().item()
     assert err < 1e-12, err
+
+
+def test_closed_ground_sector_serves_green_functions(eng):
+    """The ground-state sector of the 66-orbital model is closed under the restricted H, so
+    Green's-function runs starting inside it can use it instead of a fresh expansion.  When
+    the runs' closure is the whole sector (random start states spread over it) the spectra
+    are bit-identical to the expanded ones; a start state outside it falls back to the
+    expansion."""
+    from impuritymodel_gb300 import finite, spectra
+    from impuritymodel_gb300.engine import make_restrictions
+
+    mod = M.make_model("config2")
+    n = mod.n_spin_orbitals
+    dop = finite._device_op(mod.hOp, eng)
+    restr = make_restrictions(mod.restrictions, n)
+    sb = finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n)
+    es, psi_t, h = finite.eigensystem_device(eng, dop, sb, 1, precision=3, with_hamiltonian=True)
+    sec = spectra.closed_sector(eng, dop, restr, sb.sorted, h, sb.words)
+    assert sec is not None and sec.n == sb.sorted.shape[0]
+    rng = np.random.default_rng(11)
+    run_states, run_amps = [], []
+    for r in range(4):
+        idx = torch.as_tensor(np.sort(rng.choice(sec.n, 300, replace=False)), device=eng.device)
+        run_states.append(sb.sorted[idx].contiguous())
+        run_amps.append(torch.as_tensor(rng.standard_normal((300, 2)), device=eng.device))
+    w = np.linspace(-5.0, 15.0, 200)
+    e_runs = [es[0]] * 4
+    st = spectra.green_setup(eng, dop, restr, run_states, run_amps, 150, 3)
+    assert st.sector.n == sec.n  # the expanded closure is the whole sector
+    g1 = spectra.green_batch(eng, dop, restr, run_states, run_amps, e_runs, w, 0.1, 150, 3)
+    g2 = spectra._drive(spectra._green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, 0.1, 150, 3,
+                                                   sector_hint=sec))
+    assert torch.equal(g1, g2)
+    # a start state outside the hinted sector: falls back to the expansion
+    small = spectra.Sector.from_parts(sb.sorted[:10].contiguous(), h)
+    g3 = spectra._drive(spectra._green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, 0.1, 150, 3,
+                                                   sector_hint=small))
+    assert torch.equal(g1, g3)
