@@ -724,12 +724,14 @@ class Engine:
             j1, ev = jn, ev_next
         return (_df_to_c128(V[:j]) if df else V[:j]), ah[:j], bh[:j]
 
-    def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0):
+    def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0, check=True):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).
 
         ``precision=3`` runs the Krylov recurrence in double-float arithmetic when H is real
         (complex H stays FP64).  Returns (X [R, nz, N] complex128, krylov sizes [R]) or None
-        when the sector or the shift count exceeds the single-CTA kernel's limits."""
+        when the sector or the shift count exceeds the single-CTA kernel's limits.  With
+        ``check=False`` the work is only enqueued and a third value, a function that reads the
+        status (on the same stream), is returned."""
         r, n = Y.shape
         nz = zs.shape[1]
         k_cap = int(k_cap)
@@ -747,12 +749,19 @@ class Engine:
         L.check(solve(C.byref(csr.struct()), _ptr(torch.view_as_real(Y.contiguous())), r, _ptr(torch.view_as_real(zt)),
                       nz, k_cap, float(tol), _ptr(torch.view_as_real(X)), _ptr(m), _ptr(self.status), ws, wsn,
                       self.stream), "shifted_solve")
-        st = int(self.status.item())
-        if st == L.EDGPU_ERR_NOCONV:
-            # upstream only prints when BiCGSTAB misses its tolerance (spectra.py:963-971)
-            warnings.warn("shifted solve: residual tolerance %g not reached in %d Krylov steps" % (tol, k_cap))
-        elif st != L.EDGPU_OK:
-            raise L.EdgpuError(st, "shifted_solve")
+        status = self.status
+
+        def finish():
+            st = int(status.item())
+            if st == L.EDGPU_ERR_NOCONV:
+                # upstream only prints when BiCGSTAB misses its tolerance (spectra.py:963-971)
+                warnings.warn("shifted solve: residual tolerance %g not reached in %d Krylov steps" % (tol, k_cap))
+            elif st != L.EDGPU_OK:
+                raise L.EdgpuError(st, "shifted_solve")
+
+        if not check:
+            return X, m, finish
+        finish()
         return X, m
 
     def combine(self, V, coeffs):

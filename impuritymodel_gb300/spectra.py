@@ -555,13 +555,15 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
     _mark(stages, "rixs:core_sector")
     # 3. outgoing operators as sparse maps core basis -> output states
-    out_maps = []
-    for k in range(nout):
-        if share_out_memo and k > 0:
-            out_maps.append(out_maps[0])
-            continue
-        out_maps.append(_transfer_matrix(eng, tout_dops[0] if share_out_memo else tout_dops[k], restr, core.basis))
-    _mark(stages, "rixs:transfer")
+    def build_out_maps():
+        maps = []
+        for k in range(nout):
+            if share_out_memo and k > 0:
+                maps.append(maps[0])
+                continue
+            maps.append(_transfer_matrix(eng, tout_dops[0] if share_out_memo else tout_dops[k], restr, core.basis))
+        return maps
+
     # 4. shifted solves x(z) = (z - H)^{-1} psi1 for every incoming energy and every
     # (t_in, eigenstate) right-hand side
     keys = [k for k, (s1, _) in psi1.items() if s1.shape[0]]
@@ -576,8 +578,24 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     # without reorthogonalisation the recurrence may need a few times the sector dimension
     k_solve = min(6 * core.n + 50, max_krylov)
     if batched:
-        solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve, precision)
+        # the outgoing maps are built on a side stream while the solves (one CTA per
+        # right-hand side, most SMs idle) run; the side stream waits only for the core basis
+        main = torch.cuda.current_stream(eng.device)
+        ready = main.record_event()
+        solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve, precision, check=False)
+        side = eng.side_stream(1)
+        side.wait_event(ready)
+        with torch.cuda.stream(side):
+            out_maps = build_out_maps()
+        main.wait_stream(side)
+        for tm in set(out_maps):
+            tm.record_stream(main)
+        _mark(stages, "rixs:transfer")
+        if solved is not None:
+            solved[2]()
     else:
+        out_maps = build_out_maps()
+        _mark(stages, "rixs:transfer")
         solved = None
         blocks = []
         for r in range(len(keys)):
@@ -675,6 +693,12 @@ class _TransferMatrix:
     def __init__(self, out_states, csr):
         self.out_states = out_states
         self.csr = csr
+
+    def record_stream(self, stream):
+        """Mark the tensors as used on ``stream`` (they were made on another one)."""
+        for x in (self.out_states, self.csr.row_ptr, self.csr.col, self.csr.val_c, self.csr.val_r):
+            if x is not None:
+                x.record_stream(stream)
 
     def apply(self, eng, X):
         """P[m] = T X[m] for rows m of X [M, Nc]; returns [M, n_out] complex128."""
