@@ -368,8 +368,10 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
   const size_t term_bytes = (28 * (size_t)p.n_terms + 15) & ~(size_t)15;
   const size_t per_warp =
       (((size_t)p.cap * (20 + 8 * (size_t)n_words) + 8 * (size_t)((p.n_terms + 31) / 32)) + 15) & ~(size_t)15;
+  // four warps (one state each) per block: ~70 KB of shared memory for a 1200-term operator,
+  // so a block also fits beside two CTAs of a Lanczos kernel running on another stream
   const size_t smem_max = 220 * 1024;
-  int warps = 8;
+  int warps = 4;
   p.stage_terms = 1;
   while (warps > 1 && term_bytes + per_warp * warps > smem_max) warps >>= 1;
   if (term_bytes + per_warp * warps > smem_max) {

@@ -1213,6 +1213,12 @@ int launch_small(const edgpu_csr* h, const T* vals, const double* v0, int R, con
 
 // 256-thread CTAs when three or more fit on an SM (measured on the 1770-row RIXS final-state
 // sector with 750 runs: 256 x 3-4 per SM 6.9 ms against 7.4 ms for 512 x 2), else 512.
+// CTA slots per SM that the one-CTA-per-run double-float Lanczos leaves free (process-wide,
+// default 0), so that kernels of a pipeline running concurrently on another stream find room
+// on every SM instead of waiting for the persistent grid to drain.
+static std::atomic<int> g_small_reserve{0};
+extern "C" void edgpu_set_small_reserve(int slots) { g_small_reserve.store(slots > 0 ? slots : 0); }
+
 int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
                     double* beta, int32_t* status, cudaStream_t s) {
   const size_t smem = small_smem_bytes(h->n, 3);
@@ -1229,6 +1235,7 @@ int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* 
     threads = 512;
     kern = k512;
   }
+  per_sm -= g_small_reserve.load();
   if (per_sm < 1) per_sm = 1;
   int grid = grid_cap() * per_sm;
   if (grid > R) grid = R;

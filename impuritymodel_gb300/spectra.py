@@ -269,14 +269,21 @@ def run_concurrently(eng, jobs):
         s.wait_stream(main)
     results = [None] * len(jobs)
     pending = list(range(len(jobs)))
-    while pending:
-        for k in list(pending):
-            with torch.cuda.stream(streams[k]):
-                try:
-                    next(jobs[k])
-                except StopIteration as done:
-                    results[k] = done.value
-                    pending.remove(k)
+    # the persistent one-CTA-per-run Lanczos leaves a CTA slot per SM to the other jobs
+    if len(jobs) > 1:
+        eng.lib.edgpu_set_small_reserve(1)
+    try:
+        while pending:
+            for k in list(pending):
+                with torch.cuda.stream(streams[k]):
+                    try:
+                        next(jobs[k])
+                    except StopIteration as done:
+                        results[k] = done.value
+                        pending.remove(k)
+    finally:
+        if len(jobs) > 1:
+            eng.lib.edgpu_set_small_reserve(0)
     for s in streams[1:]:
         main.wait_stream(s)
     for k, r in enumerate(results):

@@ -267,6 +267,10 @@ int edgpu_lanczos_reorth(const edgpu_csr* h, const double* v0, int j0, int j1, i
 int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int j0, int j1, int K_cap, double* V, double* w,
                             double* alpha, double* beta, int32_t* status_dev, void* workspace, size_t workspace_bytes,
                             void* stream);
+/* Process-wide launch policy (default 0): CTA slots per SM that the double-float
+ * one-CTA-per-run Lanczos of edgpu_lanczos (precision 3, small sectors) leaves free, so that
+ * work on another stream can run beside it.  No counterpart in upstream impurityModel. */
+void edgpu_set_small_reserve(int slots);
 /* Process-wide switch (default 1): 0 sends every edgpu_lanczos_reorth call to the
  * per-step kernels (both paths compute the same recurrence; used to test one against the
  * other).  No counterpart in upstream impurityModel. */
