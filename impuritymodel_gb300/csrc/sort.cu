@@ -303,6 +303,78 @@ extern "C" int edgpu_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* 
   return scan_rec(in, out, n, reinterpret_cast<int64_t*>(workspace), s);
 }
 
+// ---------------------------------------------------------------------------------------
+// Small inputs: one CTA sorts (key, original position) pairs in shared memory with a bitonic
+// network (a total order, so the result is the stable sort), one launch instead of a
+// histogram, scan and scatter launch per varying key byte.
+// ---------------------------------------------------------------------------------------
+constexpr int kSmallSortThreads = 1024;
+constexpr size_t kSmallSortBytes = 160 * 1024;
+
+inline int small_sort_pow2(int64_t n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+inline bool small_sort_fits(int n_words, int64_t n) {
+  return n <= 8192 && (size_t)small_sort_pow2(n) * (8 * (size_t)n_words + 4) <= kSmallSortBytes;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kSmallSortThreads) small_sort_kernel(uint64_t* keys, uint32_t* payload, int n, int N) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint64_t* k = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* idx = reinterpret_cast<uint32_t*>(k + (size_t)N * W);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) k[(size_t)i * W + q] = i < n ? keys[(size_t)i * W + q] : ~0ull;
+    idx[i] = (uint32_t)i;  // padding sorts last: all-ones keys, positions >= n
+  }
+  __syncthreads();
+  for (int size = 2; size <= N; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < (N >> 1); t += blockDim.x) {
+        const int lo = 2 * t - (t & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        int c = 0;
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+          if (c == 0) {
+            const uint64_t a = k[(size_t)lo * W + q], b = k[(size_t)hi * W + q];
+            c = a < b ? -1 : (a > b ? 1 : 0);
+          }
+        }
+        if (c == 0) c = idx[lo] < idx[hi] ? -1 : 1;
+        if ((c > 0) == up) {
+#pragma unroll
+          for (int q = 0; q < W; ++q) {
+            const uint64_t tmp = k[(size_t)lo * W + q];
+            k[(size_t)lo * W + q] = k[(size_t)hi * W + q];
+            k[(size_t)hi * W + q] = tmp;
+          }
+          const uint32_t ti = idx[lo];
+          idx[lo] = idx[hi];
+          idx[hi] = ti;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // payloads follow their keys: read every original payload before any write
+  uint32_t pv[(8192 + kSmallSortThreads - 1) / kSmallSortThreads];
+  int u = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) pv[u++] = payload[idx[i]];
+  __syncthreads();
+  u = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) keys[(size_t)i * W + q] = k[(size_t)i * W + q];
+    payload[i] = pv[u++];
+  }
+}
+
 extern "C" size_t edgpu_sort_states_workspace(int n_words, int64_t n) {
   const int64_t nb = (n + kSortTile - 1) / kSortTile;
   const int64_t hist = 256 * (nb > 0 ? nb : 1);
@@ -332,8 +404,17 @@ extern "C" int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload,
   if (n_words < 1 || n_words > EDGPU_MAX_WORDS || n < 0) return EDGPU_ERR_ARG;
   if (n <= 1) return EDGPU_OK;
   if (!keys || !payload) return EDGPU_ERR_ARG;
-  if (workspace_bytes < edgpu_sort_states_workspace(n_words, n)) return EDGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
+  if (small_sort_fits(n_words, n)) {
+    const int N = small_sort_pow2(n);
+    const size_t smem = (size_t)N * (8 * (size_t)n_words + 4);
+    EDGPU_DISPATCH_W(n_words, {
+      cudaFuncSetAttribute(small_sort_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      small_sort_kernel<W><<<1, kSmallSortThreads, smem, s>>>(keys, payload, (int)n, N); note_launch();
+    });
+    return check_launch();
+  }
+  if (workspace_bytes < edgpu_sort_states_workspace(n_words, n)) return EDGPU_ERR_WORKSPACE;
   const int64_t nb = (n + kSortTile - 1) / kSortTile;
   const int64_t hist_n = 256 * nb;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);

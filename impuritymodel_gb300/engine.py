@@ -285,6 +285,11 @@ class Engine:
         m, w = keys.shape
         if m <= 1:
             return keys, payload
+        if m <= 8192 and (1 << (m - 1).bit_length()) * (8 * w + 4) <= 160 * 1024:
+            # one-CTA bitonic sort in the library: no byte-variation pass and no host read
+            L.check(self.lib.edgpu_sort_states(w, _ptr(keys), _ptr(payload), m, None, C.c_void_p(0), 0,
+                                               self.stream), "sort")
+            return keys, payload
         vary = torch.empty(w, dtype=torch.int64, device=self.device)
         L.check(self.lib.edgpu_vary_mask(w, _ptr(keys), m, _ptr(vary), self.stream), "vary_mask")
         vm = vary.cpu().numpy().view(np.uint64).copy()

@@ -130,7 +130,9 @@ int edgpu_apply_vector(int n_words, const uint64_t* states, const double* amps, 
  * ``sorted(...)`` of upstream ``expand_basis`` (finite.py:1793) and the dict merging of
  * ``applyOp``.  keys/payload are sorted in place (results written back to the inputs).
  * vary_mask: OR over keys of (key XOR first key), n_words host words (NULL = all bits);
- * digits where it is zero are skipped.
+ * digits where it is zero are skipped.  Inputs with n <= 8192 and
+ * next_pow2(n) * (8 n_words + 4) <= 160 KiB are sorted by one CTA in shared memory (bitonic
+ * network over (key, position), the same stable order) and need no workspace.
  */
 size_t edgpu_sort_states_workspace(int n_words, int64_t n);
 int edgpu_sort_states(int n_words, uint64_t* keys, uint32_t* payload, int64_t n, const uint64_t* vary_mask,

@@ -264,3 +264,18 @@ def test_closed_ground_sector_serves_green_functions(eng):
     g3 = spectra._drive(spectra._green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, 0.1, 150, 3,
                                                    sector_hint=small))
     assert torch.equal(g1, g3)
+
+
+@pytest.mark.parametrize("w,n", [(1, 2), (2, 300), (3, 4097), (2, 8192), (8, 1500)])
+def test_small_sort_is_stable(eng, w, n):
+    """The one-CTA bitonic path sorts like the stable radix sort: keys with many duplicates,
+    payloads in their original relative order within equal keys."""
+    rng = np.random.default_rng(n + w)
+    pool = _rand_states(rng, max(2, n // 7), 64 * w - 5, 5)
+    keys = pool[rng.integers(0, pool.shape[0], size=n)]
+    kt = eng.upload_states(keys)
+    pay = torch.arange(n, dtype=torch.int32, device=eng.device)
+    eng.sort_states(kt, pay)
+    order = np.lexsort([keys[:, q] for q in range(w - 1, -1, -1)])  # stable
+    assert np.array_equal(eng.download_states(kt), keys[order])
+    assert np.array_equal(pay.cpu().numpy(), order.astype(np.int32))
