@@ -65,7 +65,7 @@ def psi_to_arrays(psi, n_spin_orbitals):
     """dict {bytes: amplitude} -> (uint64[N, W], float64[N, 2])."""
     states = list(psi.keys())
     words = bytes_to_words(states, n_spin_orbitals)
-    amps = np.array([complex(psi[s]) for s in states], dtype=np.complex128)
+    amps = np.fromiter(psi.values(), dtype=np.complex128, count=len(states))
     return words, np.ascontiguousarray(amps.view(np.float64).reshape(-1, 2))
 
 

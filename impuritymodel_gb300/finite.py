@@ -591,10 +591,10 @@ def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", 
         vecs = eng.to_host(vecs_t)
     else:
         raise ValueError("Wrong diagonalization mode")
-    psis = [
-        {basis[i]: vecs[i, vi] for i in np.nonzero(np.abs(vecs[:, vi]) ** 2 >= slaterWeightMin)[0]}
-        for vi in range(len(es))
-    ]
+    psis = []
+    for vi in range(len(es)):
+        idx = np.nonzero(np.abs(vecs[:, vi]) ** 2 >= slaterWeightMin)[0]
+        psis.append(dict(zip([basis[i] for i in idx], vecs[idx, vi])))
     return np.asarray(es), psis
 
 # 3d-shell observables under upstream's names (finite.py:121-174, 843-1298)
