@@ -127,3 +127,88 @@ __device__ __forceinline__ dfl df_rcp(dfl b) {
 }
 
 }  // namespace edgpu
+
+namespace edgpu {
+
+// ---------------------------------------------------------------------------------------
+// Two independent double-floats (the real and imaginary parts of a complex number) in packed
+// float2 registers.  GB300's packed FP32 instructions (__fadd2_rn / __fmul2_rn / __ffma2_rn,
+// per component the same as __fadd_rn / __fmul_rn / __fmaf_rn) carry both in one issue, so
+// each operation below is its scalar counterpart, component by component, at half the
+// instruction count.
+// ---------------------------------------------------------------------------------------
+struct dfl2 {
+  float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2dup(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ dfl2 df2_fast_two_sum(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  return {s, __fadd2_rn(b, f2neg(__fadd2_rn(s, f2neg(a))))};
+}
+
+__device__ __forceinline__ dfl2 df2_two_sum(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, f2neg(a));
+  return {s, __fadd2_rn(__fadd2_rn(a, f2neg(__fadd2_rn(s, f2neg(bb)))), __fadd2_rn(b, f2neg(bb)))};
+}
+
+// acc + a * b, b the same double-float for both components
+__device__ __forceinline__ dfl2 df2_fma_s(dfl2 acc, dfl2 a, dfl b) {
+  const float2 bh = f2dup(b.hi), bl = f2dup(b.lo);
+  const float2 p = __fmul2_rn(a.hi, bh);
+  float2 pe = __ffma2_rn(a.hi, bh, f2neg(p));
+  pe = __ffma2_rn(a.hi, bl, pe);
+  pe = __ffma2_rn(a.lo, bh, pe);
+  const dfl2 s = df2_two_sum(acc.hi, p);
+  return df2_fast_two_sum(s.hi, __fadd2_rn(__fadd2_rn(s.lo, pe), acc.lo));
+}
+
+__device__ __forceinline__ dfl2 df2_mul_s(dfl2 a, dfl b) {
+  const float2 bh = f2dup(b.hi), bl = f2dup(b.lo);
+  const float2 p = __fmul2_rn(a.hi, bh);
+  float2 e = __ffma2_rn(a.hi, bh, f2neg(p));
+  e = __ffma2_rn(a.hi, bl, e);
+  e = __ffma2_rn(a.lo, bh, e);
+  return df2_fast_two_sum(p, e);
+}
+
+// Packed running sums (s + c per component, as dacc)
+struct dacc2 {
+  float2 s, c;
+};
+
+// a += h * x, h the same double-float for both components, x = (xh + xl) per component
+__device__ __forceinline__ void dacc2_fma(dacc2& a, dfl h, float2 xh, float2 xl) {
+  const float2 hh = f2dup(h.hi), hl = f2dup(h.lo);
+  const float2 p = __fmul2_rn(hh, xh);
+  float2 pe = __ffma2_rn(hh, xh, f2neg(p));
+  pe = __ffma2_rn(hh, xl, pe);
+  pe = __ffma2_rn(hl, xh, pe);
+  const dfl2 t = df2_two_sum(a.s, p);
+  a.s = t.hi;
+  a.c = __fadd2_rn(a.c, __fadd2_rn(t.lo, pe));
+}
+
+// a += h * x componentwise (h a pair)
+__device__ __forceinline__ void dacc2_fma2(dacc2& a, dfl2 h, float2 xh, float2 xl) {
+  const float2 p = __fmul2_rn(h.hi, xh);
+  float2 pe = __ffma2_rn(h.hi, xh, f2neg(p));
+  pe = __ffma2_rn(h.hi, xl, pe);
+  pe = __ffma2_rn(h.lo, xh, pe);
+  const dfl2 t = df2_two_sum(a.s, p);
+  a.s = t.hi;
+  a.c = __fadd2_rn(a.c, __fadd2_rn(t.lo, pe));
+}
+
+__device__ __forceinline__ dfl2 dacc2_val(dacc2 a) { return df2_two_sum(a.s, a.c); }
+
+// sum of the two components of a packed running sum, as one double-float
+__device__ __forceinline__ dfl dacc2_total(dacc2 a) {
+  const dfl2 v = dacc2_val(a);
+  return df_add({v.hi.x, v.lo.x}, {v.hi.y, v.lo.y});
+}
+
+}  // namespace edgpu

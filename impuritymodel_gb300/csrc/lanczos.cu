@@ -1096,6 +1096,8 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv, int R,
     const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
     double* __restrict__ beta, int32_t* status) {
+  // vectors in shared memory as float4 (re.hi, im.hi, re.lo, im.lo): .xy and .zw are the
+  // packed high and low parts that the float2 instructions take directly
   extern __shared__ __align__(16) unsigned char sm[];
   float4* A = reinterpret_cast<float4*>(sm);
   float4* B = A + n;
@@ -1111,7 +1113,7 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     for (int64_t i = tid; i < n; i += THREADS) {
       const double2 v = v0[i * R + r];
       const dfl re = df_split(v.x), im = df_split(v.y);
-      A[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      A[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
       B[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
@@ -1120,9 +1122,9 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     dfl bprev = zero;
     for (int j = 0; j < km; ++j) {
       const dfl nb = {-bprev.hi, -bprev.lo};
-      dacc acc = {0.f, 0.f};
+      dacc2 acc = {{0.f, 0.f}, {0.f, 0.f}};
       for (int64_t i = tid; i < n; i += THREADS) {
-        dacc yr = {0.f, 0.f}, yi = {0.f, 0.f};
+        dacc2 y = {{0.f, 0.f}, {0.f, 0.f}};
         const int e1 = srp[i + 1];
         for (int e = srp[i]; e < e1; e += kSmallBatch) {
           int c[kSmallBatch];
@@ -1136,34 +1138,30 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
 #pragma unroll
           for (int u = 0; u < kSmallBatch; ++u) {
             if (e + u < e1) {
-              const dfl h = {hh[u].x, hh[u].y};
               const float4 xv = x[c[u]];
-              dacc_fma(yr, h, xv.x, xv.y);
-              dacc_fma(yi, h, xv.z, xv.w);
+              dacc2_fma(y, {hh[u].x, hh[u].y}, make_float2(xv.x, xv.y), make_float2(xv.z, xv.w));
             }
           }
         }
-        const dfl hr = dacc_val(yr), hi = dacc_val(yi);
+        const dfl2 h = dacc2_val(y);
         const float4 xi = x[i], pi = p[i];
-        dacc_fma(acc, hr, xi.x, xi.y);
-        dacc_fma(acc, hi, xi.z, xi.w);
-        const dfl wr = df_fma(hr, nb, {pi.x, pi.y}), wi = df_fma(hi, nb, {pi.z, pi.w});
-        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+        dacc2_fma2(acc, h, make_float2(xi.x, xi.y), make_float2(xi.z, xi.w));
+        const dfl2 w = df2_fma_s(h, {make_float2(pi.x, pi.y), make_float2(pi.z, pi.w)}, nb);
+        p[i] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
       }
-      const dfl a = df_block_sum2<NW>(dacc_val(acc), red);
+      const dfl a = df_block_sum2<NW>(dacc2_total(acc), red);
       if (tid == THREADS - 1) alpha[(int64_t)r * K + j] = df_val(a);
       if (j + 1 == km) break;
       const dfl na = {-a.hi, -a.lo};
-      acc = {0.f, 0.f};
+      acc = {{0.f, 0.f}, {0.f, 0.f}};
       for (int64_t i = tid; i < n; i += THREADS) {
-        const float4 w = p[i], xi = x[i];
-        const dfl wr = df_fma({w.x, w.y}, na, {xi.x, xi.y});
-        const dfl wi = df_fma({w.z, w.w}, na, {xi.z, xi.w});
-        p[i] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
-        dacc_fma(acc, wr, wr.hi, wr.lo);
-        dacc_fma(acc, wi, wi.hi, wi.lo);
+        const float4 wv = p[i], xi = x[i];
+        const dfl2 w = df2_fma_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)},
+                                 {make_float2(xi.x, xi.y), make_float2(xi.z, xi.w)}, na);
+        p[i] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
+        dacc2_fma2(acc, w, w.hi, w.lo);
       }
-      bprev = df_sqrt(df_block_sum2<NW>(dacc_val(acc), red + 40));
+      bprev = df_sqrt(df_block_sum2<NW>(dacc2_total(acc), red + 40));
       const dfl ib = bprev.hi > 0.f ? df_rcp(bprev) : zero;
       if (tid == THREADS - 1) {
         const double b = df_val(bprev);
@@ -1171,9 +1169,9 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
       }
       for (int64_t i = tid; i < n; i += THREADS) {
-        const float4 w = p[i];
-        const dfl vr = df_mul({w.x, w.y}, ib), vi = df_mul({w.z, w.w}, ib);
-        p[i] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
+        const float4 wv = p[i];
+        const dfl2 v = df2_mul_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)}, ib);
+        p[i] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
       }
       __syncthreads();
       float4* t = p;
