@@ -303,6 +303,8 @@ extern "C" int edgpu_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* 
   return scan_rec(in, out, n, reinterpret_cast<int64_t*>(workspace), s);
 }
 
+namespace edgpu {
+
 // ---------------------------------------------------------------------------------------
 // Small inputs: one CTA sorts (key, original position) pairs in shared memory with a bitonic
 // network (a total order, so the result is the stable sort), one launch instead of a
@@ -374,6 +376,8 @@ __global__ void __launch_bounds__(kSmallSortThreads) small_sort_kernel(uint64_t*
     payload[i] = pv[u++];
   }
 }
+
+}  // namespace edgpu
 
 extern "C" size_t edgpu_sort_states_workspace(int n_words, int64_t n) {
   const int64_t nb = (n + kSortTile - 1) / kSortTile;
