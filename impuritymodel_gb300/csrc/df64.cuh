@@ -65,6 +65,13 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
 // partials that a slower thread may still be reading from the previous one (every thread
 // reads the previous result before it reaches the next sum's first barrier).
 constexpr int kDfRed = 80;  // two 40-entry partial buffers
+// first shuffle distance of a tree over NW partials: half the next power of two, so that a
+// warp count that is not a power of two (5 or 6 warps) still adds every partial
+__host__ __device__ constexpr int df_tree_top(int nw) {
+  int p = 1;
+  while (p < nw) p <<= 1;
+  return p / 2;
+}
 template <int NW>
 __device__ __forceinline__ dfl df_block_sum2(dfl v, dfl* buf) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -76,7 +83,7 @@ __device__ __forceinline__ dfl df_block_sum2(dfl v, dfl* buf) {
   if (warp == 0) {
     dfl t = lane < NW ? buf[lane] : dfl{0.f, 0.f};
 #pragma unroll
-    for (int o = NW / 2; o > 0; o >>= 1)
+    for (int o = df_tree_top(NW); o > 0; o >>= 1)
       t = df_add(t, {__shfl_down_sync(0xffffffffu, t.hi, o), __shfl_down_sync(0xffffffffu, t.lo, o)});
     if (lane == 0) buf[32] = t;
   }

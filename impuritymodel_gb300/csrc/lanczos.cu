@@ -468,7 +468,7 @@ __global__ void cfrac_kernel(const double* __restrict__ alpha, const double* __r
 
 bool small_fits(int64_t n, int precision);
 int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
-                  double* alpha, double* beta, int32_t* status, cudaStream_t s);
+                  double* alpha, double* beta, int32_t* status, void* ws, cudaStream_t s);
 
 // Mixed form: a'[r][i] = float(alpha - e_r), b2[r][i] = float(beta^2) (FP64 subtraction
 // first, so the large common energy cancels exactly), then the fraction in float32.
@@ -791,7 +791,7 @@ extern "C" int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const 
   if (workspace_bytes < edgpu_lanczos_workspace(h->n, R, K, precision)) return EDGPU_ERR_WORKSPACE;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
   if (small_fits(h->n, precision))
-    return lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, (cudaStream_t)stream);
+    return lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, ws, (cudaStream_t)stream);
   if (precision == 0)
     return lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, workspace_bytes,
                                 (cudaStream_t)stream);
@@ -813,7 +813,7 @@ extern "C" int edgpu_lanczos_timed(const edgpu_csr* h, const double* v0, int R, 
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int rc = lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, s);
+    int rc = lanczos_small(h, v0, R, k_max, K, precision, alpha, beta, status_dev, ws, s);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -1081,28 +1081,33 @@ __global__ void __launch_bounds__(kSmallThreads) lanczos_small_kernel(
   }
 }
 
-// The double-float recurrence with two vectors per run instead of three: the H v_j pass
-// reads x = v_j anywhere but p = v_{j-1} only at its own rows, so it overwrites p in place
-// with H v_j - beta_{j-1} v_{j-1} while summing alpha_j = v_j . H v_j from the same row
-// values; the second pass subtracts alpha_j v_j, the third normalises, and the buffers swap.
-// (The subtractions run in the order (H v - beta p) - alpha v instead of upstream's
-// (H v - alpha v) - beta p, a difference at the 2^-48 rounding level.)  Two vectors of
-// 16 bytes per row leave room for three or four CTAs per SM.  Every thread forms beta and
-// 1/beta itself from the broadcast sum (double-float square root and reciprocal, a few
-// FP32 instructions), so no barrier publishes them; the last thread, which has the fewest
-// rows, converts alpha and beta to FP64 for the outputs.
+// The double-float recurrence with one shared-memory vector per run.  The H v_j pass
+// gathers x = v_j from anywhere in the sector, but every other access to a vector touches
+// only the thread's own rows (i = tid, tid + THREADS, ...), so v_{j-1} lives in a per-CTA
+// slice of global memory (the Lanczos workspace; each element is read and written only by
+// the thread that owns its row, so no fence is needed) and only x occupies shared memory.
+// Pass 1 overwrites p = v_{j-1} with H v_j - beta_{j-1} v_{j-1} while summing
+// alpha_j = v_j . H v_j from the same row values; pass 2, after the SpMV of every thread
+// has finished (the alpha sum's barriers), forms w = p - alpha_j v_j, moves v_j into p and
+// w into x; pass 3 normalises x in place.  (The subtractions run in the order
+// (H v - beta p) - alpha v instead of upstream's (H v - alpha v) - beta p, a difference at
+// the 2^-48 rounding level.)  At 16 + 4 bytes per row of shared memory (vector and cached
+// row pointers) five or six CTAs fit on an SM, so a batch of runs the size of a RIXS map
+// (hundreds of runs) runs as one wave.  Every thread forms beta and 1/beta itself from the
+// broadcast sum (double-float square root and reciprocal, a few FP32 instructions), so no
+// barrier publishes them; the last thread converts alpha and beta to FP64 for the outputs.
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const float2* __restrict__ hv, int R,
     const double2* __restrict__ v0, const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha,
-    double* __restrict__ beta, int32_t* status) {
-  // vectors in shared memory as float4 (re.hi, im.hi, re.lo, im.lo): .xy and .zw are the
-  // packed high and low parts that the float2 instructions take directly
+    double* __restrict__ beta, int32_t* status, float4* __restrict__ pbuf) {
+  // vectors as float4 (re.hi, im.hi, re.lo, im.lo): .xy and .zw are the packed high and
+  // low parts that the float2 instructions take directly
   extern __shared__ __align__(16) unsigned char sm[];
-  float4* A = reinterpret_cast<float4*>(sm);
-  float4* B = A + n;
-  dfl* red = reinterpret_cast<dfl*>(B + n);                // two reduction buffers
+  float4* x = reinterpret_cast<float4*>(sm);
+  dfl* red = reinterpret_cast<dfl*>(x + n);                // two reduction buffers
   int32_t* srp = reinterpret_cast<int32_t*>(red + kDfRed);  // row pointers, cached once
+  float4* __restrict__ p = pbuf + (size_t)blockIdx.x * (size_t)n;
   constexpr int NW = THREADS / 32;
   const int tid = threadIdx.x;
   const dfl zero = {0.f, 0.f};
@@ -1113,17 +1118,16 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
     for (int64_t i = tid; i < n; i += THREADS) {
       const double2 v = v0[i * R + r];
       const dfl re = df_split(v.x), im = df_split(v.y);
-      A[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
-      B[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      x[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
+      p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
-    float4* x = A;
-    float4* p = B;
     dfl bprev = zero;
     for (int j = 0; j < km; ++j) {
       const dfl nb = {-bprev.hi, -bprev.lo};
       dacc2 acc = {{0.f, 0.f}, {0.f, 0.f}};
       for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 pi = p[i];  // issued before the row's products, used after them
         dacc2 y = {{0.f, 0.f}, {0.f, 0.f}};
         const int e1 = srp[i + 1];
         for (int e = srp[i]; e < e1; e += kSmallBatch) {
@@ -1144,7 +1148,7 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
           }
         }
         const dfl2 h = dacc2_val(y);
-        const float4 xi = x[i], pi = p[i];
+        const float4 xi = x[i];
         dacc2_fma2(acc, h, make_float2(xi.x, xi.y), make_float2(xi.z, xi.w));
         const dfl2 w = df2_fma_s(h, {make_float2(pi.x, pi.y), make_float2(pi.z, pi.w)}, nb);
         p[i] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
@@ -1158,7 +1162,8 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
         const float4 wv = p[i], xi = x[i];
         const dfl2 w = df2_fma_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)},
                                  {make_float2(xi.x, xi.y), make_float2(xi.z, xi.w)}, na);
-        p[i] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
+        p[i] = xi;  // v_j: the next step's v_{j-1}
+        x[i] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
         dacc2_fma2(acc, w, w.hi, w.lo);
       }
       bprev = df_sqrt(df_block_sum2<NW>(dacc2_total(acc), red + 40));
@@ -1169,25 +1174,28 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
       }
       for (int64_t i = tid; i < n; i += THREADS) {
-        const float4 wv = p[i];
+        const float4 wv = x[i];
         const dfl2 v = df2_mul_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)}, ib);
-        p[i] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
+        x[i] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
       }
       __syncthreads();
-      float4* t = p;
-      p = x;
-      x = t;
     }
     __syncthreads();
   }
 }
 
+// Shared memory that decides whether a sector takes the one-CTA-per-run path (unchanged by
+// the one-vector form of the double-float kernel, so that the same sectors take it).
 size_t small_smem_bytes(int64_t n, int precision) {
-  // df64: two float4 vectors and the cached row pointers; otherwise three vectors
   if (precision == 3)
     return 2 * sizeof(float4) * (size_t)n + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(n + 1) + 16;
   const size_t v = precision == 1 ? sizeof(float2) : sizeof(double2);
   return 3 * v * (size_t)n + 68 * sizeof(double) + 16;
+}
+
+// Shared memory of one lanczos_small_df_kernel CTA: x, the reduction buffers, row pointers.
+static size_t small_df_smem_bytes(int64_t n) {
+  return sizeof(float4) * (size_t)n + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(n + 1) + 16;
 }
 
 bool small_fits(int64_t n, int precision) { return small_smem_bytes(n, precision) <= 200 * 1024; }
@@ -1209,44 +1217,60 @@ int launch_small(const edgpu_csr* h, const T* vals, const double* v0, int R, con
   return check_launch();
 }
 
-// 256-thread CTAs when three or more fit on an SM (measured on the 1770-row RIXS final-state
-// sector with 750 runs: 256 x 3-4 per SM 6.9 ms against 7.4 ms for 512 x 2), else 512.
 // CTA slots per SM that the one-CTA-per-run double-float Lanczos leaves free (process-wide,
 // default 0), so that kernels of a pipeline running concurrently on another stream find room
 // on every SM instead of waiting for the persistent grid to drain.
 static std::atomic<int> g_small_reserve{0};
 extern "C" void edgpu_set_small_reserve(int slots) { g_small_reserve.store(slots > 0 ? slots : 0); }
 
+// CTA size: the largest of 512, 256, 192, 160 and 128 threads (64 registers a thread at the
+// occupancy each is compiled for) whose CTAs cover the R runs in the fewest waves with one
+// slot per SM kept back.  It depends only on (n, R) and the GPU, never on the reserve, so a
+// run's reduction order, and its result bits, do not change with concurrent work; the
+// reserve only limits how many of the CTAs are resident at once.  On the 1770-row RIXS
+// final-state sector with 750 runs this is 160 threads, five CTAs per SM, one wave.
 int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
-                    double* beta, int32_t* status, cudaStream_t s) {
-  const size_t smem = small_smem_bytes(h->n, 3);
-  auto k256 = lanczos_small_df_kernel<256, 4>;
-  auto k512 = lanczos_small_df_kernel<512, 2>;
-  cudaFuncSetAttribute(k256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k256, 256, smem);
-  int threads = 256;
-  auto kern = k256;
-  if (per_sm < 3) {
-    cudaFuncSetAttribute(k512, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k512, 512, smem);
-    threads = 512;
-    kern = k512;
+                    double* beta, int32_t* status, void* ws, cudaStream_t s) {
+  using Kern = void (*)(int64_t, const int64_t*, const int32_t*, const float2*, int, const double2*, const int32_t*,
+                        int, double*, double*, int32_t*, float4*);
+  static const Kern kerns[5] = {lanczos_small_df_kernel<512, 2>, lanczos_small_df_kernel<256, 4>,
+                                lanczos_small_df_kernel<192, 5>, lanczos_small_df_kernel<160, 6>,
+                                lanczos_small_df_kernel<128, 8>};
+  static const int threads_of[5] = {512, 256, 192, 160, 128};
+  const size_t smem = small_df_smem_bytes(h->n);
+  const int nsm = grid_cap();
+  int best = -1, best_waves = 0, best_per_sm = 1;
+  for (int c = 0; c < 5; ++c) {
+    cudaFuncSetAttribute(kerns[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[c], threads_of[c], smem);
+    if (per_sm < 1) continue;
+    const int64_t slots = (int64_t)nsm * (per_sm > 1 ? per_sm - 1 : 1);
+    const int waves = (int)((R + slots - 1) / slots);
+    if (best < 0 || waves < best_waves) {
+      best = c;
+      best_waves = waves;
+      best_per_sm = per_sm;
+    }
   }
-  per_sm -= g_small_reserve.load();
+  if (best < 0) return EDGPU_ERR_ARG;
+  int per_sm = best_per_sm - g_small_reserve.load();
   if (per_sm < 1) per_sm = 1;
-  int grid = grid_cap() * per_sm;
+  int grid = nsm * per_sm;
   if (grid > R) grid = R;
-  kern<<<grid, threads, smem, s>>>(h->n, h->row_ptr, h->col, reinterpret_cast<const float2*>(h->val_df), R,
-                                   reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta, status);
+  float4* pbuf = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
+  kerns[best]<<<grid, threads_of[best], smem, s>>>(h->n, h->row_ptr, h->col,
+                                                   reinterpret_cast<const float2*>(h->val_df), R,
+                                                   reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta,
+                                                   status, pbuf);
   note_launch();
   return check_launch();
 }
 
 int lanczos_small(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
-                  double* alpha, double* beta, int32_t* status, cudaStream_t s) {
+                  double* alpha, double* beta, int32_t* status, void* ws, cudaStream_t s) {
   if (precision == 3) {
-    if (h->val_df && !h->val_c) return launch_small_df(h, v0, R, k_max, K, alpha, beta, status, s);
+    if (h->val_df && !h->val_c) return launch_small_df(h, v0, R, k_max, K, alpha, beta, status, ws, s);
     precision = 0;  // complex H: FP64
   }
   if (precision == 0) {

@@ -117,7 +117,7 @@ class CsrMatrix:
         if self.val_rf is not None or self.val_cf is not None:
             return self
         rows = torch.repeat_interleave(torch.arange(self.n, device=self.row_ptr.device),
-                                       self.row_ptr[1:] - self.row_ptr[:-1])
+                                       self.row_ptr[1:] - self.row_ptr[:-1], output_size=int(self.col.shape[0]))
         diag = rows == self.col.to(torch.int64)
         if self.val_r is not None:
             d = self.val_r[diag]
@@ -429,9 +429,9 @@ class Engine:
         if total == 0:
             return [(out_s[:0], out_v[:0]) for _ in range(runs)]
         run_of_input = torch.repeat_interleave(torch.arange(runs, device=self.device),
-                                               torch.tensor(sizes, device=self.device))
+                                               torch.tensor(sizes, device=self.device), output_size=sum(sizes))
         counts = offsets[1:] - offsets[:-1]
-        run_of_emit = torch.repeat_interleave(run_of_input, counts)
+        run_of_emit = torch.repeat_interleave(run_of_input, counts, output_size=total)
         keys = torch.cat([run_of_emit.view(-1, 1), out_s], 1).contiguous()
         payload = torch.arange(total, dtype=torch.int32, device=self.device)
         self.sort_states(keys, payload)
@@ -489,9 +489,9 @@ class Engine:
                                                     _ptr(offsets[o * n:]), None, _ptr(out_s), _ptr(out_v),
                                                     self.stream), "apply_vector(fill)")
         run_of_input = torch.repeat_interleave(torch.arange(runs, device=self.device),
-                                               torch.tensor(sizes, device=self.device))
+                                               torch.tensor(sizes, device=self.device), output_size=n)
         group = (torch.arange(n_ops, device=self.device).view(-1, 1) * runs + run_of_input.view(1, -1)).reshape(-1)
-        group_of_emit = torch.repeat_interleave(group, offsets[1:] - offsets[:-1])
+        group_of_emit = torch.repeat_interleave(group, offsets[1:] - offsets[:-1], output_size=total)
         keys = torch.cat([group_of_emit.view(-1, 1), out_s], 1).contiguous()
         payload = torch.arange(total, dtype=torch.int32, device=self.device)
         self.sort_states(keys, payload)
@@ -556,7 +556,8 @@ class Engine:
         labels = torch.arange(n, dtype=torch.int64, device=self.device)
         if csr.nnz == 0:
             return labels
-        rows = torch.repeat_interleave(torch.arange(n, device=self.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
+        rows = torch.repeat_interleave(torch.arange(n, device=self.device), csr.row_ptr[1:] - csr.row_ptr[:-1],
+                                       output_size=int(csr.col.shape[0]))
         cols = csr.col.to(torch.int64)
         for _ in range(10 * n + 10):
             m = torch.minimum(labels[rows], labels[cols])

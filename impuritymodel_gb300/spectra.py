@@ -187,7 +187,8 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
         sizes = torch.tensor([int(x.shape[0]) for x in run_states], device=eng.device)
         states = torch.cat(run_states, 0)
         amps = torch.cat(run_amps, 0)
-        run_of_row = torch.repeat_interleave(torch.arange(runs, device=eng.device), sizes)
+        run_of_row = torch.repeat_interleave(torch.arange(runs, device=eng.device), sizes,
+                                             output_size=int(states.shape[0]))
     n2 = torch.zeros(runs, dtype=torch.float64, device=eng.device)
     if amps.shape[0]:
         # per-run squared norms as segment sums in a fixed order (rows are grouped by run), so
@@ -420,20 +421,25 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
 
 
 def spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7, precision=0,
-                  capture=None, perturb=None, batched=True):
-    """spectra_device as a step generator for :func:`run_concurrently`."""
+                  capture=None, perturb=None, batched=True, t_outs=None, sector_hint=None):
+    """spectra_device as a step generator for :func:`run_concurrently`.  ``t_outs``: the
+    result of ``eng.apply_vectors_multi`` for these operators and states when the caller
+    has it already; ``sector_hint``: a sector closed under the restricted H that may hold
+    every start state (used when it does, as in :func:`green_setup`)."""
     ne = len(es)
     w = np.asarray(w, dtype=np.float64)
     run_states, run_amps, e_runs = [], [], []
-    for outs in eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], t_dops, restr,
-                                        slaterWeightMin):
+    if t_outs is None:
+        t_outs = eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], t_dops, restr,
+                                         slaterWeightMin)
+    for outs in t_outs:
         for i, (s_, a_) in enumerate(outs):
             run_states.append(s_)
             run_amps.append(a_)
             e_runs.append(es[i])
     if batched:
         g = yield from _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize,
-                                          precision, capture=capture, perturb=perturb)
+                                          precision, capture=capture, perturb=perturb, sector_hint=sector_hint)
     else:
         g = green_runs_one_by_one(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision)
     return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
@@ -536,11 +542,14 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
 
 def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-               timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None):
+               timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None, share=None):
     """rixs_device as a step generator for :func:`run_concurrently` (yields after the launch
-    of the final-state Lanczos).  ``final_sector``: a sector from :func:`closed_sector` (the
-    ground-state sector) used for the final states when it holds them all, instead of
-    expanding their closure."""
+    of the shifted solves and after the launch of the final-state Lanczos).  ``final_sector``:
+    a sector from :func:`closed_sector` (the ground-state sector) used for the final states
+    when it holds them all, instead of expanding their closure.  ``share``: a dict that
+    receives ``t_outs`` (T_in applied to the eigenstates, as ``eng.apply_vectors_multi``
+    returns it), ``sector`` (the core-hole sector, the closure of those states) and
+    ``ready`` (an event on the current stream after both) before the first yield."""
     _mark(stages, "start")
     wIns = np.asarray(wIns, dtype=np.float64)
     wLoss = np.asarray(wLoss, dtype=np.float64)
@@ -550,8 +559,8 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
         return gs
     # 1. core-hole states psi1 = T_in psi
     psi1 = {}
-    for t_in, outs in enumerate(eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], tin_dops,
-                                                        restr, slaterWeightMin)):
+    t_outs = eng.apply_vectors_multi([p[0] for p in psi_t], [p[1] for p in psi_t], tin_dops, restr, slaterWeightMin)
+    for t_in, outs in enumerate(t_outs):
         for ie, o in enumerate(outs):
             psi1[(t_in, ie)] = o
     nonempty = [v[0] for v in psi1.values() if v[0].shape[0]]
@@ -560,6 +569,8 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     _mark(stages, "rixs:psi1")
     # 2. core-hole sector
     core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
+    if share is not None:
+        share.update(t_outs=t_outs, sector=core, ready=torch.cuda.current_stream(eng.device).record_event())
     _mark(stages, "rixs:core_sector")
     # 3. outgoing operators as sparse maps core basis -> output states
     def build_out_maps():
@@ -579,14 +590,17 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
     s_all = torch.cat([psi1[k][0] for k in keys], 0)
     a_all = torch.cat([psi1[k][1] for k in keys], 0)
     r_all = torch.repeat_interleave(torch.arange(len(keys), device=eng.device),
-                                    torch.tensor([int(psi1[k][0].shape[0]) for k in keys], device=eng.device))
+                                    torch.tensor([int(psi1[k][0].shape[0]) for k in keys], device=eng.device),
+                                    output_size=int(s_all.shape[0]))
     Y.view(-1)[r_all * core.n + eng.lookup(core.basis, s_all)] = torch.complex(a_all[:, 0], a_all[:, 1])
     zs = np.array([wIns + 1j * delta1 + es[ie] for (_, ie) in keys])
     # without reorthogonalisation the recurrence may need a few times the sector dimension
     k_solve = min(6 * core.n + 50, max_krylov)
     if batched:
         # the outgoing maps are built on a side stream while the solves (one CTA per
-        # right-hand side, most SMs idle) run; the side stream waits only for the core basis
+        # right-hand side, most SMs idle) run; the side stream waits only for the core basis.
+        # Then the step yields, so that a pipeline running beside this one (run_concurrently)
+        # does its host work while the solves occupy the GPU.
         main = torch.cuda.current_stream(eng.device)
         ready = main.record_event()
         solved = eng.shifted_solve(core.csr, Y, zs, solve_tol, k_solve, precision, check=False)
@@ -598,6 +612,7 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
         for tm in set(out_maps):
             tm.record_stream(main)
         _mark(stages, "rixs:transfer")
+        yield
         if solved is not None:
             solved[2]()
     else:
@@ -681,16 +696,35 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
 
 def xas_rixs_device(eng, dop, restr, xas_dops, tin_dops, tout_dops, psi_t, es, w, delta, wIns, wLoss, delta1, delta2,
                     krylovSize=150, slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True,
-                    max_krylov=2000, final_sector=None):
+                    max_krylov=2000, final_sector=None, stages=None):
     """XAS (:func:`spectra_device`) and the RIXS map (:func:`rixs_device`) of the same
     eigenstates, computed side by side: the RIXS pipeline on the current stream, the XAS one
-    on a side stream, so the XAS host work (operator application, sector build) runs while
-    the RIXS final-state Lanczos occupies the GPU.  Same results as the two calls one after
-    the other.  Returns (g_xas [n_states, n_ops, n_w], g_rixs) on the device."""
+    on a side stream.  When the XAS operators are the RIXS incoming ones (the same objects),
+    the XAS job takes the RIXS job's T_in psi and core-hole sector, and its remaining host
+    work (start vectors, Krylov sizes, Lanczos launch) runs while the RIXS shifted solves
+    occupy the GPU; its continued fractions run beside the RIXS final-state Lanczos.  Same
+    results as the two calls one after the other.  ``stages``: optional
+    :class:`StageTimer`-like object marking the RIXS stages.  Returns (g_xas [n_states,
+    n_ops, n_w], g_rixs) on the device."""
+    share = {}
+    same_ops = len(xas_dops) == len(tin_dops) and all(a is b for a, b in zip(xas_dops, tin_dops))
+
+    def xas_steps():
+        # first advanced after the RIXS job's first yield, by when it has shared T_in psi and
+        # the core-hole sector: with the same operators these are the XAS start states and
+        # their sector, so the XAS job neither applies the operators again nor rebuilds it
+        if share:
+            torch.cuda.current_stream(eng.device).wait_event(share["ready"])
+        g = yield from spectra_steps(eng, dop, restr, xas_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin,
+                                     precision, t_outs=share.get("t_outs") if same_ops else None,
+                                     sector_hint=share.get("sector"))
+        return g
+
     g_rixs, g_xas = run_concurrently(eng, [
         rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize,
-                   slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov, final_sector=final_sector),
-        spectra_steps(eng, dop, restr, xas_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision)])
+                   slaterWeightMin, precision, solve_tol, share_out_memo, max_krylov, stages=stages,
+                   final_sector=final_sector, share=share),
+        xas_steps()])
     return g_xas, g_rixs
 
 
@@ -727,7 +761,8 @@ def _transfer_matrix(eng, tdop, restr, core_basis):
                                                 ncols=core_basis.shape[0]))
     outs = eng.sort_unique(out_s)
     row = eng.lookup(outs, out_s)
-    col = torch.repeat_interleave(torch.arange(core_basis.shape[0], device=eng.device), offsets[1:] - offsets[:-1])
+    col = torch.repeat_interleave(torch.arange(core_basis.shape[0], device=eng.device), offsets[1:] - offsets[:-1],
+                                  output_size=m)
     # entries sorted by (row, col) via a stable sort on row of col-ordered entries
     keys = row.view(-1, 1).contiguous()
     payload = torch.arange(m, dtype=torch.int32, device=eng.device)

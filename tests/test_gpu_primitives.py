@@ -228,6 +228,73 @@ def test_reorth_double_float_matches_fp64(eng, config):
     assert err < 1e-12, err
 
 
+@pytest.mark.parametrize("runs", [5, 300, 750, 1000])
+def test_small_double_float_lanczos_matches_fp64(eng, runs):
+    """The one-CTA-per-run double-float Lanczos (one shared-memory vector per run, the
+    previous vector in the workspace; the CTA size follows the run count: 512 threads for a
+    few runs, 160 for hundreds) against the FP64 recurrence on the 1770-row ground-state
+    sector of the 66-orbital model: the first 25 alphas and betas to 1e-9 relative, ragged
+    step counts honoured (k_max 0 leaves a run's coefficients zero)."""
+    from impuritymodel_gb300 import finite
+
+    mod = M.make_model("config2")
+    n = mod.n_spin_orbitals
+    dop = finite._device_op(mod.hOp, eng)
+    sb = finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n)
+    csr = finite._device_hamiltonian(eng, dop, sb)
+    assert csr.val_c is None
+    g = torch.Generator(device=eng.device)
+    g.manual_seed(runs)
+    v0 = torch.randn(csr.n, runs, dtype=torch.complex128, device=eng.device, generator=g)
+    v0 = v0 / torch.linalg.vector_norm(v0, dim=0, keepdim=True)
+    rng = np.random.default_rng(runs)
+    k_max = rng.integers(25, 41, size=runs).astype(np.int32)
+    k_max[0] = 0
+    k_max[-1] = 1
+    a0, b0 = eng.lanczos(csr, v0, k_max, precision=0)
+    a3, b3 = eng.lanczos(csr, v0, k_max, precision=3)
+    a0, b0, a3, b3 = (x.cpu().numpy() for x in (a0, b0, a3, b3))
+    assert not a3[0].any() and not b3[0].any()
+    assert a3[-1, 0] != 0.0 and not a3[-1, 1:].any() and not b3[-1].any()
+    live = np.arange(1, runs - 1)
+    for x0, x3 in ((a0, a3), (b0, b3)):
+        d = np.abs(x3[live, :24] - x0[live, :24]) / np.maximum(np.abs(x0[live, :24]), 1e-300)
+        assert d.max() < 1e-9, d.max()
+    for r in live[:50]:
+        assert not a3[r, k_max[r]:].any() and not b3[r, k_max[r] - 1:].any()
+
+
+@pytest.mark.parametrize("precision", [0, 3])
+def test_concurrent_xas_rixs_equals_sequential(eng, precision):
+    """xas_rixs_device (RIXS on the current stream, XAS on a side stream taking the RIXS
+    job's T_in psi and core-hole sector, the ground-state sector reused for the final states)
+    gives the same bits as spectra_device and rixs_device called one after the other."""
+    from impuritymodel_gb300 import finite, spectra
+    from impuritymodel_gb300.engine import DeviceOp, make_restrictions
+
+    mod = M.make_model("config2")
+    n = mod.n_spin_orbitals
+    dop = DeviceOp(mod.hOp, eng.device)
+    restr = make_restrictions(mod.restrictions, n)
+    xas = [DeviceOp(t, eng.device) for t in mod.xas_ops()]
+    outs = [DeviceOp(t, eng.device) for t in mod.rixs_out_ops()]
+    sb = finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n)
+    es, psi_t, h = finite.eigensystem_device(eng, dop, sb, 2, precision=precision, with_hamiltonian=True)
+    gs_sector = spectra.closed_sector(eng, dop, restr, sb.sorted, h, sb.words)
+    w = np.linspace(-25.0, 25.0, 300)
+    w_in = np.linspace(-10.0, 20.0, 4)
+    w_loss = np.linspace(-2.0, 12.0, 250)
+    gx1, gr1 = spectra.xas_rixs_device(eng, dop, restr, xas, xas, outs, psi_t, es, w, 0.2, w_in, w_loss, 0.2, 0.05,
+                                       150, 1e-7, precision, final_sector=gs_sector)
+    gx2 = spectra.spectra_device(eng, dop, restr, xas, psi_t, es, w, 0.2, 150, 1e-7, precision)
+    gr2 = spectra.rixs_device(eng, dop, restr, xas, outs, psi_t, es, w_in, w_loss, 0.2, 0.05, 150, 1e-7, precision,
+                              final_sector=gs_sector)
+    torch.cuda.synchronize()
+    assert torch.equal(gx1, gx2)
+    assert torch.equal(gr1, gr2)
+    assert gx1.abs().max().item() > 0 and gr1.abs().max().item() > 0
+
+
 def test_closed_ground_sector_serves_green_functions(eng):
     """The ground-state sector of the 66-orbital model is closed under the restricted H, so
     Green's-function runs starting inside it can use it instead of a fresh expansion.  When
