@@ -478,7 +478,6 @@ __global__ void cfrac_prep_kernel(const double* __restrict__ alpha, const double
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)R * K) return;
   const int r = (int)(t / K);
-  const int i = (int)(t % K);
   ap[t] = (float)(alpha[t] - e[r]);
   b2[t] = (float)(beta[t] * beta[t]);
   (void)k_len;
@@ -1184,6 +1183,214 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
   }
 }
 
+// Sliced layout of a CSR matrix for the one-CTA-per-run double-float Lanczos.  Rows are
+// ordered by length, longest first (a stable counting sort, so equal lengths keep their
+// order), and cut into slices of 32 consecutive slots, one slice per warp iteration; slice q
+// stores entry e of its lane-th row at soff[q] + 32 e + lane, padded to the slice's longest
+// row, so that a warp's loads of the e-th entries of its 32 rows are one contiguous 128-byte
+// (columns) and 256-byte (values) line, and the rows of a warp have nearly equal lengths.
+// sinfo[slot] = row | (length << 16), or -1 for the padding slots after the last row.
+// Built by one CTA: the counting sort's histogram with atomics (order-free), the stable
+// placement by warp 0 with __match_any_sync ranks, then the fill by every thread.  When the
+// slices would need more than `cap` entries (possible only for rows with repeated columns)
+// every slot gets length 0 and *status EDGPU_ERR_WORKSPACE, so nothing reads past the arrays.
+__global__ void __launch_bounds__(1024) df_slices_kernel(int64_t n, const int64_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ col,
+                                                         const float2* __restrict__ hv, int32_t* __restrict__ sinfo,
+                                                         int32_t* __restrict__ soff, int32_t* __restrict__ ecol,
+                                                         float2* __restrict__ eval, int64_t cap, int32_t* status) {
+  extern __shared__ int32_t hist[];  // [n + 1] bucket offsets (row lengths 0..n)
+  __shared__ int32_t s_max;
+  __shared__ int32_t s_over;
+  const int tid = threadIdx.x;
+  const int npad = (int)((n + 31) & ~(int64_t)31), nslices = npad >> 5;
+  if (tid == 0) {
+    s_max = 0;
+    s_over = 0;
+  }
+  __syncthreads();
+  int lmax = 0;
+  for (int64_t i = tid; i < n; i += blockDim.x) lmax = max(lmax, (int)(rp[i + 1] - rp[i]));
+  atomicMax(&s_max, lmax);
+  __syncthreads();
+  if (s_max > n) {  // repeated columns: no sliced layout
+    for (int q = tid; q < npad; q += blockDim.x) sinfo[q] = q < n ? q : -1;
+    for (int q = tid; q <= nslices; q += blockDim.x) soff[q] = 0;
+    if (tid == 0) atomicExch(status, (int32_t)EDGPU_ERR_WORKSPACE);
+    return;
+  }
+  const int L = s_max;
+  for (int k = tid; k <= L; k += blockDim.x) hist[k] = 0;
+  __syncthreads();
+  for (int64_t i = tid; i < n; i += blockDim.x) atomicAdd(&hist[L - (int)(rp[i + 1] - rp[i])], 1);
+  __syncthreads();
+  if (tid == 0) {
+    int run = 0;
+    for (int k = 0; k <= L; ++k) {
+      const int c = hist[k];
+      hist[k] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  if (tid < 32) {
+    const unsigned lt = (1u << tid) - 1u;
+    for (int64_t c0 = 0; c0 < n; c0 += 32) {
+      const int64_t i = c0 + tid;
+      const int len = i < n ? (int)(rp[i + 1] - rp[i]) : 0;
+      const int key = i < n ? L - len : -1;
+      const unsigned same = __match_any_sync(0xffffffffu, key);
+      const int base = key >= 0 ? hist[key] : 0;
+      if (i < n) sinfo[base + __popc(same & lt)] = (int32_t)i | (len << 16);
+      __syncwarp();
+      if (key >= 0 && (__ffs(same) - 1) == tid) hist[key] = base + __popc(same);
+      __syncwarp();
+    }
+  }
+  for (int q = (int)n + tid; q < npad; q += blockDim.x) sinfo[q] = -1;
+  __syncthreads();
+  if (tid == 0) {
+    int64_t off = 0;
+    soff[0] = 0;
+    for (int q = 0; q < nslices; ++q) {
+      off += 32 * (int64_t)(sinfo[32 * q] >> 16);  // the slice's first row is its longest
+      soff[q + 1] = (int32_t)off;
+    }
+    if (off > cap) s_over = 1;
+  }
+  __syncthreads();
+  if (s_over) {
+    for (int q = tid; q < npad; q += blockDim.x) sinfo[q] = sinfo[q] < 0 ? -1 : (sinfo[q] & 0xffff);
+    for (int q = tid; q <= nslices; q += blockDim.x) soff[q] = 0;
+    if (tid == 0) atomicExch(status, (int32_t)EDGPU_ERR_WORKSPACE);
+    return;
+  }
+  for (int q = tid; q < npad; q += blockDim.x) {
+    const int info = sinfo[q];
+    const int sl = q >> 5;
+    const int m = (soff[sl + 1] - soff[sl]) >> 5;
+    const int64_t base = soff[sl] + (q & 31);
+    const int len = info < 0 ? 0 : (info >> 16);
+    const int64_t e0 = info < 0 ? 0 : rp[info & 0xffff];
+    for (int e = 0; e < m; ++e) {
+      ecol[base + 32 * e] = e < len ? col[e0 + e] : 0;
+      eval[base + 32 * e] = e < len ? hv[e0 + e] : make_float2(0.f, 0.f);
+    }
+  }
+}
+
+// Entries the sliced layout can need: every slice but the first is no wider than the
+// shortest row of the slice before it, so the padding beyond nnz is at most 32 times the
+// longest row, itself at most n for rows without repeated columns.
+static int64_t df_slices_cap(int64_t n, int64_t nnz) { return nnz + 32 * n; }
+
+// lanczos_small_df_kernel on the sliced layout: thread tid walks the slots tid, tid +
+// THREADS, ... (a warp takes whole slices), so its rows and their order follow the slots;
+// v_{j-1} is kept per slot.  The arithmetic of every row and vector element is that of
+// lanczos_small_df_kernel; only the rows' assignment to threads, and so the order of the
+// per-thread partial sums of alpha and beta, differ.
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
+    int64_t n, const int32_t* __restrict__ g_sinfo, const int32_t* __restrict__ g_soff,
+    const int32_t* __restrict__ ecol, const float2* __restrict__ eval, int R, const double2* __restrict__ v0,
+    const int32_t* __restrict__ k_max, int K, double* __restrict__ alpha, double* __restrict__ beta, int32_t* status,
+    float4* __restrict__ pbuf) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int npad = (int)((n + 31) & ~(int64_t)31), nslices = npad >> 5;
+  float4* x = reinterpret_cast<float4*>(sm);
+  dfl* red = reinterpret_cast<dfl*>(x + n);
+  int32_t* sinfo = reinterpret_cast<int32_t*>(red + kDfRed);
+  int32_t* soff = sinfo + npad;
+  float4* __restrict__ p = pbuf + (size_t)blockIdx.x * (size_t)npad;
+  constexpr int NW = THREADS / 32;
+  const int tid = threadIdx.x;
+  const dfl zero = {0.f, 0.f};
+  for (int q = tid; q < npad; q += THREADS) sinfo[q] = g_sinfo[q];
+  for (int q = tid; q <= nslices; q += THREADS) soff[q] = g_soff[q];
+  for (int r = blockIdx.x; r < R; r += gridDim.x) {
+    const int km = k_max[r];
+    if (km <= 0) continue;
+    for (int64_t i = tid; i < n; i += THREADS) {
+      const double2 v = v0[i * R + r];
+      const dfl re = df_split(v.x), im = df_split(v.y);
+      x[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
+    }
+    for (int q = tid; q < npad; q += THREADS) p[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    dfl bprev = zero;
+    for (int j = 0; j < km; ++j) {
+      const dfl nb = {-bprev.hi, -bprev.lo};
+      dacc2 acc = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int q = tid; q < npad; q += THREADS) {
+        const int info = sinfo[q];
+        if (info < 0) continue;
+        const float4 pq = p[q];
+        const int row = info & 0xffff, len = info >> 16;
+        const int64_t base = soff[q >> 5] + (q & 31);
+        dacc2 y = {{0.f, 0.f}, {0.f, 0.f}};
+        for (int e = 0; e < len; e += kSmallBatch) {
+          int c[kSmallBatch];
+          float2 hh[kSmallBatch];
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            const bool ok = e + u < len;
+            c[u] = ok ? __ldg(ecol + base + 32 * (e + u)) : 0;
+            hh[u] = ok ? __ldg(eval + base + 32 * (e + u)) : make_float2(0.f, 0.f);
+          }
+#pragma unroll
+          for (int u = 0; u < kSmallBatch; ++u) {
+            if (e + u < len) {
+              const float4 xv = x[c[u]];
+              dacc2_fma(y, {hh[u].x, hh[u].y}, make_float2(xv.x, xv.y), make_float2(xv.z, xv.w));
+            }
+          }
+        }
+        const dfl2 h = dacc2_val(y);
+        const float4 xi = x[row];
+        dacc2_fma2(acc, h, make_float2(xi.x, xi.y), make_float2(xi.z, xi.w));
+        const dfl2 w = df2_fma_s(h, {make_float2(pq.x, pq.y), make_float2(pq.z, pq.w)}, nb);
+        p[q] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
+      }
+      const dfl a = df_block_sum2<NW>(dacc2_total(acc), red);
+      if (tid == THREADS - 1) alpha[(int64_t)r * K + j] = df_val(a);
+      if (j + 1 == km) break;
+      const dfl na = {-a.hi, -a.lo};
+      acc = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int q = tid; q < npad; q += THREADS) {
+        const int info = sinfo[q];
+        if (info < 0) continue;
+        const int row = info & 0xffff;
+        const float4 wv = p[q], xi = x[row];
+        const dfl2 w = df2_fma_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)},
+                                 {make_float2(xi.x, xi.y), make_float2(xi.z, xi.w)}, na);
+        p[q] = xi;  // v_j: the next step's v_{j-1}
+        x[row] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
+        dacc2_fma2(acc, w, w.hi, w.lo);
+      }
+      bprev = df_sqrt(df_block_sum2<NW>(dacc2_total(acc), red + 40));
+      const dfl ib = bprev.hi > 0.f ? df_rcp(bprev) : zero;
+      if (tid == THREADS - 1) {
+        const double b = df_val(bprev);
+        beta[(int64_t)r * K + j] = b;
+        if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
+      }
+      // pass 2's x[row] writes are ordered before these reads by the barriers of the beta sum
+      for (int64_t i = tid; i < n; i += THREADS) {
+        const float4 wv = x[i];
+        const dfl2 v = df2_mul_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)}, ib);
+        x[i] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+  }
+}
+
+static size_t sliced_df_smem_bytes(int64_t n) {
+  const int64_t npad = (n + 31) & ~(int64_t)31;
+  return sizeof(float4) * (size_t)n + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(npad + npad / 32 + 1) + 16;
+}
+
 // Shared memory that decides whether a sector takes the one-CTA-per-run path (unchanged by
 // the one-vector form of the double-float kernel, so that the same sectors take it).
 size_t small_smem_bytes(int64_t n, int precision) {
@@ -1229,40 +1436,91 @@ extern "C" void edgpu_set_small_reserve(int slots) { g_small_reserve.store(slots
 // run's reduction order, and its result bits, do not change with concurrent work; the
 // reserve only limits how many of the CTAs are resident at once.  On the 1770-row RIXS
 // final-state sector with 750 runs this is 160 threads, five CTAs per SM, one wave.
-int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
-                    double* beta, int32_t* status, void* ws, cudaStream_t s) {
-  using Kern = void (*)(int64_t, const int64_t*, const int32_t*, const float2*, int, const double2*, const int32_t*,
-                        int, double*, double*, int32_t*, float4*);
-  static const Kern kerns[5] = {lanczos_small_df_kernel<512, 2>, lanczos_small_df_kernel<256, 4>,
-                                lanczos_small_df_kernel<192, 5>, lanczos_small_df_kernel<160, 6>,
-                                lanczos_small_df_kernel<128, 8>};
-  static const int threads_of[5] = {512, 256, 192, 160, 128};
-  const size_t smem = small_df_smem_bytes(h->n);
+// The sliced layout is used when the smallest workspace edgpu_lanczos accepts for (n, R, K)
+// holds it next to the per-CTA vectors (a function of the problem only, so a given problem
+// always takes the same path); otherwise the kernel reads the CSR arrays directly.
+using SmallDfKern = void (*)(int64_t, const int64_t*, const int32_t*, const float2*, int, const double2*,
+                             const int32_t*, int, double*, double*, int32_t*, float4*);
+using SlicedDfKern = void (*)(int64_t, const int32_t*, const int32_t*, const int32_t*, const float2*, int,
+                              const double2*, const int32_t*, int, double*, double*, int32_t*, float4*);
+static const int kDfThreads[5] = {512, 256, 192, 160, 128};
+
+static int pick_df_config(const void* const* kerns, size_t smem, int R, int* per_sm_out) {
   const int nsm = grid_cap();
-  int best = -1, best_waves = 0, best_per_sm = 1;
+  int best = -1, best_waves = 0;
   for (int c = 0; c < 5; ++c) {
     cudaFuncSetAttribute(kerns[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[c], threads_of[c], smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[c], kDfThreads[c], smem);
     if (per_sm < 1) continue;
     const int64_t slots = (int64_t)nsm * (per_sm > 1 ? per_sm - 1 : 1);
     const int waves = (int)((R + slots - 1) / slots);
     if (best < 0 || waves < best_waves) {
       best = c;
       best_waves = waves;
-      best_per_sm = per_sm;
+      *per_sm_out = per_sm;
     }
   }
-  if (best < 0) return EDGPU_ERR_ARG;
-  int per_sm = best_per_sm - g_small_reserve.load();
-  if (per_sm < 1) per_sm = 1;
-  int grid = nsm * per_sm;
+  return best;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int launch_small_df(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, double* alpha,
+                    double* beta, int32_t* status, void* ws, cudaStream_t s) {
+  static const SmallDfKern csr_kerns[5] = {lanczos_small_df_kernel<512, 2>, lanczos_small_df_kernel<256, 4>,
+                                           lanczos_small_df_kernel<192, 5>, lanczos_small_df_kernel<160, 6>,
+                                           lanczos_small_df_kernel<128, 8>};
+  static const SlicedDfKern sl_kerns[5] = {lanczos_sliced_df_kernel<512, 2>, lanczos_sliced_df_kernel<256, 4>,
+                                           lanczos_sliced_df_kernel<192, 5>, lanczos_sliced_df_kernel<160, 6>,
+                                           lanczos_sliced_df_kernel<128, 8>};
+  const int64_t n = h->n, nnz = h->nnz;
+  const int64_t npad = (n + 31) & ~(int64_t)31, nslices = npad / 32;
+  const int nsm = grid_cap();
+  const int reserve = g_small_reserve.load();
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
+  // sliced layout: per-CTA vectors, slot table, slice offsets, columns, values
+  if (n <= 32767) {
+    const size_t smem = sliced_df_smem_bytes(n);
+    int per_sm = 1;
+    const int c = pick_df_config(reinterpret_cast<const void* const*>(sl_kerns), smem, R, &per_sm);
+    if (c >= 0) {
+      int grid = nsm * (per_sm - reserve > 0 ? per_sm - reserve : 1);
+      if (grid > R) grid = R;
+      const int64_t cap = df_slices_cap(n, nnz);
+      const size_t b_p = align256(sizeof(float4) * (size_t)npad * (size_t)(R < nsm * per_sm ? R : nsm * per_sm));
+      const size_t b_info = align256(sizeof(int32_t) * (size_t)npad);
+      const size_t b_off = align256(sizeof(int32_t) * (size_t)(nslices + 1));
+      const size_t b_col = align256(sizeof(int32_t) * (size_t)cap);
+      const size_t b_val = align256(sizeof(float2) * (size_t)cap);
+      if (256 + b_p + b_info + b_off + b_col + b_val <= edgpu_lanczos_workspace(n, R, K, 3)) {
+        float4* pbuf = reinterpret_cast<float4*>(base);
+        int32_t* sinfo = reinterpret_cast<int32_t*>(base + b_p);
+        int32_t* soff = reinterpret_cast<int32_t*>(base + b_p + b_info);
+        int32_t* ecol = reinterpret_cast<int32_t*>(base + b_p + b_info + b_off);
+        float2* eval = reinterpret_cast<float2*>(base + b_p + b_info + b_off + b_col);
+        const size_t hist_bytes = sizeof(int32_t) * (size_t)(n + 1);
+        cudaFuncSetAttribute(df_slices_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_bytes);
+        df_slices_kernel<<<1, 1024, hist_bytes, s>>>(n, h->row_ptr, h->col, reinterpret_cast<const float2*>(h->val_df),
+                                                     sinfo, soff, ecol, eval, cap, status);
+        note_launch();
+        sl_kerns[c]<<<grid, kDfThreads[c], smem, s>>>(n, sinfo, soff, ecol, eval, R,
+                                                       reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta,
+                                                       status, pbuf);
+        note_launch();
+        return check_launch();
+      }
+    }
+  }
+  const size_t smem = small_df_smem_bytes(n);
+  int per_sm = 1;
+  const int c = pick_df_config(reinterpret_cast<const void* const*>(csr_kerns), smem, R, &per_sm);
+  if (c < 0) return EDGPU_ERR_ARG;
+  int grid = nsm * (per_sm - reserve > 0 ? per_sm - reserve : 1);
   if (grid > R) grid = R;
-  float4* pbuf = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
-  kerns[best]<<<grid, threads_of[best], smem, s>>>(h->n, h->row_ptr, h->col,
-                                                   reinterpret_cast<const float2*>(h->val_df), R,
-                                                   reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta,
-                                                   status, pbuf);
+  csr_kerns[c]<<<grid, kDfThreads[c], smem, s>>>(n, h->row_ptr, h->col, reinterpret_cast<const float2*>(h->val_df), R,
+                                                 reinterpret_cast<const double2*>(v0), k_max, K, alpha, beta, status,
+                                                 reinterpret_cast<float4*>(base));
   note_launch();
   return check_launch();
 }
