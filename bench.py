@@ -504,7 +504,10 @@ def pipeline_kernel_stats(timing):
     t = timing[-1]
     alg = t["nnz"] * (t["val_bytes"] + 4) + (t["n"] + 1) * 8 + 2 * t["n"] * t["R"] * t["vec_bytes"]
     avg = t["spmm_ms"] / max(t["spmm_launches"], 1) / 1e3
-    return {"kernel": "spmm_alpha_kernel (RIXS final-state Lanczos)", "n": t["n"], "nnz": t["nnz"], "R": t["R"],
+    kern = ("df_slices_kernel + lanczos_sliced_df_kernel (RIXS final-state Lanczos, one persistent launch; "
+            "avg_launch_us is its time per Lanczos step)" if t["precision"] == 3
+            else "spmm_alpha_kernel (RIXS final-state Lanczos)")
+    return {"kernel": kern, "n": t["n"], "nnz": t["nnz"], "R": t["R"],
             "K": t["K"], "precision": {0: "c128", 1: "c64", 3: "df64"}.get(t["precision"], "c128"), "avg_launch_us": round(avg * 1e6, 2),
             "achieved_gbs": round(alg / avg / 1e9, 1) if avg > 0 else None,
             "note": "working set resident in L2; kernel times summed over the Lanczos call",

@@ -363,15 +363,16 @@ class Engine:
                                              _ptr(self.status), self.stream),
                 "apply_columns(count)",
             )
-            st = int(self.status.item())
+            offsets = self.scan(counts)
+            # the status and the emission total in one read (the scan of an overflowed count
+            # pass is discarded)
+            st, total = (int(x) for x in torch.cat([self.status.to(torch.int64).view(1), offsets[-1:]]).cpu())
             if st == L.EDGPU_ERR_OVERFLOW and self.scratch_entries < 8192:
                 self.scratch_entries *= 4
                 continue
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "apply_columns(count)")
             break
-        offsets = self.scan(counts)
-        total = int(offsets[-1].item())
         out_s = torch.empty((total, w), dtype=torch.int64, device=self.device) if want_states else None
         out_i = torch.empty(total, dtype=torch.int64, device=self.device) if want_index else None
         out_v = torch.empty((total, 2), dtype=torch.float64, device=self.device) if want_vals else None

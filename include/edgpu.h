@@ -198,7 +198,11 @@ int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* st
  * anywhere else runs as 0.  Breakdown (beta == 0 before k_max) sets
  * *status_dev = EDGPU_ERR_BREAKDOWN.  Sectors whose three Krylov vectors fit in shared
  * memory run as one persistent launch with one CTA per run; larger ones as three
- * grid-wide kernels per step.
+ * grid-wide kernels per step.  In the double-float form the CTA keeps one vector in shared
+ * memory and the previous one in the workspace, and, when the workspace size returned for
+ * (n, R, K) also holds it, reads H through a sliced copy (rows sorted by length in 32-row
+ * column-major slices) that one extra launch builds in the workspace; a matrix whose rows
+ * repeat a column then sets *status_dev = EDGPU_ERR_WORKSPACE.
  */
 size_t edgpu_lanczos_workspace(int64_t n, int R, int K, int precision);
 int edgpu_lanczos(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
