@@ -1189,7 +1189,9 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_small_df_kernel(
 // stores entry e of its lane-th row at soff[q] + 32 e + lane, padded to the slice's longest
 // row, so that a warp's loads of the e-th entries of its 32 rows are one contiguous 128-byte
 // (columns) and 256-byte (values) line, and the rows of a warp have nearly equal lengths.
-// sinfo[slot] = row | (length << 16), or -1 for the padding slots after the last row.
+// sinfo[slot] = row | (length << 16), or -1 for the padding slots after the last row; the
+// stored columns are slots too (the slot that holds the column's row), so the Lanczos kernel
+// keeps its vector in slot order and touches a warp's own rows contiguously.
 // Built by one CTA: the counting sort's histogram with atomics (order-free), the stable
 // placement by warp 0 with __match_any_sync ranks, then the fill by every thread.  When the
 // slices would need more than `cap` entries (possible only for rows with repeated columns)
@@ -1249,6 +1251,9 @@ __global__ void __launch_bounds__(1024) df_slices_kernel(int64_t n, const int64_
   }
   for (int q = (int)n + tid; q < npad; q += blockDim.x) sinfo[q] = -1;
   __syncthreads();
+  // the bucket offsets are spent: hist becomes the slot of each row
+  for (int q = tid; q < (int)n; q += blockDim.x) hist[sinfo[q] & 0xffff] = q;
+  __syncthreads();
   if (tid == 0) {
     int64_t off = 0;
     soff[0] = 0;
@@ -1273,7 +1278,7 @@ __global__ void __launch_bounds__(1024) df_slices_kernel(int64_t n, const int64_
     const int len = info < 0 ? 0 : (info >> 16);
     const int64_t e0 = info < 0 ? 0 : rp[info & 0xffff];
     for (int e = 0; e < m; ++e) {
-      ecol[base + 32 * e] = e < len ? col[e0 + e] : 0;
+      ecol[base + 32 * e] = e < len ? hist[col[e0 + e]] : 0;
       eval[base + 32 * e] = e < len ? hv[e0 + e] : make_float2(0.f, 0.f);
     }
   }
@@ -1286,7 +1291,8 @@ static int64_t df_slices_cap(int64_t n, int64_t nnz) { return nnz + 32 * n; }
 
 // lanczos_small_df_kernel on the sliced layout: thread tid walks the slots tid, tid +
 // THREADS, ... (a warp takes whole slices), so its rows and their order follow the slots;
-// v_{j-1} is kept per slot.  The arithmetic of every row and vector element is that of
+// both vectors are kept in slot order (the stored columns are slots), so every access but
+// the H v gathers is contiguous.  The arithmetic of every row and vector element is that of
 // lanczos_small_df_kernel; only the rows' assignment to threads, and so the order of the
 // per-thread partial sums of alpha and beta, differ.
 template <int THREADS, int MINB>
@@ -1297,8 +1303,8 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
     float4* __restrict__ pbuf) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int npad = (int)((n + 31) & ~(int64_t)31), nslices = npad >> 5;
-  float4* x = reinterpret_cast<float4*>(sm);
-  dfl* red = reinterpret_cast<dfl*>(x + n);
+  float4* x = reinterpret_cast<float4*>(sm);  // in slot order, zero in the padding slots
+  dfl* red = reinterpret_cast<dfl*>(x + npad);
   int32_t* sinfo = reinterpret_cast<int32_t*>(red + kDfRed);
   int32_t* soff = sinfo + npad;
   float4* __restrict__ p = pbuf + (size_t)blockIdx.x * (size_t)npad;
@@ -1310,12 +1316,17 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
   for (int r = blockIdx.x; r < R; r += gridDim.x) {
     const int km = k_max[r];
     if (km <= 0) continue;
-    for (int64_t i = tid; i < n; i += THREADS) {
-      const double2 v = v0[i * R + r];
-      const dfl re = df_split(v.x), im = df_split(v.y);
-      x[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
+    for (int q = tid; q < npad; q += THREADS) {
+      const int info = sinfo[q];
+      float4 xv = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (info >= 0) {
+        const double2 v = v0[(int64_t)(info & 0xffff) * R + r];
+        const dfl re = df_split(v.x), im = df_split(v.y);
+        xv = make_float4(re.hi, im.hi, re.lo, im.lo);
+      }
+      x[q] = xv;
+      p[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int q = tid; q < npad; q += THREADS) p[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     dfl bprev = zero;
     for (int j = 0; j < km; ++j) {
@@ -1325,7 +1336,7 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
         const int info = sinfo[q];
         if (info < 0) continue;
         const float4 pq = p[q];
-        const int row = info & 0xffff, len = info >> 16;
+        const int len = info >> 16;
         const int64_t base = soff[q >> 5] + (q & 31);
         dacc2 y = {{0.f, 0.f}, {0.f, 0.f}};
         for (int e = 0; e < len; e += kSmallBatch) {
@@ -1346,7 +1357,7 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
           }
         }
         const dfl2 h = dacc2_val(y);
-        const float4 xi = x[row];
+        const float4 xi = x[q];
         dacc2_fma2(acc, h, make_float2(xi.x, xi.y), make_float2(xi.z, xi.w));
         const dfl2 w = df2_fma_s(h, {make_float2(pq.x, pq.y), make_float2(pq.z, pq.w)}, nb);
         p[q] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
@@ -1357,14 +1368,12 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
       const dfl na = {-a.hi, -a.lo};
       acc = {{0.f, 0.f}, {0.f, 0.f}};
       for (int q = tid; q < npad; q += THREADS) {
-        const int info = sinfo[q];
-        if (info < 0) continue;
-        const int row = info & 0xffff;
-        const float4 wv = p[q], xi = x[row];
+        if (sinfo[q] < 0) continue;
+        const float4 wv = p[q], xi = x[q];
         const dfl2 w = df2_fma_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)},
                                  {make_float2(xi.x, xi.y), make_float2(xi.z, xi.w)}, na);
         p[q] = xi;  // v_j: the next step's v_{j-1}
-        x[row] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
+        x[q] = make_float4(w.hi.x, w.hi.y, w.lo.x, w.lo.y);
         dacc2_fma2(acc, w, w.hi, w.lo);
       }
       bprev = df_sqrt(df_block_sum2<NW>(dacc2_total(acc), red + 40));
@@ -1374,11 +1383,10 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
         beta[(int64_t)r * K + j] = b;
         if (!(b > 0.0)) atomicExch(status, (int32_t)(b == 0.0 ? EDGPU_ERR_BREAKDOWN : EDGPU_ERR_NAN));
       }
-      // pass 2's x[row] writes are ordered before these reads by the barriers of the beta sum
-      for (int64_t i = tid; i < n; i += THREADS) {
-        const float4 wv = x[i];
+      for (int q = tid; q < npad; q += THREADS) {  // the padding slots stay zero
+        const float4 wv = x[q];
         const dfl2 v = df2_mul_s({make_float2(wv.x, wv.y), make_float2(wv.z, wv.w)}, ib);
-        x[i] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
+        x[q] = make_float4(v.hi.x, v.hi.y, v.lo.x, v.lo.y);
       }
       __syncthreads();
     }
@@ -1388,7 +1396,7 @@ __global__ void __launch_bounds__(THREADS, MINB) lanczos_sliced_df_kernel(
 
 static size_t sliced_df_smem_bytes(int64_t n) {
   const int64_t npad = (n + 31) & ~(int64_t)31;
-  return sizeof(float4) * (size_t)n + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(npad + npad / 32 + 1) + 16;
+  return sizeof(float4) * (size_t)npad + kDfRed * sizeof(dfl) + sizeof(int32_t) * (size_t)(npad + npad / 32 + 1) + 16;
 }
 
 // Shared memory that decides whether a sector takes the one-CTA-per-run path (unchanged by
