@@ -359,6 +359,10 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
         "fp64": {"achieved": round(alg64 / avg64 / 1e9, 1), "avg_launch_us": round(avg64 * 1e6, 2),
                  "algorithmic_bytes_per_launch": int(alg64)},
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+        "note": ("DRAM traffic equals the algorithmic bytes (no re-reads); x (59 MB) stays in L2 and every "
+                 "nonzero gathers a 128-byte x row from it (about 3.7x the algorithmic bytes from L2 to "
+                 "the SMs), so the kernel is bound by the latency of those gathers, not by HBM "
+                 "(profiles/spmm_c64_hv_ps300bath.md)"),
     }
 
 
