@@ -742,17 +742,89 @@ def traffic_from_profile(roof):
 # ---------------------------------------------------------------------------------------
 
 
-def cpu_reference_time(budget_s=20.0):
+def _ref_rixs_setup(O, mod, es, psis):
+    """Oracle state for the RIXS units of one (in-polarisation, eigenstate): T_in psi, the
+    core-hole sector Hamiltonian, and the column memos of upstream's getRIXSmap."""
+    W = WORKLOAD
+    n = mod.n_spin_orbitals
+    psi1 = O.apply_op(n, mod.xas_ops()[0], psis[0], W["slater_weight_min"], mod.restrictions)
+    memo_c = O._ColumnMemo(n, mod.hOp, mod.restrictions)
+    h, idx = O.expand_basis_and_hamiltonian(n, None, mod.hOp, list(psi1.keys()), mod.restrictions, memo=memo_c)
+    y = np.zeros(len(idx), dtype=complex)
+    for s_, a in psi1.items():
+        y[idx[s_]] = a
+    return {"n": n, "mod": mod, "e0": es[0], "h": h, "y": y, "basis_state": {k: s_ for s_, k in idx.items()},
+            "touts": mod.rixs_out_ops(), "memo_g": O._ColumnMemo(n, mod.hOp, mod.restrictions), "shared": {}}
+
+
+def _ref_rixs_unit(O, st, wi, w_loss):
+    """One RIXS unit of upstream's getRIXSmap: the BiCGSTAB solve at one incoming energy and
+    the Green's functions of the three outgoing polarisations."""
+    import scipy.sparse
+    import scipy.sparse.linalg
+
+    W = WORKLOAD
+    n, mod, h = st["n"], st["mod"], st["h"]
+    m = h.shape[0]
+    a = scipy.sparse.csr_matrix(([wi + 1j * W["rixs"]["delta_in"] + st["e0"]] * m, (range(m), range(m))),
+                                shape=h.shape) - h
+    x, _ = scipy.sparse.linalg.bicgstab(a, st["y"], rtol=1e-5)
+    psi2 = {st["basis_state"][i]: amp for i, amp in enumerate(x) if amp != 0}
+    for top in st["touts"]:
+        psi3 = O.apply_op(n, top, psi2, W["slater_weight_min"], mod.restrictions, st["shared"])
+        nrm = np.sqrt(O.norm2(psi3))
+        psi3 = {s_: a_ / nrm for s_, a_ in psi3.items()}
+        psi3 = {s_: a_ for s_, a_ in psi3.items() if abs(a_) ** 2 >= W["slater_weight_min"]}
+        O.get_green(n, st["e0"], psi3, mod.hOp, w_loss, W["rixs"]["delta_loss"], W["krylov"],
+                    W["slater_weight_min"], mod.restrictions, memo=st["memo_g"])
+
+
+_REF_WORKER = None
+
+
+def _ref_worker_init():
+    """Pool initialiser (spawned process): the oracle's ground state and RIXS setup."""
+    global _REF_WORKER
+    import oracle.ed_oracle as O
+
+    from impuritymodel_gb300 import models
+
+    mod = models.make_model("config2")
+    basis = O.get_basis(*mod.basis_args())
+    es, psis = O.eigensystem(mod.n_spin_orbitals, mod.hOp, basis, WORKLOAD["n_psi"])
+    _REF_WORKER = (O, _ref_rixs_setup(O, mod, es, psis))
+
+
+def _ref_worker_units(args):
+    """RIXS unit times of one worker: incoming energies rank, rank + procs, ... (cycling)
+    until ``budget_s`` has passed and at least three units ran."""
+    rank, procs, budget_s = args
+    O, st = _REF_WORKER
+    _, w_in, w_loss = meshes()
+    times = []
+    t_start = time.perf_counter()
+    k = rank
+    while True:
+        t0 = time.perf_counter()
+        _ref_rixs_unit(O, st, w_in[k % len(w_in)], w_loss)
+        times.append(time.perf_counter() - t0)
+        k += procs
+        if time.perf_counter() - t_start > budget_s and len(times) >= 3:
+            return times
+
+
+def cpu_reference_time(budget_s=20.0, pool=None, procs=1):
     """Time the oracle on pieces of the workload and extrapolate to one full step.
 
     Sample: full ground state; two XAS Green's functions (the first builds the sector
     memo); for one (in-polarisation, eigenstate): the core-hole sector, BiCGSTAB solves
     and outgoing Green's functions for as many incoming energies as fit in ``budget_s``.
-    The full step = GS + XAS runs + RIXS units scaled by their counts.
+    The full step = GS + XAS runs + RIXS units scaled by their counts.  With a process
+    ``pool`` of ``procs`` workers the RIXS units are timed on all workers at once and the
+    independent pieces (XAS runs, RIXS setups, RIXS units) are divided among the workers
+    (upstream's eigen_states / wIn parallel modes); the ground state stays serial.
     """
     import oracle.ed_oracle as O
-    import scipy.sparse
-    import scipy.sparse.linalg
 
     from impuritymodel_gb300 import models
 
@@ -773,54 +845,58 @@ def cpu_reference_time(budget_s=20.0):
         t0 = time.perf_counter()
         pr = O.apply_op(n, tops[0], psis[i], W["slater_weight_min"], mod.restrictions)
         nrm = np.sqrt(O.norm2(pr))
-        pr = {s: a / nrm for s, a in pr.items()}
+        pr = {s_: a / nrm for s_, a in pr.items()}
         O.get_green(n, es[i], pr, mod.hOp, w, W["xas"]["delta"], W["krylov"], W["slater_weight_min"],
                     mod.restrictions, memo=memo)
         xt.append(time.perf_counter() - t0)
     n_xas = 3 * ne
-    t_xas = xt[0] + (n_xas - 1) * (xt[-1] if len(xt) > 1 else xt[0])
+    t_xas_rest = xt[-1] if len(xt) > 1 else xt[0]
     # RIXS sample
     t0 = time.perf_counter()
-    psi1 = O.apply_op(n, tops[0], psis[0], W["slater_weight_min"], mod.restrictions)
-    memo_c = O._ColumnMemo(n, mod.hOp, mod.restrictions)
-    h, idx = O.expand_basis_and_hamiltonian(n, None, mod.hOp, list(psi1.keys()), mod.restrictions, memo=memo_c)
-    y = np.zeros(len(idx), dtype=complex)
-    for s, a in psi1.items():
-        y[idx[s]] = a
-    basis_state = {k: s for s, k in idx.items()}
+    st = _ref_rixs_setup(O, mod, es, psis)
     t_setup = time.perf_counter() - t0
-    memo_g = O._ColumnMemo(n, mod.hOp, mod.restrictions)
-    shared = {}
-    touts = mod.rixs_out_ops()
-    unit_times = []
-    first_unit = None
-    for k, wi in enumerate(w_in):
-        t0 = time.perf_counter()
-        a = scipy.sparse.csr_matrix(([wi + 1j * W["rixs"]["delta_in"] + es[0]] * len(idx),
-                                     (range(len(idx)), range(len(idx)))), shape=h.shape) - h
-        x, _ = scipy.sparse.linalg.bicgstab(a, y, rtol=1e-5)
-        psi2 = {basis_state[i]: amp for i, amp in enumerate(x) if amp != 0}
-        for top in touts:
-            psi3 = O.apply_op(n, top, psi2, W["slater_weight_min"], mod.restrictions, shared)
-            nrm = np.sqrt(O.norm2(psi3))
-            psi3 = {s: a / nrm for s, a in psi3.items()}
-            psi3 = {s: a for s, a in psi3.items() if abs(a) ** 2 >= W["slater_weight_min"]}
-            O.get_green(n, es[0], psi3, mod.hOp, w_loss, W["rixs"]["delta_loss"], W["krylov"],
-                        W["slater_weight_min"], mod.restrictions, memo=memo_g)
-        dt = time.perf_counter() - t0
-        if first_unit is None:
-            first_unit = dt
-        else:
-            unit_times.append(dt)
-        if time.perf_counter() - t_start > budget_s and len(unit_times) >= 2:
-            break
-    per_unit = statistics.mean(unit_times) if unit_times else first_unit
     n_units = 3 * ne * len(w_in)  # (t_in, eigenstate, w_in); each unit covers the 3 t_out
-    t_rixs = 3 * ne * t_setup + (first_unit - per_unit) + n_units * per_unit
+    n_setups = 3 * ne
+    if pool is None:
+        unit_times = []
+        first_unit = None
+        for wi in w_in:
+            t0 = time.perf_counter()
+            _ref_rixs_unit(O, st, wi, w_loss)
+            dt = time.perf_counter() - t0
+            if first_unit is None:
+                first_unit = dt
+            else:
+                unit_times.append(dt)
+            if time.perf_counter() - t_start > budget_s and len(unit_times) >= 2:
+                break
+        per_unit = statistics.mean(unit_times) if unit_times else first_unit
+        t_xas = xt[0] + (n_xas - 1) * t_xas_rest
+        t_rixs = n_setups * t_setup + (first_unit - per_unit) + n_units * per_unit
+        done = len(unit_times) + 1
+        cores = 1
+    else:
+        per_worker = pool.map(_ref_worker_units, [(r, procs, budget_s) for r in range(procs)])
+        first_unit = statistics.mean(t[0] for t in per_worker)
+        per_unit = statistics.mean(x for t in per_worker for x in t[1:])
+        done = sum(len(t) for t in per_worker)
+
+        def waves(count):
+            return -(-count // procs)
+
+        t_xas = xt[0] + (waves(n_xas) - 1) * t_xas_rest
+        t_rixs = waves(n_setups) * t_setup + (first_unit - per_unit) + waves(n_units) * per_unit
+        cores = procs
     total = t_gs + t_xas + t_rixs
-    sample = ("oracle on 1 core: full GS (%.2fs), 2 of %d XAS Green's functions, core-hole sector + %d of %d "
-              "RIXS (w_in, 3 t_out) units for one (t_in, state); extrapolated by unit counts"
-              % (t_gs, n_xas, len(unit_times) + 1, n_units))
+    if pool is None:
+        sample = ("oracle on 1 core: full GS (%.2fs), 2 of %d XAS Green's functions, core-hole sector + %d of %d "
+                  "RIXS (w_in, 3 t_out) units for one (t_in, state); extrapolated by unit counts"
+                  % (t_gs, n_xas, done, n_units))
+    else:
+        sample = ("oracle on %d cores: full GS (%.2fs, serial), 2 of %d XAS Green's functions, core-hole sector, "
+                  "%d timed RIXS (w_in, 3 t_out) units of one (t_in, state), run on all workers at once; the "
+                  "step's %d XAS runs, %d RIXS setups and %d RIXS units divided among the workers"
+                  % (cores, t_gs, n_xas, done, n_xas, n_setups, n_units))
     return total, sample, {"gs_s": t_gs, "xas_s": t_xas, "rixs_s": t_rixs}
 
 
@@ -834,13 +910,17 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    import multiprocessing
+
+    # every host core: one oracle process each (spawned: no CUDA state is inherited)
+    procs = max(1, os.cpu_count() or 1)
     steps = []
     sample = ""
-    for k in range(args.warmup + args.steps):
-        total, sample, parts = cpu_reference_time(args.cpu_sample_seconds)
-        if k >= args.warmup:
-            steps.append(total)
+    with multiprocessing.get_context("spawn").Pool(procs, initializer=_ref_worker_init) as pool:
+        for k in range(args.warmup + args.steps):
+            total, sample, parts = cpu_reference_time(args.cpu_sample_seconds, pool=pool, procs=procs)
+            if k >= args.warmup:
+                steps.append(total)
     value = statistics.mean(steps)
     line = {
         "impl": "reference",
@@ -857,7 +937,7 @@ def run_reference(args):
         "dtype": "c128",
         "data": "synthetic seeded model (numpy default_rng), no dataset",
         "config": dict(WORKLOAD, form="upstream algorithm (NumPy/SciPy oracle port)"),
-        "cpu_baseline": {"value": round(value, 3), "unit": "s", "cores": 1, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": round(value, 3), "unit": "s", "cores": procs, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
