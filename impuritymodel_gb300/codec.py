@@ -28,11 +28,14 @@ def bytes_to_words(states, n_spin_orbitals):
     if not states:
         return np.zeros((0, w), dtype=np.uint64)
     want = n_bytes(n_spin_orbitals)
-    if any(len(s) != want for s in states):
+    if set(map(len, states)) != {want}:
         raise ValueError("product states must all be %d bytes long" % want)
-    tail = b"\x00" * (nb - want)
-    buf = b"".join(s + tail for s in states) if tail else b"".join(states)
-    return np.frombuffer(buf, dtype=">u8").astype(np.uint64).reshape(len(states), w)
+    raw = np.frombuffer(b"".join(states), dtype=np.uint8).reshape(len(states), want)
+    if want != nb:  # zero-pad each state to whole words
+        padded = np.zeros((len(states), nb), dtype=np.uint8)
+        padded[:, :want] = raw
+        raw = padded
+    return raw.view(">u8").astype(np.uint64).reshape(len(states), w)
 
 
 def words_to_bytes(words, n_spin_orbitals):
