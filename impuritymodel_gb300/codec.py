@@ -73,6 +73,7 @@ def psi_to_arrays(psi, n_spin_orbitals):
 
 
 def arrays_to_psi(words, amps, n_spin_orbitals):
+    """(uint64[N, W], float64[N, 2]) -> dict {bytes: complex} in row order."""
     states = words_to_bytes(words, n_spin_orbitals)
-    a = np.asarray(amps, dtype=np.float64).reshape(-1, 2)
-    return {s: complex(x, y) for s, (x, y) in zip(states, a)}
+    a = np.ascontiguousarray(np.asarray(amps, dtype=np.float64).reshape(-1, 2))
+    return dict(zip(states, a.view(np.complex128).ravel().tolist()))
