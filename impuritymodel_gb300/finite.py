@@ -73,15 +73,18 @@ _OP_CACHE = {}
 
 
 def _device_op(op, eng):
-    key = (id(op), len(op), str(eng.device))
+    """The device term table of an operator dict, compiled once per dict and content: a dict
+    edited in place (a coefficient changed, a term added or removed) is compiled again."""
+    key = (id(op), str(eng.device))
+    items = tuple(op.items())
     hit = _OP_CACHE.get(key)
-    if hit is not None and hit[0] is op:
-        return hit[1]
+    if hit is not None and hit[0] is op and hit[1] == items:
+        return hit[2]
     d = DeviceOp(op, eng.device)
     eng.h2d_bytes += d.nbytes
     if len(_OP_CACHE) > 64:
         _OP_CACHE.clear()
-    _OP_CACHE[key] = (op, d)
+    _OP_CACHE[key] = (op, items, d)
     return d
 
 

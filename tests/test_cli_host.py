@@ -67,3 +67,27 @@ def test_popcount64_matches_python():
     x = rng.integers(0, 2**63, size=500, dtype=np.int64).astype(np.uint64) * np.uint64(2) + np.uint64(1)
     x[:3] = [0, np.uint64(0xFFFFFFFFFFFFFFFF), np.uint64(1) << np.uint64(63)]
     assert np.array_equal(_popcount64(x), [bin(int(v)).count("1") for v in x])
+
+
+def test_device_op_cache_follows_in_place_edits():
+    """The compiled operator is reused for the same dict and content only: changing a
+    coefficient, adding or removing a term in place recompiles it (upstream code may edit an
+    operator dict between calls)."""
+    import types
+
+    from impuritymodel_gb300 import finite, models
+
+    op = dict(models.make_model("config1").hOp)
+    eng = types.SimpleNamespace(device="cpu", h2d_bytes=0)
+    d1 = finite._device_op(op, eng)
+    assert finite._device_op(op, eng) is d1
+    key = next(iter(op))
+    op[key] = op[key] + 0.5
+    d2 = finite._device_op(op, eng)
+    assert d2 is not d1 and d2.coeff[0, 0].item() == d1.coeff[0, 0].item() + 0.5
+    del op[key]
+    d3 = finite._device_op(op, eng)
+    assert d3.n_terms == d1.n_terms - 1
+    new_key = next(k for k in (((i, "c"), (j, "a")) for i in range(26) for j in range(26)) if k not in op)
+    op[new_key] = 1.0
+    assert finite._device_op(op, eng).n_terms == d1.n_terms
