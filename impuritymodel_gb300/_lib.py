@@ -28,7 +28,6 @@ FILTER_NOT_IN_BASIS = 2
 ABI_VERSION = 2  # EDGPU_ABI_VERSION in include/edgpu.h
 MAX_RESTRICTIONS = 8
 MAX_WORDS = 8
-EDGPU_LANCZOS_NOALLOC_BYTES = 16 << 20  # size of the library's static scratch array
 
 # Exported symbols and their signatures (restype, argtypes).
 _P = C.c_void_p
@@ -100,6 +99,8 @@ SIGNATURES = {
     "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),
     "edgpu_launch_count": (C.c_longlong, []),
     "edgpu_lanczos_noalloc": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P]),
+    "edgpu_lanczos_noalloc_bytes": (_SZ, []),
+    "edgpu_lanczos_noalloc_forget": (None, []),
     "edgpu_lanczos_reorth_workspace": (_SZ, [_I64, _I]),
     "edgpu_lanczos_reorth": (_I, [C.POINTER(CSR), _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_lanczos_reorth_df": (_I, [C.POINTER(CSR), _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
@@ -165,6 +166,11 @@ def load(path=None):
     if path is None:
         _lib = lib
     return lib
+
+
+def noalloc_bytes():
+    """Size of the static scratch array of ``edgpu_lanczos_noalloc``, read from the library."""
+    return int(load().edgpu_lanczos_noalloc_bytes())
 
 
 def check(rc, where):

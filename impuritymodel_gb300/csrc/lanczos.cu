@@ -2087,6 +2087,8 @@ int noalloc_scratch_address(void** out) {
 extern "C" int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K,
                                      int precision, double* alpha, double* beta, int32_t* status_dev, void* stream) {
   if (!h || !v0 || R < 1 || K < 1 || !k_max || !alpha || !beta || !status_dev || h->n < 1) return EDGPU_ERR_ARG;
+  // the same precision values as edgpu_lanczos accepts
+  if (precision < 0 || precision > 3 || precision == 2) return EDGPU_ERR_ARG;
   if (precision == 3) precision = 0;  // the df64 form has no grid-wide variant
   if (precision == 0 && !h->val_c && !h->val_r) return EDGPU_ERR_ARG;
   if (precision != 0 && !h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
@@ -2103,4 +2105,11 @@ extern "C" int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R
   // the kernel that precedes their reader), so nothing has to be cleared between calls.
   if (precision == 0) return edgpu::lanczos_impl<double>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, bytes, s);
   return edgpu::lanczos_impl<float>(h, v0, R, k_max, K, alpha, beta, status_dev, ws, bytes, s);
+}
+
+extern "C" size_t edgpu_lanczos_noalloc_bytes(void) { return (size_t)EDGPU_LANCZOS_NOALLOC_BYTES; }
+
+extern "C" void edgpu_lanczos_noalloc_forget(void) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  for (int d = 0; d < kMaxDevices; ++d) g_noalloc_ptr[d] = nullptr;
 }

@@ -234,14 +234,26 @@ long long edgpu_launch_count(void);
  * EDGPU_ERR_WORKSPACE before anything runs.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress,
  * with that device current); make that first call before any stream capture.
+ * The looked-up address is cached per device index for the life of the process.  It is
+ * not valid after cudaDeviceReset or after the device's primary context is destroyed and
+ * created again: a caller that resets a device calls edgpu_lanczos_noalloc_forget() before
+ * the next edgpu_lanczos_noalloc, which then looks the address up again.
  * All calls share the one array: calls that overlap on the GPU (different streams, or
  * threads without ordering) race on it and must be serialised by the caller.  No part of
- * the scratch needs to start at zero.
+ * the scratch needs to start at zero.  precision: 0, 1 or 3 as in edgpu_lanczos (3 runs
+ * as 0 here); other values return EDGPU_ERR_ARG.
  * No counterpart in upstream impurityModel.
  */
 #define EDGPU_LANCZOS_NOALLOC_BYTES (16u << 20)
 int edgpu_lanczos_noalloc(const edgpu_csr* h, const double* v0, int R, const int32_t* k_max, int K, int precision,
                           double* alpha, double* beta, int32_t* status_dev, void* stream);
+/* Size in bytes of the static scratch array of edgpu_lanczos_noalloc
+ * (EDGPU_LANCZOS_NOALLOC_BYTES of the library that was built).  No counterpart upstream. */
+size_t edgpu_lanczos_noalloc_bytes(void);
+/* Drops the cached device addresses of that array (all devices); the next
+ * edgpu_lanczos_noalloc on a device looks its address up again.  Call it after a device
+ * reset.  No counterpart in upstream impurityModel. */
+void edgpu_lanczos_noalloc_forget(void);
 
 /*
  * Lanczos with full (twice classical Gram-Schmidt) reorthogonalisation, one run, complex128,

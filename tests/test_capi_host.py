@@ -56,6 +56,38 @@ def test_entry_points_reject_bad_arguments_without_a_gpu(lib):
     assert lib.edgpu_cfrac(None, None, None, 1, 1, None, 1, 0.1, None, None, None, None) == L.EDGPU_ERR_ARG
 
 
+def test_noalloc_rejects_bad_arguments_without_a_gpu(lib):
+    """edgpu_lanczos_noalloc validates its arguments before any CUDA call: bad precision,
+    missing outputs and problems larger than the static scratch array return their codes.
+    The pointers below are never dereferenced (host-side stand-ins)."""
+    import ctypes as C
+
+    from impuritymodel_gb300 import _lib as L
+
+    fake = C.c_void_p(0x1000)
+    csr = L.CSR()
+    csr.n, csr.nnz = 1000, 3000
+    csr.row_ptr = csr.col = csr.val_r = csr.val_rf = 0x1000
+    size = L.noalloc_bytes()
+    assert size == lib.edgpu_lanczos_noalloc_bytes() and size > 0
+
+    def call(R=2, K=10, precision=0, alpha=fake, beta=fake, status=fake):
+        return lib.edgpu_lanczos_noalloc(C.byref(csr), fake, R, fake, K, precision, alpha, beta, status, None)
+
+    for bad in (-1, 2, 4, 7):
+        assert call(precision=bad) == L.EDGPU_ERR_ARG
+    assert call(alpha=None) == L.EDGPU_ERR_ARG
+    assert call(beta=None) == L.EDGPU_ERR_ARG
+    assert call(status=None) == L.EDGPU_ERR_ARG
+    assert call(R=0) == L.EDGPU_ERR_ARG
+    for prec in (0, 1, 3):
+        big_r = 1
+        while lib.edgpu_lanczos_workspace(csr.n, big_r, 10, 0 if prec == 3 else prec) <= size:
+            big_r *= 2
+        assert call(R=big_r, precision=prec) == L.EDGPU_ERR_WORKSPACE
+    lib.edgpu_lanczos_noalloc_forget()  # no device state is touched
+
+
 def test_operator_compilation():
     from impuritymodel_gb300.engine import DeviceOp
 

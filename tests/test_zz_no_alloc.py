@@ -89,7 +89,7 @@ def test_noalloc_lanczos_matches_workspace_entry_point(precision, complex_vals):
 
     a_ref, b_ref, st = outputs()
     ws_bytes = lib.edgpu_lanczos_workspace(n, R, K, precision)
-    assert ws_bytes <= L.EDGPU_LANCZOS_NOALLOC_BYTES
+    assert ws_bytes <= L.noalloc_bytes()
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     rc = lib.edgpu_lanczos(C.byref(csr), C.c_void_p(v0_t.data_ptr()), R, C.c_void_p(kmax.data_ptr()), K, precision,
                            C.c_void_p(a_ref.data_ptr()), C.c_void_p(b_ref.data_ptr()), C.c_void_p(st.data_ptr()),
@@ -110,7 +110,7 @@ def test_noalloc_lanczos_matches_workspace_entry_point(precision, complex_vals):
                                    atol=RTOL)
     # a problem whose scratch exceeds the static array is rejected before anything runs
     big_r = 4096
-    assert lib.edgpu_lanczos_workspace(n, big_r, K, precision) > L.EDGPU_LANCZOS_NOALLOC_BYTES
+    assert lib.edgpu_lanczos_workspace(n, big_r, K, precision) > L.noalloc_bytes()
     rc = lib.edgpu_lanczos_noalloc(C.byref(csr), C.c_void_p(v0_t.data_ptr()), big_r, C.c_void_p(kmax.data_ptr()), K,
                                    precision, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
                                    C.c_void_p(st2.data_ptr()), stream)
