@@ -662,7 +662,7 @@ class Engine:
                                      _ptr(e_t), _ptr(sc), _ptr(torch.view_as_real(g)), self.stream), "cfrac")
         return g
 
-    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16, precision=0, remaining=None):
+    def krylov_reorth(self, csr, v0, k_cap, stop=None, chunk=16, precision=0, remaining=None, locked=None):
         """Lanczos with full reorthogonalisation from v0 (normalised, [N] complex128).
 
         ``stop(alpha, beta, j)`` (host arrays of length j) returns True when converged.
@@ -671,22 +671,35 @@ class Engine:
         the next Krylov vector (0 when the space is exhausted).  ``precision=3`` runs the
         recurrence in double-float arithmetic (real H up to 65536 rows; otherwise FP64); V is
         returned in complex128 either way.  ``remaining(j)`` (optional) estimates the steps
-        still needed after step j; the chunk queued ahead of each convergence test is then cut
+        still needed after step j; the chunk queued ahead of each convergence test is cut
         to that estimate (at least 8 steps), so little work runs past convergence.
+
+        ``locked`` ([m, N] complex128, orthonormal, optional): vectors every new Krylov vector
+        is orthogonalised against (deflation).  They are placed ahead of v0 in the Krylov
+        basis with a zero coupling, so the Gram-Schmidt passes of every step remove their
+        components and the recurrence runs on the orthogonal complement; v0 must be
+        orthogonal to them.  The deflated recurrence runs in FP64.
         """
         n = csr.n
         if csr.ncols != n or v0.numel() != n:
             raise ValueError("krylov_reorth: square matrix and start vector of matching size required")
-        k_cap = int(min(k_cap, n))
-        df = precision == 3 and csr.val_c is None and csr.val_r is not None and n <= (1 << 16)
+        m = 0 if locked is None else int(locked.shape[0])
+        k_cap = int(min(k_cap, n - m))
+        if k_cap < 1:
+            raise ValueError("krylov_reorth: no room for a Krylov vector beside the locked ones")
+        K_tot = m + k_cap
+        df = m == 0 and precision == 3 and csr.val_c is None and csr.val_r is not None and n <= (1 << 16)
         if df:
             csr.double_float()
         launch = self.lib.edgpu_lanczos_reorth_df if df else self.lib.edgpu_lanczos_reorth
-        V = torch.zeros((k_cap, n), dtype=torch.complex128, device=self.device)
+        V = torch.zeros((K_tot, n), dtype=torch.complex128, device=self.device)
         w = torch.zeros(n, dtype=torch.complex128, device=self.device)
-        alpha = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
-        beta = torch.zeros(k_cap, dtype=torch.float64, device=self.device)
-        ws, wsn = self.workspace(self.lib.edgpu_lanczos_reorth_workspace(n, k_cap))
+        alpha = torch.zeros(K_tot, dtype=torch.float64, device=self.device)
+        beta = torch.zeros(K_tot, dtype=torch.float64, device=self.device)
+        if m:
+            V[:m] = locked
+            V[m] = v0
+        ws, wsn = self.workspace(self.lib.edgpu_lanczos_reorth_workspace(n, K_tot))
         v0r = torch.view_as_real(v0.contiguous())
         # one pinned device-to-host copy per chunk (status, alpha and beta together), read
         # through an event, so the next chunk is already queued while the host tests this
@@ -694,11 +707,12 @@ class Engine:
         host_t = torch.empty(1 + 2 * k_cap, dtype=torch.float64, pin_memory=True)
 
         def enqueue(j0, j1):
+            # j0, j1 count the run's own steps; the kernel sees them after the locked vectors
             self.reset_status()
-            L.check(launch(C.byref(csr.struct()), _ptr(v0r), j0, j1, k_cap, _ptr(torch.view_as_real(V)),
+            L.check(launch(C.byref(csr.struct()), _ptr(v0r), m + j0, m + j1, K_tot, _ptr(torch.view_as_real(V)),
                            _ptr(torch.view_as_real(w)), _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn,
                            self.stream), "lanczos_reorth")
-            host_t[: 1 + 2 * j1].copy_(torch.cat([self.status.to(torch.float64), alpha[:j1], beta[:j1]]),
+            host_t[: 1 + 2 * j1].copy_(torch.cat([self.status.to(torch.float64), alpha[m:m + j1], beta[m:m + j1]]),
                                        non_blocking=True)
             ev = torch.cuda.Event()
             ev.record()
@@ -722,14 +736,14 @@ class Engine:
             if st == L.EDGPU_ERR_BREAKDOWN:
                 # invariant subspace: the Krylov space is exact at the first zero beta
                 kb = int(np.argmax(bh == 0.0)) + 1
-                return (_df_to_c128(V[:kb]) if df else V[:kb]), ah[:kb], bh[:kb]
+                return (_df_to_c128(V[:kb]) if df else V[m:m + kb]), ah[:kb], bh[:kb]
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "lanczos_reorth")
             j = j1
             if ev_next is None or (stop is not None and stop(ah, bh, j)):
                 break
             j1, ev = jn, ev_next
-        return (_df_to_c128(V[:j]) if df else V[:j]), ah[:j], bh[:j]
+        return (_df_to_c128(V[:j]) if df else V[m:m + j]), ah[:j], bh[:j]
 
     def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0, check=True):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).

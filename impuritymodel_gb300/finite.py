@@ -471,42 +471,43 @@ def get_tridiagonal_krylov_vectors(h, psi0, krylovSize, h_local=False, mode="spa
     return alpha[0, :k].cpu().numpy(), beta[0, : k - 1].cpu().numpy()
 
 
-def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
-    """Lowest ``k`` eigenpairs by Lanczos with full reorthogonalisation (FP64 on the GPU;
-    double-float arithmetic for a real H with ``precision=3``).
+def _ritz_run(eng, csr, v0, want, k_cap, tol_rel, precision=0, locked=None, q_cap=None):
+    """One reorthogonalised Lanczos run from v0 until the Ritz pairs it wants have converged.
 
-    Ritz values come from the Krylov tridiagonal matrix on the host each chunk; iteration
-    stops when every wanted residual ``beta_j |s_{j,i}|`` is below
-    ``tol_rel * max(1, |theta_i|)`` or the Krylov space spans the basis.
-    Returns (energies [k] ascending, eigenvectors [k, N] complex128 device tensor).
-    """
+    ``want(theta)`` gives how many of the lowest Ritz pairs must have converged (``theta``:
+    the current lowest Ritz values, ascending); a pair has converged when its residual
+    ``beta_j |s_{j,i}|`` is below ``tol_rel * max(1, |theta_i|)``.  The Krylov space grows
+    (its cap doubling) until they have or until it spans the sector (or, with ``locked``
+    vectors, their orthogonal complement).  ``q_cap`` bounds ``want`` (the number of Ritz
+    values it is shown).  Returns (theta [q] ascending, Ritz vectors [q, N] complex128
+    device tensor) for the q wanted pairs."""
     n = csr.n
-    k = min(k, n)
-    k_cap = int(min(n, k_cap or max(300, 4 * k + 100)))
-    g = torch.Generator(device=eng.device)
-    g.manual_seed(seed)
-    v0 = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
-    v0 = v0 / torch.linalg.vector_norm(v0)
+    m = 0 if locked is None else int(locked.shape[0])
+    room = n - m
+    k_cap = int(min(room, k_cap))
 
-    def ritz(a, bfull):
-        # the lowest min(k, j) Ritz pairs only (all that the stop test and the result use)
+    def ritz(a, bfull, q):
+        # the lowest min(q, j) Ritz pairs only (all that the stop test and the result use)
         if len(a) == 1:
             return np.array(a, dtype=float), np.ones((1, 1))
-        return scipy.linalg.eigh_tridiagonal(a, bfull[: len(a) - 1], select="i", select_range=(0, min(k, len(a)) - 1))
+        return scipy.linalg.eigh_tridiagonal(a, bfull[: len(a) - 1], select="i", select_range=(0, min(q, len(a)) - 1))
 
-    def residuals(a, bfull, j):
-        th, s = ritz(a, bfull)
-        if j >= n:
-            return th, s, np.zeros(min(k, j))
-        return th, s, np.abs(bfull[j - 1] * s[-1, : min(k, j)])
+    def residuals(a, bfull, j, q):
+        th, s = ritz(a, bfull, q)
+        if j >= room:
+            return th, s, np.zeros(min(q, j))
+        return th, s, np.abs(bfull[j - 1] * s[-1, : min(q, j)])
 
     history = []  # (j, log of the worst residual / tolerance ratio) at each convergence test
+    q_max = max(1, min(room, q_cap or room))
 
     def stop(a, bfull, j):
-        if j < k:
+        th, _, _ = residuals(a, bfull, j, min(q_max, len(a)))
+        q = min(want(th), len(a))
+        if j < q or q < 1:
             return False
-        th, _, res = residuals(a, bfull, j)
-        ratio = res / (tol_rel * np.maximum(1.0, np.abs(th[:k])))
+        th, _, res = residuals(a, bfull, j, q)
+        ratio = res[:q] / (tol_rel * np.maximum(1.0, np.abs(th[:q])))
         history.append((j, float(np.log(max(ratio.max(), 1e-300)))))
         return bool(np.all(ratio <= 1.0))
 
@@ -523,19 +524,77 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0):
 
     while True:
         V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32, precision=precision,
-                                        remaining=remaining)
+                                        remaining=remaining, locked=locked)
         kk = len(a)
-        th, s, res = residuals(a, bfull, kk)
-        exact = kk >= n or (kk < k_cap and bfull[kk - 1] == 0.0)
-        if exact or stop(a, bfull, kk) or k_cap >= n:
+        exact = kk >= room or (kk < k_cap and bfull[kk - 1] == 0.0)
+        if exact or stop(a, bfull, kk) or k_cap >= room:
             break
-        k_cap = min(n, 2 * k_cap)
-    kk = len(a)
-    kw = min(k, kk)
-    coeffs = np.ascontiguousarray(s[:, :kw]).astype(np.complex128)
+        k_cap = min(room, 2 * k_cap)
+    th, _, _ = residuals(a, bfull, kk, min(q_max, kk))
+    q = max(1, min(want(th), kk))
+    th, s, _ = residuals(a, bfull, kk, q)
+    coeffs = np.ascontiguousarray(s[:, :q]).astype(np.complex128)
     X = eng.combine(V, coeffs)
     X = X / torch.linalg.vector_norm(X, dim=1, keepdim=True)
-    return th[:kw], X
+    return th[:q], X
+
+
+def _project_out(X, v):
+    """v minus its components along the (orthonormal) rows of X, twice (classical
+    Gram-Schmidt twice is orthogonal to working precision)."""
+    for _ in range(2):
+        v = v - X.t() @ (X.conj() @ v)
+    return v
+
+
+def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0, complete_multiplets=True):
+    """Lowest ``k`` eigenpairs by Lanczos with full reorthogonalisation (FP64 on the GPU;
+    double-float arithmetic for a real H with ``precision=3``), counted with multiplicity.
+
+    Ritz values come from the Krylov tridiagonal matrix on the host each chunk; iteration
+    stops when every wanted residual ``beta_j |s_{j,i}|`` is below
+    ``tol_rel * max(1, |theta_i|)`` or the Krylov space spans the basis.
+
+    One Krylov space holds a single vector of each eigenspace, so an exactly degenerate
+    eigenvalue shows up once.  With ``complete_multiplets`` (upstream's eigsh(k) returns the
+    copies too, finite.py:105) further runs start from random vectors orthogonal to the
+    pairs found, with those pairs locked (deflated) in their Gram-Schmidt passes; each run
+    converges its Ritz pairs below the current k-th energy and the first one above it, and
+    any pair below the k-th energy joins the result.  The runs end when one finds nothing
+    below it.
+    Returns (energies [k] ascending, eigenvectors [k, N] complex128 device tensor).
+    """
+    n = csr.n
+    k = min(k, n)
+    k_cap = int(min(n, k_cap or max(300, 4 * k + 100)))
+    g = torch.Generator(device=eng.device)
+    g.manual_seed(seed)
+    v0 = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
+    v0 = v0 / torch.linalg.vector_norm(v0)
+    th, X = _ritz_run(eng, csr, v0, lambda t: k, k_cap, tol_rel, precision, q_cap=k)
+    if not complete_multiplets:
+        return th, X
+    while X.shape[0] < n:
+        thr = th[-1] if len(th) >= k else np.inf
+        v = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
+        v = _project_out(X, v)
+        nv = torch.linalg.vector_norm(v)
+        v = v / nv
+
+        def want(t, thr=thr):
+            below = int(np.sum(t < thr - tol_rel * max(1.0, abs(thr))))
+            return min(k, below + 1)
+
+        th2, X2 = _ritz_run(eng, csr, v, want, max(64, min(k_cap, 4 * k + 60)), tol_rel, 0, locked=X, q_cap=k + 1)
+        new = th2 < thr - tol_rel * max(1.0, abs(thr)) if np.isfinite(thr) else np.ones(len(th2), dtype=bool)
+        if not new.any():
+            break
+        th_all = np.concatenate([th, th2[new]])
+        X_all = torch.cat([X, X2[torch.from_numpy(np.nonzero(new)[0]).to(X.device)]], 0)
+        order = np.argsort(th_all, kind="stable")[:k]
+        th = th_all[order]
+        X = X_all[torch.from_numpy(order).to(X.device)]
+    return th, X
 
 
 def eigensystem_device(eng, dop, sb, nPsiMax, eigenValueTol=1e-9, slaterWeightMin=1e-7, precision=0,

@@ -392,20 +392,32 @@ def getGreen(n_spin_orbitals, e, psi, hOp, omega, delta, krylovSize, slaterWeigh
     r"""``<psi|((omega + i delta + e) - H)^{-1}|psi>`` (upstream spectra.py:551-681).
 
     ``psi`` is used as given (upstream does not normalise inside getGreen).  ``h_dict`` is
-    accepted for signature compatibility; the sector is built on the device.
+    upstream's in/out memo ``{state: H|state>}``: as upstream's expand_basis_and_hamiltonian
+    (finite.py:1806-1894) the closure reuses the outputs stored for states already in it,
+    and every state of the closure without an entry gets one (``applyOp(hOp, {b: 1},
+    restrictions=...)``, computed on the device), in breadth-first order.
     """
     omega = np.asarray(omega)
     if len(psi) == 0:
         return np.zeros(len(omega), dtype=complex)
     if mode not in ("sparse", "dense", "dict"):
         raise Exception("Value of variable 'mode' is incorrect.")
+    from .finite import _expand_device, _fill_h_dict
+
     eng = get_engine()
     n = int(n_spin_orbitals)
     words_for(n)
     dop = _device_op(hOp, eng)
     restr = make_restrictions(restrictions, n)
-    s_t, a_t = _psi_tensors(eng, psi, n)
-    g = green_batch(eng, dop, restr, [s_t], [a_t], [e], omega, delta, krylovSize, precision, normalize=False)
+    words, amps = codec.psi_to_arrays(psi, n)
+    s_t, a_t = eng.upload_states(words), eng.to_device(amps)
+    sector = None
+    if h_dict is not None:
+        s_sorted, order = _expand_device(eng, n, dop, restr, words, h_dict)
+        sector = Sector.from_parts(s_sorted, eng.build_csr(s_sorted, dop, restr))
+        _fill_h_dict(eng, n, dop, restr, order, h_dict)
+    g = green_batch(eng, dop, restr, [s_t], [a_t], [e], omega, delta, krylovSize, precision, sector=sector,
+                    normalize=False)
     return eng.to_host(g[0])
 
 

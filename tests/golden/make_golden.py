@@ -302,8 +302,69 @@ def nio_cli():
     print("nio cli done: %d h0 terms" % len(keys))
 
 
+def dropin():
+    """Upstream's drop-in functions on the seeded models, for the parity tests of the same
+    functions here: get_basis of the 66-spin-orbital model (finite.py:294-374),
+    get_hamiltonian_matrix_from_h_dict on an h_dict that expand_basis filled
+    (finite.py:1613-1693, 1696-1803), getGreen with the h_dict it fills (spectra.py:551-681),
+    and eigensystem of the 26-spin-orbital model without a magnetic field and without 3d
+    spin-orbit coupling, whose ground multiplet is an exactly degenerate spin triplet
+    (finite.py:58-118, eigsh k=nPsiMax)."""
+    import contextlib
+
+    finite, spectra, psr, create, remove = refenv.load()
+    from tests.golden.fixtures import decode_psi, load
+
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    out = {}
+    mod2 = M.make_model("config2")
+    n2 = mod2.n_spin_orbitals
+    with quiet:
+        basis2 = finite.get_basis(*mod2.basis_args())
+    out["basis2"] = encode_states(list(basis2), n2)
+    # h_dict from expand_basis, then the matrix built from it
+    mod = M.make_model("config1")
+    n = mod.n_spin_orbitals
+    z = load("config1.npz")
+    psi1 = decode_psi(z, "psi1", n)
+    h_dict = {}
+    with quiet:
+        exp_basis = finite.expand_basis(n, h_dict, mod.hOp, tuple(psi1.keys()), mod.restrictions)
+        hx, bidx = finite.get_hamiltonian_matrix_from_h_dict(h_dict, exp_basis)
+    keys = list(h_dict.keys())
+    out["hd_keys"] = encode_states(keys, n)
+    out["hd_ptr"] = np.cumsum([0] + [len(h_dict[k]) for k in keys])
+    out["hd_out"] = encode_states([s for k in keys for s in h_dict[k]], n)
+    out["hd_val"] = np.array([complex(v) for k in keys for v in h_dict[k].values()], dtype=np.complex128)
+    out["hd_basis"] = encode_states(list(exp_basis), n)
+    hc = hx.tocoo()
+    out["hd_row"], out["hd_col"], out["hd_h"] = hc.row, hc.col, hc.data
+    # getGreen on the normalised psi1 with a fresh h_dict (filled by upstream)
+    nrm = np.sqrt(finite.norm2(psi1))
+    psin = {s_: a / nrm for s_, a in psi1.items()}
+    w = np.linspace(-25, 25, 500)
+    g_dict = {}
+    with quiet:
+        g = spectra.getGreen(n, float(z["es"][0]), psin, mod.hOp, w, 0.1, 150, 1e-7, mod.restrictions, g_dict)
+    out["green_w"] = w
+    out["green_g"] = g
+    out["green_keys"] = encode_states(list(g_dict.keys()), n)
+    out["green_nout"] = np.array([len(v) for v in g_dict.values()])
+    # exactly degenerate ground multiplet: no magnetic field and no 3d spin-orbit coupling,
+    # so the d8 ground state is a spin triplet (three equal energies)
+    mod0 = M.make_model("config1", hfield=(0.0, 0.0, 0.0), xi_3d=0.0)
+    with quiet:
+        basis0 = finite.get_basis(*mod0.basis_args())
+        es0, psis0 = finite.eigensystem(n, mod0.hOp, basis0, 6)
+    out["deg_es"] = np.asarray(es0)
+    np.savez_compressed(os.path.join(HERE, "dropin.npz"), **out)
+    print("dropin done: basis2 %d, h_dict %d, deg es %s" % (len(basis2), len(keys), np.round(es0, 6)))
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["nio_cli"]:
+    if sys.argv[1:] == ["dropin"]:
+        dropin()
+    elif sys.argv[1:] == ["nio_cli"]:
         nio_cli()
     elif sys.argv[1:] == ["observables"]:
         observables()
@@ -314,3 +375,4 @@ if __name__ == "__main__":
         observables()
         simulate()
         nio_cli()
+        dropin()
