@@ -178,6 +178,16 @@ def _df_to_c128(v):
     f = torch.view_as_real(v).contiguous().view(torch.float32).view(*v.shape, 4).to(torch.float64)
     return torch.complex(f[..., 0] + f[..., 1], f[..., 2] + f[..., 3])
 
+def _c128_to_df(v):
+    """complex128 values -> a complex128-sized buffer of double-float elements (re.hi, re.lo,
+    im.hi, im.lo as float32; hi + lo equals the value to about 2^-48 relative)."""
+    r = torch.view_as_real(v.contiguous())
+    hi = r.to(torch.float32)
+    lo = (r - hi.to(torch.float64)).to(torch.float32)
+    f = torch.stack([hi[..., 0], lo[..., 0], hi[..., 1], lo[..., 1]], -1).contiguous()
+    return torch.view_as_complex(f.view(torch.float64).view(*v.shape, 2))
+
+
 # raw handle of the current stream without building a torch Stream object (about 10 us less
 # per library call); the public accessor is the fallback
 _raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
@@ -676,9 +686,9 @@ class Engine:
 
         ``locked`` ([m, N] complex128, orthonormal, optional): vectors every new Krylov vector
         is orthogonalised against (deflation).  They are placed ahead of v0 in the Krylov
-        basis with a zero coupling, so the Gram-Schmidt passes of every step remove their
-        components and the recurrence runs on the orthogonal complement; v0 must be
-        orthogonal to them.  The deflated recurrence runs in FP64.
+        basis with a negligible coupling, so the Gram-Schmidt passes of every step remove
+        their components and the recurrence runs on the orthogonal complement; v0 must be
+        orthogonal to them.
         """
         n = csr.n
         if csr.ncols != n or v0.numel() != n:
@@ -688,7 +698,7 @@ class Engine:
         if k_cap < 1:
             raise ValueError("krylov_reorth: no room for a Krylov vector beside the locked ones")
         K_tot = m + k_cap
-        df = m == 0 and precision == 3 and csr.val_c is None and csr.val_r is not None and n <= (1 << 16)
+        df = precision == 3 and csr.val_c is None and csr.val_r is not None and n <= (1 << 16)
         if df:
             csr.double_float()
         launch = self.lib.edgpu_lanczos_reorth_df if df else self.lib.edgpu_lanczos_reorth
@@ -696,9 +706,19 @@ class Engine:
         w = torch.zeros(n, dtype=torch.complex128, device=self.device)
         alpha = torch.zeros(K_tot, dtype=torch.float64, device=self.device)
         beta = torch.zeros(K_tot, dtype=torch.float64, device=self.device)
-        if m:
+        if m and not df:
+            # step m reads v_m = V[m]; beta_{m-1} = 0 leaves the locked vectors out of the
+            # three-term update (the Gram-Schmidt passes remove their components)
             V[:m] = locked
             V[m] = v0
+        elif m:
+            # the double-float step m forms v_m = w / beta_{m-1} itself: w = 2^-60 v0 with
+            # beta_{m-1} = 2^-60 gives v0 exactly (powers of two), and the three-term update
+            # then subtracts only 2^-60 of V[m-1]
+            tiny = 2.0 ** -60
+            V[:m] = _c128_to_df(locked)
+            w.copy_(_c128_to_df(v0 * tiny))
+            beta[m - 1] = tiny
         ws, wsn = self.workspace(self.lib.edgpu_lanczos_reorth_workspace(n, K_tot))
         v0r = torch.view_as_real(v0.contiguous())
         # one pinned device-to-host copy per chunk (status, alpha and beta together), read
@@ -736,14 +756,14 @@ class Engine:
             if st == L.EDGPU_ERR_BREAKDOWN:
                 # invariant subspace: the Krylov space is exact at the first zero beta
                 kb = int(np.argmax(bh == 0.0)) + 1
-                return (_df_to_c128(V[:kb]) if df else V[m:m + kb]), ah[:kb], bh[:kb]
+                return (_df_to_c128(V[m:m + kb]) if df else V[m:m + kb]), ah[:kb], bh[:kb]
             if st != L.EDGPU_OK:
                 raise L.EdgpuError(st, "lanczos_reorth")
             j = j1
             if ev_next is None or (stop is not None and stop(ah, bh, j)):
                 break
             j1, ev = jn, ev_next
-        return (_df_to_c128(V[:j]) if df else V[m:m + j]), ah[:j], bh[:j]
+        return (_df_to_c128(V[m:m + j]) if df else V[m:m + j]), ah[:j], bh[:j]
 
     def shifted_solve(self, csr, Y, zs, tol, k_cap, precision=0, check=True):
         """X[r, z] = (zs[r, z] - H)^{-1} Y[r] for all right-hand sides (one launch set).

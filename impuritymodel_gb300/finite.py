@@ -471,20 +471,23 @@ def get_tridiagonal_krylov_vectors(h, psi0, krylovSize, h_local=False, mode="spa
     return alpha[0, :k].cpu().numpy(), beta[0, : k - 1].cpu().numpy()
 
 
-def _ritz_run(eng, csr, v0, want, k_cap, tol_rel, precision=0, locked=None, q_cap=None):
+def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=None):
     """One reorthogonalised Lanczos run from v0 until the Ritz pairs it wants have converged.
 
-    ``want(theta)`` gives how many of the lowest Ritz pairs must have converged (``theta``:
-    the current lowest Ritz values, ascending); a pair has converged when its residual
-    ``beta_j |s_{j,i}|`` is below ``tol_rel * max(1, |theta_i|)``.  The Krylov space grows
-    (its cap doubling) until they have or until it spans the sector (or, with ``locked``
-    vectors, their orthogonal complement).  ``q_cap`` bounds ``want`` (the number of Ritz
-    values it is shown).  Returns (theta [q] ascending, Ritz vectors [q, N] complex128
-    device tensor) for the q wanted pairs."""
+    A Ritz pair (theta_i, residual ``r_i = beta_j |s_{j,i}|``) has converged when
+    ``r_i <= tol_rel * max(1, |theta_i|)``.  Without ``thr`` the lowest ``k`` pairs are
+    wanted.  With ``thr`` (a deflated run) the pairs below ``thr`` are wanted, at most
+    ``k``: the run stops once every Ritz pair up to the first one that lies above ``thr``
+    by more than its residual (and beyond the tolerance) has converged.  The Krylov space
+    grows (its cap doubling) until then or until it spans the sector (or, with ``locked``
+    vectors, their orthogonal complement).  Returns (theta [q] ascending, Ritz vectors
+    [q, N] complex128 device tensor) of the q wanted pairs."""
     n = csr.n
     m = 0 if locked is None else int(locked.shape[0])
     room = n - m
     k_cap = int(min(room, k_cap))
+    q_max = max(1, min(room, k + (0 if thr is None else 1)))
+    tol_thr = 0.0 if thr is None else tol_rel * max(1.0, abs(thr))
 
     def ritz(a, bfull, q):
         # the lowest min(q, j) Ritz pairs only (all that the stop test and the result use)
@@ -499,17 +502,30 @@ def _ritz_run(eng, csr, v0, want, k_cap, tol_rel, precision=0, locked=None, q_ca
         return th, s, np.abs(bfull[j - 1] * s[-1, : min(q, j)])
 
     history = []  # (j, log of the worst residual / tolerance ratio) at each convergence test
-    q_max = max(1, min(room, q_cap or room))
+
+    def converged(th, res):
+        tol = tol_rel * np.maximum(1.0, np.abs(th))
+        if thr is None:
+            if len(th) < k:
+                return False, 0.0
+            ratio = res[:k] / tol[:k]
+            return bool(np.all(ratio <= 1.0)), float(ratio.max())
+        worst = 0.0
+        for i in range(len(th)):
+            if th[i] - res[i] > thr + tol_thr:
+                return True, worst  # this pair and the ones above it lie above the threshold
+            if i >= k:
+                return True, worst
+            worst = max(worst, res[i] / tol[i])
+            if res[i] > tol[i]:
+                return False, worst
+        return len(th) >= q_max, worst
 
     def stop(a, bfull, j):
-        th, _, _ = residuals(a, bfull, j, min(q_max, len(a)))
-        q = min(want(th), len(a))
-        if j < q or q < 1:
-            return False
-        th, _, res = residuals(a, bfull, j, q)
-        ratio = res[:q] / (tol_rel * np.maximum(1.0, np.abs(th[:q])))
-        history.append((j, float(np.log(max(ratio.max(), 1e-300)))))
-        return bool(np.all(ratio <= 1.0))
+        th, _, res = residuals(a, bfull, j, q_max)
+        ok, worst = converged(th, res)
+        history.append((j, float(np.log(max(worst, 1e-300)))))
+        return ok
 
     def remaining(j):
         # steps still needed after step j, extrapolating the geometric residual decay of the
@@ -530,9 +546,10 @@ def _ritz_run(eng, csr, v0, want, k_cap, tol_rel, precision=0, locked=None, q_ca
         if exact or stop(a, bfull, kk) or k_cap >= room:
             break
         k_cap = min(room, 2 * k_cap)
-    th, _, _ = residuals(a, bfull, kk, min(q_max, kk))
-    q = max(1, min(want(th), kk))
-    th, s, _ = residuals(a, bfull, kk, q)
+    th, s, _ = residuals(a, bfull, kk, q_max)
+    q = min(k, len(th)) if thr is None else int(np.sum(th[:k] < thr - tol_thr))
+    if q == 0:
+        return th[:0], None
     coeffs = np.ascontiguousarray(s[:, :q]).astype(np.complex128)
     X = eng.combine(V, coeffs)
     X = X / torch.linalg.vector_norm(X, dim=1, keepdim=True)
@@ -559,9 +576,9 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0, comp
     eigenvalue shows up once.  With ``complete_multiplets`` (upstream's eigsh(k) returns the
     copies too, finite.py:105) further runs start from random vectors orthogonal to the
     pairs found, with those pairs locked (deflated) in their Gram-Schmidt passes; each run
-    converges its Ritz pairs below the current k-th energy and the first one above it, and
-    any pair below the k-th energy joins the result.  The runs end when one finds nothing
-    below it.
+    converges its Ritz pairs below the current k-th energy and stops at the first one that
+    lies above it by more than its residual; the pairs below the k-th energy join the
+    result.  The runs end when one finds nothing below it.
     Returns (energies [k] ascending, eigenvectors [k, N] complex128 device tensor).
     """
     n = csr.n
@@ -571,26 +588,20 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0, comp
     g.manual_seed(seed)
     v0 = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
     v0 = v0 / torch.linalg.vector_norm(v0)
-    th, X = _ritz_run(eng, csr, v0, lambda t: k, k_cap, tol_rel, precision, q_cap=k)
+    th, X = _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision)
     if not complete_multiplets:
         return th, X
     while X.shape[0] < n:
         thr = th[-1] if len(th) >= k else np.inf
         v = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
         v = _project_out(X, v)
-        nv = torch.linalg.vector_norm(v)
-        v = v / nv
-
-        def want(t, thr=thr):
-            below = int(np.sum(t < thr - tol_rel * max(1.0, abs(thr))))
-            return min(k, below + 1)
-
-        th2, X2 = _ritz_run(eng, csr, v, want, max(64, min(k_cap, 4 * k + 60)), tol_rel, 0, locked=X, q_cap=k + 1)
-        new = th2 < thr - tol_rel * max(1.0, abs(thr)) if np.isfinite(thr) else np.ones(len(th2), dtype=bool)
-        if not new.any():
+        v = v / torch.linalg.vector_norm(v)
+        th2, X2 = _ritz_run(eng, csr, v, k, max(64, min(k_cap, 4 * k + 60)), tol_rel, precision, locked=X,
+                            thr=float(thr) if np.isfinite(thr) else 1e300)
+        if len(th2) == 0:
             break
-        th_all = np.concatenate([th, th2[new]])
-        X_all = torch.cat([X, X2[torch.from_numpy(np.nonzero(new)[0]).to(X.device)]], 0)
+        th_all = np.concatenate([th, th2])
+        X_all = torch.cat([X, X2], 0)
         order = np.argsort(th_all, kind="stable")[:k]
         th = th_all[order]
         X = X_all[torch.from_numpy(order).to(X.device)]

@@ -60,10 +60,13 @@ def test_eigensystem_returns_every_copy_of_degenerate_levels(eng, precision):
     # two triplets: three copies each
     assert np.abs(es[:3] - es[0]).max() < 1e-8 and np.abs(es[3:] - es[3]).max() < 1e-8
     assert es[3] - es[0] > 1e-2
-    # upstream's own call found two copies of each: each of its energies is one of ours
+    # upstream's own call found two copies of each triplet (and then higher levels): each of
+    # its energies is an eigenvalue, but the lowest six counted with multiplicity are ours
     up = load("dropin.npz")["deg_es"]
+    es_all, _ = O.eigensystem(n, mod.hOp, basis, 12, groundDiagMode="full")
     for e in up:
-        assert np.abs(es_x - e).min() < 1e-8
+        assert np.abs(es_all - e).min() < 1e-8
+    assert np.sum(np.abs(up - es[0]) < 1e-8) == 2
     # eigenvectors: orthonormal and eigenvectors of H (dense check on the 190-state basis)
     h = O.get_hamiltonian_matrix(n, mod.hOp, basis).toarray()
     idx = {b: i for i, b in enumerate(basis)}
