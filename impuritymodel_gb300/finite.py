@@ -471,7 +471,7 @@ def get_tridiagonal_krylov_vectors(h, psi0, krylovSize, h_local=False, mode="spa
     return alpha[0, :k].cpu().numpy(), beta[0, : k - 1].cpu().numpy()
 
 
-def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=None):
+def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=None, chunk=32):
     """One reorthogonalised Lanczos run from v0 until the Ritz pairs it wants have converged.
 
     A Ritz pair (theta_i, residual ``r_i = beta_j |s_{j,i}|``) has converged when
@@ -539,7 +539,7 @@ def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=Non
         return j2 + (-r2 / slope) - j
 
     while True:
-        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=32, precision=precision,
+        V, a, bfull = eng.krylov_reorth(csr, v0, k_cap, stop=stop, chunk=chunk, precision=precision,
                                         remaining=remaining, locked=locked)
         kk = len(a)
         exact = kk >= room or (kk < k_cap and bfull[kk - 1] == 0.0)
@@ -596,8 +596,8 @@ def eig_lowest(eng, csr, k, tol_rel=1e-12, k_cap=None, seed=0, precision=0, comp
         v = torch.randn(n, dtype=torch.complex128, device=eng.device, generator=g)
         v = _project_out(X, v)
         v = v / torch.linalg.vector_norm(v)
-        th2, X2 = _ritz_run(eng, csr, v, k, max(64, min(k_cap, 4 * k + 60)), tol_rel, precision, locked=X,
-                            thr=float(thr) if np.isfinite(thr) else 1e300)
+        th2, X2 = _ritz_run(eng, csr, v, k, max(48, min(k_cap, 4 * k + 60)), tol_rel, precision, locked=X,
+                            thr=float(thr) if np.isfinite(thr) else 1e300, chunk=16)
         if len(th2) == 0:
             break
         th_all = np.concatenate([th, th2])
