@@ -94,6 +94,10 @@ SIGNATURES = {
     "edgpu_lookup_states": (_I, [_I, _P, _I64, _P, _I64, _P, _P]),
     "edgpu_spmv": (_I, [C.POINTER(CSR), _P, _P, _I, _P]),
     "edgpu_spmv_c64": (_I, [C.POINTER(CSR), _P, _P, _I, _P]),
+    "edgpu_spmv_plan_workspace": (_SZ, [_I64]),
+    "edgpu_spmv_plan": (_I, [C.POINTER(CSR), _I64, _I, _P, C.POINTER(_I64), _P, _SZ, _P]),
+    "edgpu_spmv_planned": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P]),
+    "edgpu_spmv_planned_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P]),
     "edgpu_lanczos_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_lanczos": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),

@@ -17,6 +17,7 @@ import torch
 
 from . import _lib as L
 from .codec import n_words
+from .tuner import bucket, get_tuner
 
 _U64 = np.uint64
 
@@ -634,8 +635,12 @@ class Engine:
             alpha += csr.mixed_shift  # Lanczos ran on H - shift*I
         return alpha, beta
 
-    def spmv(self, csr, x, precision=0):
-        """y [csr.n, R] = csr @ x for x [csr.ncols, R]."""
+    def spmv(self, csr, x, precision=0, mapping=None):
+        """y [csr.n, R] = csr @ x for x [csr.ncols, R].
+
+        For R with R / (complex numbers per 16 bytes) dividing 32 the row-scheduled kernel
+        runs with the launch mapping the autotuner picked for this matrix's shape bucket (or
+        ``mapping`` = (window, heavy_min, unroll, block)); other R use the row kernel."""
         nx, r = x.shape
         if nx != csr.ncols:
             raise ValueError("spmv: x has %d rows, matrix has %d columns" % (nx, csr.ncols))
@@ -644,16 +649,78 @@ class Engine:
             csr.mixed()
             xr = torch.view_as_real(x.to(torch.complex64).contiguous())
             y = torch.empty((n, r), dtype=torch.complex64, device=self.device)
-            L.check(self.lib.edgpu_spmv_c64(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r,
-                                            self.stream), "spmv_c64")
+            if self.spmv_planned_ok(r, precision) and csr.nnz:
+                self.spmv_into(csr, xr, torch.view_as_real(y), r, precision, mapping)
+            else:
+                L.check(self.lib.edgpu_spmv_c64(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r,
+                                                self.stream), "spmv_c64")
             if csr.mixed_shift:
                 y += csr.mixed_shift * x.to(torch.complex64)  # float32 copy holds H - shift*I
             return y
         xr = torch.view_as_real(x.contiguous())
         y = torch.empty((n, r), dtype=torch.complex128, device=self.device)
-        L.check(self.lib.edgpu_spmv(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r, self.stream),
-                "spmv")
+        if self.spmv_planned_ok(r, precision) and csr.nnz:
+            self.spmv_into(csr, xr, torch.view_as_real(y), r, precision, mapping)
+        else:
+            L.check(self.lib.edgpu_spmv(C.byref(csr.struct()), _ptr(xr), _ptr(torch.view_as_real(y)), r,
+                                        self.stream), "spmv")
         return y
+
+    # -- H.v with a row schedule (edgpu_spmv_plan / edgpu_spmv_planned) --------------------
+    SPMV_WINDOWS = (256, 4096, 0)
+    SPMV_HEAVY = (16, 32, 64)
+    SPMV_UNROLL = (4, 8)
+    SPMV_BLOCK = (128, 256)
+
+    @staticmethod
+    def spmv_planned_ok(R, precision):
+        runs = 2 if precision else 1
+        if R % runs:
+            return False
+        lanes = R // runs
+        return lanes <= 32 and 32 % lanes == 0
+
+    def spmv_plan(self, csr, window, heavy_min):
+        """Row schedule (sched int32 [n], heavy-row count) of ``csr``, built once per
+        (window, heavy_min) and kept with the matrix."""
+        key = (int(window), int(heavy_min))
+        plans = csr.__dict__.setdefault("_plans", {})
+        if key not in plans:
+            sched = torch.empty(csr.n, dtype=torch.int32, device=self.device)
+            nh = C.c_int64(0)
+            ws, wsn = self.workspace(self.lib.edgpu_spmv_plan_workspace(csr.n))
+            L.check(self.lib.edgpu_spmv_plan(C.byref(csr.struct()), key[0], key[1], _ptr(sched), C.byref(nh), ws, wsn,
+                                             self.stream), "spmv_plan")
+            plans[key] = (sched, int(nh.value))
+        return plans[key]
+
+    def spmv_key(self, csr, R, precision):
+        """Autotuner bucket of an H.v launch: sizes as powers of two, vector width, types."""
+        return (bucket(csr.n), bucket(max(1, csr.nnz // max(csr.n, 1))), int(R), "c64" if precision else "c128",
+                "c" if (csr.val_c is not None or csr.val_cf is not None) else "r")
+
+    def spmv_mapping(self, csr, xr, yr, R, precision):
+        """The launch mapping (window, heavy_min, unroll, block) the autotuner picked for this
+        shape bucket, measured on this matrix and these vectors on first use."""
+        cands = [(w, hm, u, b) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY for u in self.SPMV_UNROLL
+                 for b in self.SPMV_BLOCK]
+        return get_tuner().pick("spmv", self.spmv_key(csr, R, precision), cands,
+                                lambda c: self._spmv_planned(csr, xr, yr, R, precision, c))
+
+    def _spmv_planned(self, csr, xr, yr, R, precision, mapping):
+        w, hm, u, b = mapping
+        sched, nh = self.spmv_plan(csr, w, hm)
+        fn = self.lib.edgpu_spmv_planned_c64 if precision else self.lib.edgpu_spmv_planned
+        L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, int(u), int(b), _ptr(xr), _ptr(yr), int(R), self.stream),
+                "spmv_planned")
+
+    def spmv_into(self, csr, xr, yr, R, precision=0, mapping=None):
+        """yr = csr @ xr on real views of complex [rows][R] buffers (no allocation once the
+        plan exists): the launch the H.v roofline times."""
+        if mapping is None:
+            mapping = self.spmv_mapping(csr, xr, yr, R, precision)
+        self._spmv_planned(csr, xr, yr, R, precision, mapping)
+        return mapping
 
     def cfrac(self, alpha, beta, k_len, omega, delta, e, scale, precision=0):
         r, K = alpha.shape

@@ -185,6 +185,31 @@ int edgpu_spmv(const edgpu_csr* h, const double* x, double* y, int R, void* stre
 int edgpu_spmv_c64(const edgpu_csr* h, const float* x, float* y, int R, void* stream);
 
 /*
+ * Row schedule for edgpu_spmv_planned (built once per matrix).  sched[n] (device, int32)
+ * receives the rows in service order: first the *n_heavy (host) rows with at least
+ * heavy_min entries, longest first, each served by a whole warp; then the other rows sorted
+ * by length (longest first, stable) within windows of `window` consecutive rows (0: one
+ * window).  Synchronises the stream (reads the heavy-row count).  n < 2^31.
+ * The same y = H x as edgpu_spmv (h.dot of upstream get_tridiagonal_krylov_vectors,
+ * finite.py:1946-1989); the schedule only changes which threads serve which rows.
+ */
+size_t edgpu_spmv_plan_workspace(int64_t n);
+int edgpu_spmv_plan(const edgpu_csr* h, int64_t window, int heavy_min, int32_t* sched, int64_t* n_heavy,
+                    void* workspace, size_t workspace_bytes, void* stream);
+/*
+ * y = H x with a row schedule from edgpu_spmv_plan: x [ncols][R], y [n][R] complex128 (or
+ * complex64 with float32 accumulation for the _c64 form), 16-byte aligned; R a multiple of
+ * the complex numbers per 16 bytes (1 for complex128, 2 for complex64) with R / that count
+ * dividing 32.  unroll (gathers in flight per lane: 2, 4 or 8) and block (threads per block:
+ * 64, 128, 256 or 512) are launch choices that leave the result unchanged up to the order
+ * of the additions in heavy rows.  Replaces upstream's h.dot (finite.py:1946-1989).
+ */
+int edgpu_spmv_planned(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, int unroll, int block,
+                       const double* x, double* y, int R, void* stream);
+int edgpu_spmv_planned_c64(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, int unroll, int block,
+                           const float* x, float* y, int R, void* stream);
+
+/*
  * Batched Lanczos tridiagonalisation without reorthogonalisation, R independent runs on one
  * CSR matrix.  Replaces upstream ``get_tridiagonal_krylov_vectors`` (finite.py:1897-1995):
  * same recurrence (alpha_j = Re<H v_j, v_j>, w = H v_j - alpha_j v_j - beta_{j-1} v_{j-1},
