@@ -120,15 +120,17 @@ class CsrMatrix:
         rows = torch.repeat_interleave(torch.arange(self.n, device=self.row_ptr.device),
                                        self.row_ptr[1:] - self.row_ptr[:-1], output_size=int(self.col.shape[0]))
         diag = rows == self.col.to(torch.int64)
+        # the shift needs a stored diagonal entry in every row (H - shift*I keeps H's pattern)
+        full_diag = int(diag.sum().item()) == self.n
         if self.val_r is not None:
             d = self.val_r[diag]
-            self.mixed_shift = float(d.mean().item()) if d.numel() else 0.0
+            self.mixed_shift = float(d.mean().item()) if d.numel() and full_diag else 0.0
             v = self.val_r.clone()
             v[diag] -= self.mixed_shift
             self.val_rf = v.to(torch.float32)
         else:
             d = self.val_c[diag, 0]
-            self.mixed_shift = float(d.mean().item()) if d.numel() else 0.0
+            self.mixed_shift = float(d.mean().item()) if d.numel() and full_diag else 0.0
             v = self.val_c.clone()
             v[diag, 0] -= self.mixed_shift
             self.val_cf = v.to(torch.float32)
