@@ -355,10 +355,11 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     alg64 = csr.nnz * (val64 + 4) + (csr.n + 1) * 8 + 2 * csr.n * R * 16
     del y64, y, y_rows
     peak = peaks.get("hbm_gbs")
-    _, n_heavy = eng.spmv_plan(csr, mapping[0], mapping[1])
+    _, n_heavy = eng.spmv_plan(csr, mapping[1], mapping[2])
     return {
         "bound": "hbm",
-        "kernel": "spmv_sched_kernel<float> (edgpu_spmv_planned_c64)",
+        "kernel": ("spmv_sched_kernel (heavy rows) + spmv_pages_kernel<float> (edgpu_spmv_paged_c64)"
+                   if mapping[0] == "pages" else "spmv_sched_kernel<float> (edgpu_spmv_planned_c64)"),
         "achieved": round(achieved, 1),
         "peak": peak,
         "unit": "GB/s",
@@ -367,7 +368,8 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
         "algorithmic_bytes_per_launch": int(alg),
         "avg_launch_us": round(avg_s * 1e6, 2),
         "launches": launches,
-        "mapping": {"window": mapping[0], "heavy_min": mapping[1], "unroll": mapping[2], "block": mapping[3],
+        "mapping": {"kernel": mapping[0], "window": mapping[1], "heavy_min": mapping[2], "unroll": mapping[3],
+                    ("page_entries" if mapping[0] == "pages" else "block"): mapping[4],
                     "heavy_rows": int(n_heavy), "tune_s": round(tune_s, 3),
                     "candidates_us": get_tuner_report("spmv", eng.spmv_key(csr, R, 1))},
         "row_kernel_us": round(rows_s * 1e6, 2),

@@ -668,11 +668,12 @@ class Engine:
                                         self.stream), "spmv")
         return y
 
-    # -- H.v with a row schedule (edgpu_spmv_plan / edgpu_spmv_planned) --------------------
+    # -- H.v with a row schedule (edgpu_spmv_plan / edgpu_spmv_planned / edgpu_spmv_paged) -
     SPMV_WINDOWS = (256, 4096, 0)
     SPMV_HEAVY = (16, 32, 64)
     SPMV_UNROLL = (4, 8)
     SPMV_BLOCK = (128, 256)
+    SPMV_PAGES = (256, 512)
 
     @staticmethod
     def spmv_planned_ok(R, precision):
@@ -681,6 +682,28 @@ class Engine:
             return False
         lanes = R // runs
         return lanes <= 32 and 32 % lanes == 0
+
+    def spmv_candidates(self, csr, R, precision):
+        """Launch mappings of H.v that the autotuner chooses from, as tuples:
+        ("sched", window, heavy_min, unroll, block): every row through the CSR, heavy rows
+        one warp each, light rows in length-sorted windows;
+        ("pages", window, heavy_min, unroll, page_entries): the same heavy rows, the light
+        rows from a paged copy streamed through shared memory (real values, or complex64)."""
+        out = [("sched", w, hm, u, b) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY for u in self.SPMV_UNROLL
+               for b in self.SPMV_BLOCK]
+        lanes = R // (2 if precision else 1)
+        kind = self._pages_kind(csr, precision)
+        if kind is not None and lanes in (2, 4, 8, 16):
+            rows_per_slice = 32 // lanes
+            out += [("pages", w, hm, u, ch) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY
+                    for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES if rows_per_slice * (hm + 1) <= ch]
+        return out
+
+    @staticmethod
+    def _pages_kind(csr, precision):
+        if precision:
+            return 2 if csr.val_cf is not None else (0 if csr.val_rf is not None else None)
+        return 1 if (csr.val_c is None and csr.val_r is not None) else None
 
     def spmv_plan(self, csr, window, heavy_min):
         """Row schedule (sched int32 [n], heavy-row count) of ``csr``, built once per
@@ -696,33 +719,61 @@ class Engine:
             plans[key] = (sched, int(nh.value))
         return plans[key]
 
+    def spmv_pages(self, csr, window, heavy_min, lanes, page_entries, kind):
+        """Paged copy of the light rows (uint8 device buffer, page count), built once per
+        (schedule, lanes, page size, value kind) and kept with the matrix."""
+        key = (int(window), int(heavy_min), int(lanes), int(page_entries), int(kind))
+        pages = csr.__dict__.setdefault("_pages", {})
+        if key not in pages:
+            sched, nh = self.spmv_plan(csr, window, heavy_min)
+            ws, wsn = self.workspace(self.lib.edgpu_spmv_pages_workspace(csr.n, lanes))
+            npg = C.c_int64(0)
+            rc = self.lib.edgpu_spmv_pages_build(C.byref(csr.struct()), _ptr(sched), nh, lanes, page_entries, kind,
+                                                 None, 0, C.byref(npg), ws, wsn, self.stream)
+            if rc not in (L.EDGPU_OK, L.EDGPU_ERR_OVERFLOW):
+                raise L.EdgpuError(rc, "spmv_pages_build")
+            ebytes = 8 if kind == 0 else 16
+            buf = torch.empty(max(1, npg.value) * page_entries * ebytes, dtype=torch.uint8, device=self.device)
+            if npg.value:
+                ws, wsn = self.workspace(self.lib.edgpu_spmv_pages_workspace(csr.n, lanes))
+                L.check(self.lib.edgpu_spmv_pages_build(C.byref(csr.struct()), _ptr(sched), nh, lanes, page_entries,
+                                                        kind, _ptr(buf), npg.value, C.byref(npg), ws, wsn, self.stream),
+                        "spmv_pages_build")
+            pages[key] = (buf, int(npg.value))
+        return pages[key]
+
     def spmv_key(self, csr, R, precision):
         """Autotuner bucket of an H.v launch: sizes as powers of two, vector width, types."""
         return (bucket(csr.n), bucket(max(1, csr.nnz // max(csr.n, 1))), int(R), "c64" if precision else "c128",
                 "c" if (csr.val_c is not None or csr.val_cf is not None) else "r")
 
     def spmv_mapping(self, csr, xr, yr, R, precision):
-        """The launch mapping (window, heavy_min, unroll, block) the autotuner picked for this
-        shape bucket, measured on this matrix and these vectors on first use."""
-        cands = [(w, hm, u, b) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY for u in self.SPMV_UNROLL
-                 for b in self.SPMV_BLOCK]
-        return get_tuner().pick("spmv", self.spmv_key(csr, R, precision), cands,
+        """The launch mapping the autotuner picked for this shape bucket, measured on this
+        matrix and these vectors on first use."""
+        return get_tuner().pick("spmv", self.spmv_key(csr, R, precision), self.spmv_candidates(csr, R, precision),
                                 lambda c: self._spmv_planned(csr, xr, yr, R, precision, c))
 
     def _spmv_planned(self, csr, xr, yr, R, precision, mapping):
-        w, hm, u, b = mapping
+        kernel, w, hm, u, last = mapping
         sched, nh = self.spmv_plan(csr, w, hm)
+        if kernel == "pages":
+            lanes = R // (2 if precision else 1)
+            buf, npg = self.spmv_pages(csr, w, hm, lanes, last, self._pages_kind(csr, precision))
+            fn = self.lib.edgpu_spmv_paged_c64 if precision else self.lib.edgpu_spmv_paged
+            L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, _ptr(buf), npg, int(last), int(u), _ptr(xr), _ptr(yr),
+                       int(R), self.stream), "spmv_paged")
+            return
         fn = self.lib.edgpu_spmv_planned_c64 if precision else self.lib.edgpu_spmv_planned
-        L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, int(u), int(b), _ptr(xr), _ptr(yr), int(R), self.stream),
+        L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, int(u), int(last), _ptr(xr), _ptr(yr), int(R), self.stream),
                 "spmv_planned")
 
     def spmv_into(self, csr, xr, yr, R, precision=0, mapping=None):
         """yr = csr @ xr on real views of complex [rows][R] buffers (no allocation once the
-        plan exists): the launch the H.v roofline times."""
+        plan exists): the launch the H.v roofline times.  Returns the mapping used."""
         if mapping is None:
             mapping = self.spmv_mapping(csr, xr, yr, R, precision)
-        self._spmv_planned(csr, xr, yr, R, precision, mapping)
-        return mapping
+        self._spmv_planned(csr, xr, yr, R, precision, tuple(mapping))
+        return tuple(mapping)
 
     def cfrac(self, alpha, beta, k_len, omega, delta, e, scale, precision=0):
         r, K = alpha.shape

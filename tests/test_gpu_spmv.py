@@ -39,16 +39,19 @@ def test_planned_spmv_matches_fp64_for_every_mapping(eng, complex_vals):
     h = _matrix(n, 3 + complex_vals, complex_vals)
     csr = finite._scipy_to_device_csr(eng, h)
     rng = np.random.default_rng(9)
-    mappings = [(w, hm, u, b) for w in eng.SPMV_WINDOWS for hm in eng.SPMV_HEAVY for u in eng.SPMV_UNROLL
-                for b in eng.SPMV_BLOCK]
     for precision, widths in ((0, (1, 2, 4, 8, 16, 32)), (1, (2, 4, 8, 16, 32, 64))):
+        if precision:
+            csr.mixed()
         for R in widths:
+            mappings = eng.spmv_candidates(csr, R, precision)
+            assert any(m[0] == "pages" for m in mappings) == (
+                (precision or not complex_vals) and R // (2 if precision else 1) in (2, 4, 8, 16))
             x = rng.standard_normal((n, R)) + 1j * rng.standard_normal((n, R))
             ref = h @ x
             xt = torch.from_numpy(x).to(eng.device)
             scale = np.abs(h).dot(np.abs(x)).max()
             tol = 1e-13 if precision == 0 else 2e-6
-            for m in (mappings if R in (2, 16) else mappings[::7]):
+            for m in (mappings if R in (2, 16) else mappings[::5]):
                 y = eng.spmv(csr, xt, precision=precision, mapping=m).cpu().numpy()
                 err = np.abs(y - ref).max() / scale
                 assert err < tol, (precision, R, m, err)
@@ -93,8 +96,7 @@ def test_autotuner_picks_and_caches_a_mapping(eng, tmp_path):
     xr, yr = torch.view_as_real(x), torch.view_as_real(y)
     path = str(tmp_path / "tune.json")
     t = Autotuner(path)
-    cands = [(w, hm, u, b) for w in eng.SPMV_WINDOWS for hm in eng.SPMV_HEAVY for u in eng.SPMV_UNROLL
-             for b in eng.SPMV_BLOCK]
+    cands = eng.spmv_candidates(csr, R, 0)
     key = eng.spmv_key(csr, R, 0)
     calls = []
 
@@ -104,6 +106,7 @@ def test_autotuner_picks_and_caches_a_mapping(eng, tmp_path):
 
     best = t.pick("spmv", key, cands, run)
     assert best in cands and len(calls) >= len(cands)
+    assert any(c[0] == "pages" for c in cands) and any(c[0] == "sched" for c in cands)
     n_calls = len(calls)
     assert t.pick("spmv", key, cands, run) == best and len(calls) == n_calls  # cached
     t2 = Autotuner(path)  # reloaded from the file
