@@ -21,6 +21,7 @@
 // Each lane keeps U gathers in flight per batch (predicated tail, no divergence inside a
 // group).  The plan (the schedule and the count of heavy rows) is built once per matrix by a
 // stable radix sort of one 64-bit key per row.
+#include <climits>
 #include <vector>
 
 #include "common.cuh"
@@ -271,66 +272,79 @@ __global__ void __launch_bounds__(128) spmv_pages_kernel(int64_t n_pages, const 
     if (pa + st < pb) issue(pa + st);
     cp_async_commit();
   }
+  T ar[RV], ai[RV];
+  int64_t row = -1;
+  auto flush = [&]() {
+    if (row >= 0) {
+      P out;
+      T* os = reinterpret_cast<T*>(&out);
+#pragma unroll
+      for (int q = 0; q < RV; ++q) {
+        os[2 * q] = ar[q];
+        os[2 * q + 1] = ai[q];
+      }
+      __stcs(Y + row * L + sub, out);
+    }
+#pragma unroll
+    for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
+  };
   for (int64_t p = pa; p < pb; ++p) {
     if (p + NS - 1 < pb) issue(p + NS - 1);
     cp_async_commit();
     cp_async_wait<NS - 1>();
     __syncwarp();
     const E* pg = ring + ((p - pa) % NS) * CH;
-    const int ns = pg[0].c;
-    int off = C;
-    for (int sl = 0; sl < ns; ++sl) {
-      const E hd = pg[off + grp];
-      const int row = hd.c, w = hd.w();
-      off += C;
-      T ar[RV], ai[RV];
+    // the page's columns after its header as one stream: a slice header column (c <= -2)
+    // closes the previous row of the group and opens the next; every entry column's gather
+    // is independent of the others, so U of them are in flight per lane
+    const int ncols = pg[0].c;
+    row = -1;
 #pragma unroll
-      for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
-      for (int e = 0; e < w; e += U) {
-        E en[U];
-        P xv[U];
+    for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
+    for (int k = 1; k < ncols; k += U) {
+      E en[U];
+      P xv[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          en[u] = (e + u < w) ? pg[off + (e + u) * C + grp] : E{};
-          if (e + u >= w) en[u].c = -1;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) xv[u] = en[u].c >= 0 ? __ldg(X + (int64_t)en[u].c * L + sub) : P{};
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const T* xs = reinterpret_cast<const T*>(&xv[u]);
-          T hr, hi = T(0);
-          if constexpr (VALC) {
-            hr = en[u].vr;
-            hi = en[u].vi;
-          } else {
-            hr = en[u].v;
-          }
-          if (en[u].c < 0) hr = hi = T(0);
-#pragma unroll
-          for (int q = 0; q < RV; ++q) {
-            const T xr = xs[2 * q], xi = xs[2 * q + 1];
-            ar[q] += hr * xr;
-            ai[q] += hr * xi;
-            if (VALC) {
-              ar[q] -= hi * xi;
-              ai[q] += hi * xr;
-            }
-          }
+      for (int u = 0; u < U; ++u) {
+        if (k + u < ncols) {
+          en[u] = pg[(k + u) * C + grp];
+        } else {
+          en[u] = E{};
+          en[u].c = -1;
         }
       }
-      off += w * C;
-      if (row >= 0) {
-        P out;
-        T* os = reinterpret_cast<T*>(&out);
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = en[u].c >= 0 ? __ldg(X + (int64_t)en[u].c * L + sub) : P{};
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = en[u].c;
+        if (c <= -2) {
+          flush();
+          row = c == INT_MIN ? -1 : (int64_t)(-2 - c);
+          continue;
+        }
+        if (c < 0) continue;
+        const T* xs = reinterpret_cast<const T*>(&xv[u]);
+        T hr, hi = T(0);
+        if constexpr (VALC) {
+          hr = en[u].vr;
+          hi = en[u].vi;
+        } else {
+          hr = en[u].v;
+        }
 #pragma unroll
         for (int q = 0; q < RV; ++q) {
-          os[2 * q] = ar[q];
-          os[2 * q + 1] = ai[q];
+          const T xr = xs[2 * q], xi = xs[2 * q + 1];
+          ar[q] += hr * xr;
+          ai[q] += hr * xi;
+          if (VALC) {
+            ar[q] -= hi * xi;
+            ai[q] += hi * xr;
+          }
         }
-        __stcs(Y + (int64_t)row * L + sub, out);
       }
     }
+    flush();
     __syncwarp();  // every lane is done with this stage before it is refilled
   }
   cp_async_wait<0>();
@@ -365,14 +379,15 @@ __device__ __forceinline__ E make_ent(int32_t c, int w) {
   return e;
 }
 
-// Every entry of every page: empty (column -1, value 0); page headers: slice counts.
+// Every entry of every page: empty (column -1, value 0); page headers: the number of used
+// columns (header column included).
 template <typename E>
-__global__ void pages_clear_kernel(int64_t n_pages, int CH, const int32_t* __restrict__ page_slice0, E* pages) {
+__global__ void pages_clear_kernel(int64_t n_pages, int CH, const int32_t* __restrict__ page_cols, E* pages) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pages * CH) return;
   const int64_t p = i / CH;
   const int k = (int)(i - p * CH);
-  pages[i] = make_ent<E>(k == 0 ? page_slice0[p + 1] - page_slice0[p] : -1, 0);
+  pages[i] = make_ent<E>(k == 0 ? page_cols[p] : -1, 0);
 }
 
 // One warp per slice: its header column and w columns at its place in its page.
@@ -392,7 +407,8 @@ __global__ void pages_fill_kernel(int64_t n_slices, int64_t n_light, int C, int 
     const int64_t p = s * C + r;
     const int64_t row = p < n_light ? light[p] : -1;
     if (e < 0) {
-      base[k] = make_ent<E>((int32_t)row, w);
+      // slice header: the group's row as -2 - row (INT_MIN when the group has none)
+      base[k] = make_ent<E>(row >= 0 ? (int32_t)(-2 - row) : INT_MIN, w);
       continue;
     }
     E en = make_ent<E>(-1, 0);
@@ -578,21 +594,20 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
   }
   // greedy packing in schedule order: a page holds its header column and whole slices
   std::vector<int64_t> pos_h((size_t)n_slices);
-  std::vector<int32_t> ps0_h;
-  ps0_h.push_back(0);
+  std::vector<int32_t> ps0_h;  // used columns of each page (its header column included)
   int64_t page = 0, used = C;
   for (int64_t sl = 0; sl < n_slices; ++sl) {
     const int64_t size = (int64_t)C * (w_h[(size_t)sl] + 1);
     if (size + C > CH) return EDGPU_ERR_ARG;  // a light row too long for the page size
     if (used + size > CH) {
-      ps0_h.push_back((int32_t)sl);
+      ps0_h.push_back((int32_t)(used / C));
       ++page;
       used = C;
     }
     pos_h[(size_t)sl] = page * CH + used;
     used += size;
   }
-  ps0_h.push_back((int32_t)n_slices);
+  ps0_h.push_back((int32_t)(used / C));
   const int64_t np = n_slices > 0 ? page + 1 : 0;
   *n_pages = np;
   if (np > cap_pages || (np > 0 && !pages)) return EDGPU_ERR_OVERFLOW;
@@ -600,7 +615,7 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
   if ((reinterpret_cast<uintptr_t>(pages) & 15) != 0) return EDGPU_ERR_ARG;
   if (cudaMemcpyAsync(slice_pos, pos_h.data(), sizeof(int64_t) * (size_t)n_slices, cudaMemcpyHostToDevice, s) !=
           cudaSuccess ||
-      cudaMemcpyAsync(page_slice0, ps0_h.data(), sizeof(int32_t) * (size_t)(np + 1), cudaMemcpyHostToDevice, s) !=
+      cudaMemcpyAsync(page_slice0, ps0_h.data(), sizeof(int32_t) * (size_t)np, cudaMemcpyHostToDevice, s) !=
           cudaSuccess)
     return EDGPU_ERR_CUDA;
   int rc;
