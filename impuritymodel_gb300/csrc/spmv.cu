@@ -201,17 +201,23 @@ int spmv_planned(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, int 
 
 
 // ---------------------------------------------------------------------------------------
-// Paged layout of the light rows (edgpu_spmv_pages_build / edgpu_spmv_paged[_c64]).
+// Paged layout (edgpu_spmv_pages_build / edgpu_spmv_paged[_c64]).
 //
-// The light rows of a schedule, C = 32 / L of them per slice (the rows a warp serves
-// together), are stored slice by slice in fixed-size pages of CH entries: a page header
-// column (C entries, the first holding the page's slice count), then per slice a header
-// column (entry r: row of group r or -1, and the slice width w) and w columns of C entries
-// (entry (e, r): column and value of the e-th entry of row r, or column -1 past its end).
-// A warp serves a contiguous range of pages.  Its lanes copy the pages NS - 1 ahead into a
-// ring of NS stages in shared memory with cp.async (16 bytes a lane, no registers held), so
-// the only memory latency left on a slice's path is the gather of x from L2; the rows, the
-// widths, the columns and the values are read from shared memory.
+// The rows of a schedule are cut into slices and packed whole, in schedule order, into
+// fixed-size pages of CH entries.  A heavy row is a slice of its own whose entries are dealt
+// to the C = 32 / L row groups of a warp in turn (group r takes entries r, r + C, ...); a
+// light slice holds C consecutive light rows, one per group.  A page is a header column (C
+// entries; the first holds the number of used columns), then per slice a header column
+// (entry r: column -2 - row of group r, or INT_MIN for none, and a flag set for a heavy row)
+// and the slice's entry columns (entry (k, r): column and value of the group's k-th entry,
+// column -1 past its end).
+//
+// One warp serves one page: it copies the page into shared memory with cp.async (16-byte
+// chunks, coalesced) and reads its columns as one stream, U columns per batch, so U gathers
+// of x rows per lane are in flight whatever the slice boundaries; a slice header column
+// closes the groups' previous rows (adding a heavy row's partial sums across the groups with
+// xor shuffles) and opens the next.  The only memory latencies on a warp's path are the page
+// copy and the gathers; the rows, columns and values come from shared memory.
 // ---------------------------------------------------------------------------------------
 template <typename T, bool VALC>
 struct Ent;
@@ -219,21 +225,24 @@ template <>
 struct __align__(8) Ent<float, false> {
   int32_t c;
   float v;
-  __device__ __forceinline__ int w() const { return __float_as_int(v); }
+  __device__ __forceinline__ int flag() const { return __float_as_int(v); }
+  __device__ __forceinline__ void set_flag(int f) { v = __int_as_float(f); }
 };
 template <>
 struct __align__(16) Ent<double, false> {
   int32_t c;
   int32_t aux;
   double v;
-  __device__ __forceinline__ int w() const { return aux; }
+  __device__ __forceinline__ int flag() const { return aux; }
+  __device__ __forceinline__ void set_flag(int f) { aux = f; }
 };
 template <>
 struct __align__(16) Ent<float, true> {
   int32_t c;
   int32_t aux;
   float vr, vi;
-  __device__ __forceinline__ int w() const { return aux; }
+  __device__ __forceinline__ int flag() const { return aux; }
+  __device__ __forceinline__ void set_flag(int f) { aux = f; }
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -241,41 +250,51 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-template <typename T, bool VALC, int L, int U, int CH, int NS>
-__global__ void __launch_bounds__(128) spmv_pages_kernel(int64_t n_pages, const Ent<T, VALC>* __restrict__ pages,
-                                                         const typename Pack16<T>::type* __restrict__ X,
-                                                         typename Pack16<T>::type* __restrict__ Y) {
+constexpr int kPageWarps = 4;  // warps (pages) per block of the paged kernel
+
+template <typename T, bool VALC, int L, int U, int CH>
+__global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_pages,
+                                                                     const Ent<T, VALC>* __restrict__ pages,
+                                                                     const typename Pack16<T>::type* __restrict__ X,
+                                                                     typename Pack16<T>::type* __restrict__ Y) {
   using E = Ent<T, VALC>;
   using P = typename Pack16<T>::type;
   constexpr int RV = Pack16<T>::runs;
   constexpr int C = 32 / L;
   constexpr int CHUNKS = CH * (int)sizeof(E) / 16;  // 16-byte copies per page
-  extern __shared__ __align__(16) unsigned char ring_raw[];
+  extern __shared__ __align__(16) unsigned char page_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int grp = lane / L, sub = lane - grp * L;
-  E* ring = reinterpret_cast<E*>(ring_raw) + (size_t)wib * NS * CH;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t pa = gw * n_pages / nw, pb = (gw + 1) * n_pages / nw;
-  auto issue = [&](int64_t q) {
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(pages + q * CH);
-    unsigned char* dst = reinterpret_cast<unsigned char*>(ring + ((q - pa) % NS) * CH);
-    for (int k = lane; k < CHUNKS; k += 32) cp_async16(dst + 16 * k, src + 16 * k);
-  };
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= n_pages) return;  // warp-uniform
+  E* pg = reinterpret_cast<E*>(page_raw) + (size_t)wib * CH;
+  {
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(pages + p * CH);
+    unsigned char* dst = reinterpret_cast<unsigned char*>(pg);
 #pragma unroll
-  for (int st = 0; st < NS - 1; ++st) {
-    if (pa + st < pb) issue(pa + st);
+    for (int k = lane; k < CHUNKS; k += 32) cp_async16(dst + 16 * k, src + 16 * k);
     cp_async_commit();
+    cp_async_wait_all();
+    __syncwarp();
   }
   T ar[RV], ai[RV];
+#pragma unroll
+  for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
   int64_t row = -1;
-  auto flush = [&]() {
-    if (row >= 0) {
+  bool heavy = false;
+  auto flush = [&]() {  // called by the whole warp at the same column
+    if (heavy) {
+#pragma unroll
+      for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+        for (int q = 0; q < RV; ++q) {
+          ar[q] += __shfl_xor_sync(0xffffffffu, ar[q], o);
+          ai[q] += __shfl_xor_sync(0xffffffffu, ai[q], o);
+        }
+    }
+    if (row >= 0 && (!heavy || grp == 0)) {
       P out;
       T* os = reinterpret_cast<T*>(&out);
 #pragma unroll
@@ -288,99 +307,87 @@ __global__ void __launch_bounds__(128) spmv_pages_kernel(int64_t n_pages, const 
 #pragma unroll
     for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
   };
-  for (int64_t p = pa; p < pb; ++p) {
-    if (p + NS - 1 < pb) issue(p + NS - 1);
-    cp_async_commit();
-    cp_async_wait<NS - 1>();
-    __syncwarp();
-    const E* pg = ring + ((p - pa) % NS) * CH;
-    // the page's columns after its header as one stream: a slice header column (c <= -2)
-    // closes the previous row of the group and opens the next; every entry column's gather
-    // is independent of the others, so U of them are in flight per lane
-    const int ncols = pg[0].c;
-    row = -1;
+  const int ncols = pg[0].c;
+  for (int k = 1; k < ncols; k += U) {
+    E en[U];
+    P xv[U];
 #pragma unroll
-    for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
-    for (int k = 1; k < ncols; k += U) {
-      E en[U];
-      P xv[U];
+    for (int u = 0; u < U; ++u) {
+      if (k + u < ncols) {
+        en[u] = pg[(k + u) * C + grp];
+      } else {
+        en[u] = E{};
+        en[u].c = -1;
+      }
+    }
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (k + u < ncols) {
-          en[u] = pg[(k + u) * C + grp];
-        } else {
-          en[u] = E{};
-          en[u].c = -1;
-        }
+    for (int u = 0; u < U; ++u) xv[u] = en[u].c >= 0 ? __ldg(X + (int64_t)en[u].c * L + sub) : P{};
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int c = en[u].c;
+      if (c <= -2) {  // a slice header column (the same kind in every group)
+        flush();
+        row = c == INT_MIN ? -1 : (int64_t)(-2 - (int64_t)c);
+        heavy = en[u].flag() != 0;
+        continue;
+      }
+      if (c < 0) continue;
+      const T* xs = reinterpret_cast<const T*>(&xv[u]);
+      T hr, hi = T(0);
+      if constexpr (VALC) {
+        hr = en[u].vr;
+        hi = en[u].vi;
+      } else {
+        hr = en[u].v;
       }
 #pragma unroll
-      for (int u = 0; u < U; ++u) xv[u] = en[u].c >= 0 ? __ldg(X + (int64_t)en[u].c * L + sub) : P{};
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int c = en[u].c;
-        if (c <= -2) {
-          flush();
-          row = c == INT_MIN ? -1 : (int64_t)(-2 - c);
-          continue;
-        }
-        if (c < 0) continue;
-        const T* xs = reinterpret_cast<const T*>(&xv[u]);
-        T hr, hi = T(0);
-        if constexpr (VALC) {
-          hr = en[u].vr;
-          hi = en[u].vi;
-        } else {
-          hr = en[u].v;
-        }
-#pragma unroll
-        for (int q = 0; q < RV; ++q) {
-          const T xr = xs[2 * q], xi = xs[2 * q + 1];
-          ar[q] += hr * xr;
-          ai[q] += hr * xi;
-          if (VALC) {
-            ar[q] -= hi * xi;
-            ai[q] += hi * xr;
-          }
+      for (int q = 0; q < RV; ++q) {
+        const T xr = xs[2 * q], xi = xs[2 * q + 1];
+        ar[q] += hr * xr;
+        ai[q] += hr * xi;
+        if (VALC) {
+          ar[q] -= hi * xi;
+          ai[q] += hi * xr;
         }
       }
     }
-    flush();
-    __syncwarp();  // every lane is done with this stage before it is refilled
   }
-  cp_async_wait<0>();
+  flush();
 }
 
-// Slice widths of the light rows: w[s] = the longest of the C rows of slice s.
-__global__ void pages_width_kernel(int64_t n_light, int C, const int32_t* __restrict__ light,
-                                   const int64_t* __restrict__ rp, int32_t* wout) {
+// Slice widths: heavy slice s < n_heavy: ceil(len / C); light slices: the longest row.
+__global__ void pages_width_kernel(int64_t n_heavy, int64_t n_rows, int64_t n_slices, int C,
+                                   const int32_t* __restrict__ sched, const int64_t* __restrict__ rp,
+                                   int32_t* wout) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s * C >= n_light) return;
+  if (s >= n_slices) return;
   int64_t w = 0;
-  for (int r = 0; r < C; ++r) {
-    const int64_t p = s * C + r;
-    if (p < n_light) {
-      const int64_t row = light[p];
-      const int64_t len = rp[row + 1] - rp[row];
-      w = len > w ? len : w;
+  if (s < n_heavy) {
+    const int64_t row = sched[s];
+    w = (rp[row + 1] - rp[row] + C - 1) / C;
+  } else {
+    for (int r = 0; r < C; ++r) {
+      const int64_t q = n_heavy + (s - n_heavy) * C + r;
+      if (q < n_rows) {
+        const int64_t row = sched[q];
+        const int64_t len = rp[row + 1] - rp[row];
+        w = len > w ? len : w;
+      }
     }
   }
   wout[s] = (int32_t)w;
 }
 
 template <typename E>
-__device__ __forceinline__ E make_ent(int32_t c, int w) {
+__device__ __forceinline__ E make_ent(int32_t c, int flag) {
   E e{};
   e.c = c;
-  if constexpr (sizeof(E) == 8) {
-    e.v = __int_as_float(w);
-  } else {
-    e.aux = w;
-  }
+  e.set_flag(flag);
   return e;
 }
 
-// Every entry of every page: empty (column -1, value 0); page headers: the number of used
-// columns (header column included).
+// Every entry of every page: empty (column -1, value 0); the first header entry of a page:
+// its number of used columns.
 template <typename E>
 __global__ void pages_clear_kernel(int64_t n_pages, int CH, const int32_t* __restrict__ page_cols, E* pages) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -390,37 +397,45 @@ __global__ void pages_clear_kernel(int64_t n_pages, int CH, const int32_t* __res
   pages[i] = make_ent<E>(k == 0 ? page_cols[p] : -1, 0);
 }
 
-// One warp per slice: its header column and w columns at its place in its page.
+// One warp per slice: its header column and w entry columns at its place in its page.
 template <typename T, bool VALC>
-__global__ void pages_fill_kernel(int64_t n_slices, int64_t n_light, int C, int CH, const int32_t* __restrict__ light,
-                                  const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                  const T* __restrict__ vals, const int32_t* __restrict__ width,
-                                  const int64_t* __restrict__ slice_pos, Ent<T, VALC>* pages) {
+__global__ void pages_fill_kernel(int64_t n_slices, int64_t n_heavy, int64_t n_rows, int C,
+                                  const int32_t* __restrict__ sched, const int64_t* __restrict__ rp,
+                                  const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                  const int32_t* __restrict__ width, const int64_t* __restrict__ slice_pos,
+                                  Ent<T, VALC>* pages) {
   using E = Ent<T, VALC>;
   const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= n_slices) return;
   const int w = width[s];
+  const bool hv = s < n_heavy;
   E* base = pages + slice_pos[s];
   for (int k = lane; k < (w + 1) * C; k += 32) {
     const int e = k / C - 1, r = k - (k / C) * C;
-    const int64_t p = s * C + r;
-    const int64_t row = p < n_light ? light[p] : -1;
+    int64_t row, idx;
+    if (hv) {
+      row = sched[s];
+      idx = (int64_t)e * C + r;  // heavy row: entries dealt to the groups in turn
+    } else {
+      const int64_t q = n_heavy + (s - n_heavy) * C + r;
+      row = q < n_rows ? sched[q] : -1;
+      idx = e;
+    }
     if (e < 0) {
-      // slice header: the group's row as -2 - row (INT_MIN when the group has none)
-      base[k] = make_ent<E>(row >= 0 ? (int32_t)(-2 - row) : INT_MIN, w);
+      base[k] = make_ent<E>(row >= 0 ? (int32_t)(-2 - row) : INT_MIN, hv ? 1 : 0);
       continue;
     }
     E en = make_ent<E>(-1, 0);
     if (row >= 0) {
       const int64_t e0 = rp[row], len = rp[row + 1] - e0;
-      if (e < len) {
-        en.c = col[e0 + e];
+      if (idx < len) {
+        en.c = col[e0 + idx];
         if constexpr (VALC) {
-          en.vr = vals[2 * (e0 + e)];
-          en.vi = vals[2 * (e0 + e) + 1];
+          en.vr = vals[2 * (e0 + idx)];
+          en.vi = vals[2 * (e0 + idx) + 1];
         } else {
-          en.v = vals[e0 + e];
+          en.v = vals[e0 + idx];
         }
       }
     }
@@ -428,29 +443,19 @@ __global__ void pages_fill_kernel(int64_t n_slices, int64_t n_light, int C, int 
   }
 }
 
-
-constexpr int kPageStages = 4;
-constexpr int kPageWarps = 4;  // warps per block of the paged kernel
-
 template <typename T, bool VALC, int L, int U, int CH>
 int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, cudaStream_t s) {
   using P = typename Pack16<T>::type;
   using E = Ent<T, VALC>;
-  auto kern = spmv_pages_kernel<T, VALC, L, U, CH, kPageStages>;
-  const size_t smem = (size_t)kPageWarps * kPageStages * CH * sizeof(E);
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  auto kern = spmv_pages_kernel<T, VALC, L, U, CH>;
+  const size_t smem = (size_t)kPageWarps * CH * sizeof(E);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return EDGPU_ERR_CUDA;
   }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kPageWarps, smem) != cudaSuccess ||
-      per_sm < 1) {
-    cudaGetLastError();
-    return EDGPU_ERR_CUDA;
-  }
-  int64_t blocks = (int64_t)grid_cap() * per_sm;
-  const int64_t need = (n_pages + kPageWarps - 1) / kPageWarps;
-  if (blocks > need) blocks = need > 0 ? need : 1;
+  const int64_t blocks = (n_pages + kPageWarps - 1) / kPageWarps;
+  if (blocks > 0x7fffffffLL) return EDGPU_ERR_ARG;
   kern<<<(unsigned)blocks, 32 * kPageWarps, smem, s>>>(n_pages, reinterpret_cast<const E*>(pages),
                                                         reinterpret_cast<const P*>(x), reinterpret_cast<P*>(y));
   note_launch();
@@ -463,6 +468,8 @@ int launch_pages_l(int64_t n_pages, const void* pages, int CH, int unroll, const
   if (CH == 256 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 256>(n_pages, pages, x, y, s);
   if (CH == 512 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 512>(n_pages, pages, x, y, s);
   if (CH == 512 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 512>(n_pages, pages, x, y, s);
+  if (CH == 1024 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 1024>(n_pages, pages, x, y, s);
+  if (CH == 1024 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 1024>(n_pages, pages, x, y, s);
   return EDGPU_ERR_ARG;
 }
 
@@ -482,16 +489,16 @@ int launch_pages(int64_t n_pages, const void* pages, int CH, int unroll, int L, 
 enum { kPagesRealF = 0, kPagesRealD = 1, kPagesCplxF = 2 };
 
 template <typename T, bool VALC>
-int fill_pages(const edgpu_csr* h, const T* vals, const int32_t* light, int64_t n_light, int C, int CH,
-               const int32_t* width, const int64_t* slice_pos, const int32_t* page_slice0, int64_t n_slices,
+int fill_pages(const edgpu_csr* h, const T* vals, const int32_t* sched, int64_t n_heavy, int C, int CH,
+               const int32_t* width, const int64_t* slice_pos, const int32_t* page_cols, int64_t n_slices,
                int64_t n_pages, void* pages, cudaStream_t s) {
   using E = Ent<T, VALC>;
   const int64_t total = n_pages * CH;
-  pages_clear_kernel<E><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_pages, CH, page_slice0,
+  pages_clear_kernel<E><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_pages, CH, page_cols,
                                                                         reinterpret_cast<E*>(pages));
   note_launch();
   pages_fill_kernel<T, VALC><<<(unsigned)((n_slices * 32 + 255) / 256), 256, 0, s>>>(
-      n_slices, n_light, C, CH, light, h->row_ptr, h->col, vals, width, slice_pos, reinterpret_cast<E*>(pages));
+      n_slices, n_heavy, h->n, C, sched, h->row_ptr, h->col, vals, width, slice_pos, reinterpret_cast<E*>(pages));
   note_launch();
   return check_launch();
 }
@@ -556,7 +563,7 @@ extern "C" int edgpu_spmv_planned_c64(const edgpu_csr* h, const int32_t* sched, 
 
 extern "C" size_t edgpu_spmv_pages_workspace(int64_t n, int lanes) {
   if (n < 1 || lanes < 1 || lanes > 32) return 0;
-  const int64_t C = 32 / lanes, n_slices = (n + C - 1) / C;
+  const int64_t n_slices = n;  // at most one slice per row
   return 256 + ((sizeof(int32_t) * (size_t)n_slices + 255) & ~(size_t)255) +
          ((sizeof(int64_t) * (size_t)n_slices + 255) & ~(size_t)255) + sizeof(int32_t) * (size_t)(n_slices + 2);
 }
@@ -565,8 +572,9 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
                                       int page_entries, int value_kind, void* pages, int64_t cap_pages,
                                       int64_t* n_pages, void* workspace, size_t workspace_bytes, void* stream) {
   if (!h || !sched || !n_pages || h->n < 1 || n_heavy < 0 || n_heavy > h->n) return EDGPU_ERR_ARG;
+  if (h->n >= (1ll << 31) - 2) return EDGPU_ERR_ARG;
   if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return EDGPU_ERR_ARG;
-  if (page_entries != 256 && page_entries != 512) return EDGPU_ERR_ARG;
+  if (page_entries != 256 && page_entries != 512 && page_entries != 1024) return EDGPU_ERR_ARG;
   const void* vals = value_kind == kPagesRealF ? (const void*)h->val_rf
                      : value_kind == kPagesRealD ? (const void*)h->val_r
                      : value_kind == kPagesCplxF ? (const void*)h->val_cf : nullptr;
@@ -574,17 +582,16 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
   if (workspace_bytes < edgpu_spmv_pages_workspace(h->n, lanes)) return EDGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   const int C = 32 / lanes, CH = page_entries;
-  const int64_t n_light = h->n - n_heavy, n_slices = (n_light + C - 1) / C;
+  const int64_t n_light = h->n - n_heavy, n_slices = n_heavy + (n_light + C - 1) / C;
   unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
   int32_t* width = reinterpret_cast<int32_t*>(ws + 256);
-  int64_t* slice_pos =
-      reinterpret_cast<int64_t*>(ws + 256 + ((sizeof(int32_t) * (size_t)n_slices + 255) & ~(size_t)255));
-  int32_t* page_slice0 = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(slice_pos) +
-                                                    ((sizeof(int64_t) * (size_t)n_slices + 255) & ~(size_t)255));
+  int64_t* slice_pos = reinterpret_cast<int64_t*>(ws + 256 + ((sizeof(int32_t) * (size_t)h->n + 255) & ~(size_t)255));
+  int32_t* page_cols = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(slice_pos) +
+                                                  ((sizeof(int64_t) * (size_t)h->n + 255) & ~(size_t)255));
   std::vector<int32_t> w_h((size_t)n_slices);
   if (n_slices > 0) {
-    pages_width_kernel<<<(unsigned)((n_slices + 255) / 256), 256, 0, s>>>(n_light, C, sched + n_heavy, h->row_ptr,
-                                                                          width);
+    pages_width_kernel<<<(unsigned)((n_slices + 255) / 256), 256, 0, s>>>(n_heavy, h->n, n_slices, C, sched,
+                                                                          h->row_ptr, width);
     note_launch();
     if (check_launch() != EDGPU_OK ||
         cudaMemcpyAsync(w_h.data(), width, sizeof(int32_t) * (size_t)n_slices, cudaMemcpyDeviceToHost, s) !=
@@ -594,20 +601,20 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
   }
   // greedy packing in schedule order: a page holds its header column and whole slices
   std::vector<int64_t> pos_h((size_t)n_slices);
-  std::vector<int32_t> ps0_h;  // used columns of each page (its header column included)
+  std::vector<int32_t> cols_h;  // used columns of each page (its header column included)
   int64_t page = 0, used = C;
   for (int64_t sl = 0; sl < n_slices; ++sl) {
     const int64_t size = (int64_t)C * (w_h[(size_t)sl] + 1);
-    if (size + C > CH) return EDGPU_ERR_ARG;  // a light row too long for the page size
+    if (size + C > CH) return EDGPU_ERR_ARG;  // a row too long for the page size
     if (used + size > CH) {
-      ps0_h.push_back((int32_t)(used / C));
+      cols_h.push_back((int32_t)(used / C));
       ++page;
       used = C;
     }
     pos_h[(size_t)sl] = page * CH + used;
     used += size;
   }
-  ps0_h.push_back((int32_t)(used / C));
+  cols_h.push_back((int32_t)(used / C));
   const int64_t np = n_slices > 0 ? page + 1 : 0;
   *n_pages = np;
   if (np > cap_pages || (np > 0 && !pages)) return EDGPU_ERR_OVERFLOW;
@@ -615,29 +622,28 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
   if ((reinterpret_cast<uintptr_t>(pages) & 15) != 0) return EDGPU_ERR_ARG;
   if (cudaMemcpyAsync(slice_pos, pos_h.data(), sizeof(int64_t) * (size_t)n_slices, cudaMemcpyHostToDevice, s) !=
           cudaSuccess ||
-      cudaMemcpyAsync(page_slice0, ps0_h.data(), sizeof(int32_t) * (size_t)np, cudaMemcpyHostToDevice, s) !=
+      cudaMemcpyAsync(page_cols, cols_h.data(), sizeof(int32_t) * (size_t)np, cudaMemcpyHostToDevice, s) !=
           cudaSuccess)
     return EDGPU_ERR_CUDA;
   int rc;
   if (value_kind == kPagesRealF)
-    rc = fill_pages<float, false>(h, h->val_rf, sched + n_heavy, n_light, C, CH, width, slice_pos, page_slice0,
-                                  n_slices, np, pages, s);
+    rc = fill_pages<float, false>(h, h->val_rf, sched, n_heavy, C, CH, width, slice_pos, page_cols, n_slices, np,
+                                  pages, s);
   else if (value_kind == kPagesRealD)
-    rc = fill_pages<double, false>(h, h->val_r, sched + n_heavy, n_light, C, CH, width, slice_pos, page_slice0,
-                                   n_slices, np, pages, s);
+    rc = fill_pages<double, false>(h, h->val_r, sched, n_heavy, C, CH, width, slice_pos, page_cols, n_slices, np,
+                                   pages, s);
   else
-    rc = fill_pages<float, true>(h, h->val_cf, sched + n_heavy, n_light, C, CH, width, slice_pos, page_slice0,
-                                 n_slices, np, pages, s);
+    rc = fill_pages<float, true>(h, h->val_cf, sched, n_heavy, C, CH, width, slice_pos, page_cols, n_slices, np,
+                                 pages, s);
   if (rc) return rc;
   // the host vectors above are read by the copies: wait for them before they go out of scope
   return cudaStreamSynchronize(s) == cudaSuccess ? EDGPU_OK : EDGPU_ERR_CUDA;
 }
 
 template <typename T>
-static int spmv_paged_impl(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, const void* pages,
-                           int64_t n_pages, int page_entries, int unroll, const void* x, void* y, int R,
-                           cudaStream_t s) {
-  if (!h || !sched || !x || !y || h->n < 1 || n_heavy < 0 || n_heavy > h->n || n_pages < 0) return EDGPU_ERR_ARG;
+static int spmv_paged_impl(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
+                           const void* x, void* y, int R, cudaStream_t s) {
+  if (!h || !x || !y || h->n < 1 || n_pages < 0) return EDGPU_ERR_ARG;
   if (n_pages > 0 && !pages) return EDGPU_ERR_ARG;
   if (unroll != 4 && unroll != 8) return EDGPU_ERR_ARG;
   constexpr int RV = Pack16<T>::runs;
@@ -646,34 +652,20 @@ static int spmv_paged_impl(const edgpu_csr* h, const int32_t* sched, int64_t n_h
   if (L != 2 && L != 4 && L != 8 && L != 16) return EDGPU_ERR_ARG;
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(pages)) & 15)
     return EDGPU_ERR_ARG;
-  int rc = EDGPU_OK;
-  const bool cf = sizeof(T) == 4 && h->val_cf;
-  const T* vc = sizeof(T) == 4 ? (const T*)h->val_cf : (const T*)h->val_c;
-  const T* vr = sizeof(T) == 4 ? (const T*)h->val_rf : (const T*)h->val_r;
-  if (sizeof(T) == 8 && h->val_c) return EDGPU_ERR_ARG;  // complex128 values have no paged layout
-  if (!vc && !vr) return EDGPU_ERR_ARG;
-  // heavy rows: one warp each, through the CSR
-  if (n_heavy > 0) {
-    rc = vc ? dispatch_lanes<T, true>(h, vc, sched, n_heavy, 4, 128, x, y, L, s, n_heavy)
-            : dispatch_lanes<T, false>(h, vr, sched, n_heavy, 4, 128, x, y, L, s, n_heavy);
-    if (rc) return rc;
-  }
+  if (sizeof(T) == 8 && (h->val_c || !h->val_r)) return EDGPU_ERR_ARG;  // complex128 values: no paged form
+  if (sizeof(T) == 4 && !h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
   if (n_pages == 0) return EDGPU_OK;
   if (sizeof(T) == 8) return launch_pages<double, false>(n_pages, pages, page_entries, unroll, L, x, y, s);
-  if (cf) return launch_pages<float, true>(n_pages, pages, page_entries, unroll, L, x, y, s);
+  if (h->val_cf) return launch_pages<float, true>(n_pages, pages, page_entries, unroll, L, x, y, s);
   return launch_pages<float, false>(n_pages, pages, page_entries, unroll, L, x, y, s);
 }
 
-extern "C" int edgpu_spmv_paged(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, const void* pages,
-                                int64_t n_pages, int page_entries, int unroll, const double* x, double* y, int R,
-                                void* stream) {
-  return spmv_paged_impl<double>(h, sched, n_heavy, pages, n_pages, page_entries, unroll, x, y, R,
-                                 (cudaStream_t)stream);
+extern "C" int edgpu_spmv_paged(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
+                                const double* x, double* y, int R, void* stream) {
+  return spmv_paged_impl<double>(h, pages, n_pages, page_entries, unroll, x, y, R, (cudaStream_t)stream);
 }
 
-extern "C" int edgpu_spmv_paged_c64(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, const void* pages,
-                                    int64_t n_pages, int page_entries, int unroll, const float* x, float* y, int R,
-                                    void* stream) {
-  return spmv_paged_impl<float>(h, sched, n_heavy, pages, n_pages, page_entries, unroll, x, y, R,
-                                (cudaStream_t)stream);
+extern "C" int edgpu_spmv_paged_c64(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries,
+                                    int unroll, const float* x, float* y, int R, void* stream) {
+  return spmv_paged_impl<float>(h, pages, n_pages, page_entries, unroll, x, y, R, (cudaStream_t)stream);
 }

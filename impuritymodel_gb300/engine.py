@@ -673,7 +673,7 @@ class Engine:
     SPMV_HEAVY = (16, 32, 64)
     SPMV_UNROLL = (4, 8)
     SPMV_BLOCK = (128, 256)
-    SPMV_PAGES = (256, 512)
+    SPMV_PAGES = (256, 512, 1024)
 
     @staticmethod
     def spmv_planned_ok(R, precision):
@@ -694,10 +694,21 @@ class Engine:
         lanes = R // (2 if precision else 1)
         kind = self._pages_kind(csr, precision)
         if kind is not None and lanes in (2, 4, 8, 16):
-            rows_per_slice = 32 // lanes
-            out += [("pages", w, hm, u, ch) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY
-                    for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES if rows_per_slice * (hm + 1) <= ch]
+            # a slice must fit a page: light rows are shorter than heavy_min, a heavy row is
+            # dealt to the row groups (its page share is about len / groups columns)
+            groups = 32 // lanes
+            max_len = self._max_row_len(csr)
+            for w in self.SPMV_WINDOWS:
+                for hm in self.SPMV_HEAVY:
+                    need = groups * (max(hm, -(-max_len // groups)) + 2)
+                    out += [("pages", w, hm, u, ch) for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES if need <= ch]
         return out
+
+    @staticmethod
+    def _max_row_len(csr):
+        if "_max_len" not in csr.__dict__:
+            csr._max_len = int((csr.row_ptr[1:] - csr.row_ptr[:-1]).max().item()) if csr.n else 0
+        return csr._max_len
 
     @staticmethod
     def _pages_kind(csr, precision):
@@ -760,8 +771,8 @@ class Engine:
             lanes = R // (2 if precision else 1)
             buf, npg = self.spmv_pages(csr, w, hm, lanes, last, self._pages_kind(csr, precision))
             fn = self.lib.edgpu_spmv_paged_c64 if precision else self.lib.edgpu_spmv_paged
-            L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, _ptr(buf), npg, int(last), int(u), _ptr(xr), _ptr(yr),
-                       int(R), self.stream), "spmv_paged")
+            L.check(fn(C.byref(csr.struct()), _ptr(buf), npg, int(last), int(u), _ptr(xr), _ptr(yr), int(R),
+                       self.stream), "spmv_paged")
             return
         fn = self.lib.edgpu_spmv_planned_c64 if precision else self.lib.edgpu_spmv_planned
         L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, int(u), int(last), _ptr(xr), _ptr(yr), int(R), self.stream),

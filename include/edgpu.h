@@ -210,35 +210,34 @@ int edgpu_spmv_planned_c64(const edgpu_csr* h, const int32_t* sched, int64_t n_h
                            const float* x, float* y, int R, void* stream);
 
 /*
- * Paged copy of the light rows of a schedule, for edgpu_spmv_paged[_c64].  The light rows
- * (sched[n_heavy..n)) are cut into slices of 32 / lanes rows (lanes = R / complex numbers per
- * 16 bytes: the lane count serving one row) and packed whole, in schedule order, into pages
- * of page_entries (256 or 512) entries: a header column, then per slice a header column (its
- * rows and width) and its entries column by column.  Entries are 8 bytes (value_kind 0: real
+ * Paged copy of a scheduled matrix, for edgpu_spmv_paged[_c64].  In schedule order, each
+ * heavy row (sched[0..n_heavy)) is a slice of its own whose entries are dealt in turn to the
+ * 32 / lanes row groups of a warp (lanes = R / complex numbers per 16 bytes: the lanes serving
+ * one row), and the light rows follow, 32 / lanes per slice; slices are packed whole into
+ * pages of page_entries (256, 512 or 1024) entries: a header column, then per slice a header
+ * column (its rows, heavy flag) and its entry columns.  Entries are 8 bytes (value_kind 0: real
  * float32 values from val_rf) or 16 bytes (1: real float64 from val_r; 2: complex64 from
  * val_cf).  Writes *n_pages; returns EDGPU_ERR_OVERFLOW without filling when it exceeds
  * cap_pages or pages is NULL (call again with room for *n_pages pages, 16-byte aligned), and
- * EDGPU_ERR_ARG when a light row does not fit a page (32 / lanes * (heavy_min + 1) entries
- * must not exceed page_entries).  Synchronises the stream.  No counterpart upstream (a layout
- * of upstream's sparse H for the product below).
+ * EDGPU_ERR_ARG when a slice does not fit a page.  Synchronises the stream.  No counterpart
+ * upstream (a layout of upstream's sparse H for the product below).
  */
 size_t edgpu_spmv_pages_workspace(int64_t n, int lanes);
 int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, int lanes, int page_entries,
                            int value_kind, void* pages, int64_t cap_pages, int64_t* n_pages, void* workspace,
                            size_t workspace_bytes, void* stream);
 /*
- * y = H x with the heavy rows of the schedule served through the CSR (one warp each) and the
- * light rows from the pages: each warp streams a contiguous range of pages into a shared-
- * memory ring with cp.async, four pages deep, and gathers x rows for them.  Two launches.
- * Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4, 8, 16}; unroll
- * 4 or 8.  complex128 H values have no paged form (EDGPU_ERR_ARG).  Replaces upstream's h.dot
- * (finite.py:1946-1989).
+ * y = H x from the pages of edgpu_spmv_pages_build, one launch: a warp copies one page into
+ * shared memory with cp.async and gathers the x rows its columns name, unroll (4 or 8) per
+ * lane in flight; heavy rows' partial sums are added across the warp's row groups with xor
+ * shuffles.  Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4, 8,
+ * 16} and equal to the lanes the pages were built for.  complex128 H values have no paged
+ * form (EDGPU_ERR_ARG).  Replaces upstream's h.dot (finite.py:1946-1989).
  */
-int edgpu_spmv_paged(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, const void* pages, int64_t n_pages,
-                     int page_entries, int unroll, const double* x, double* y, int R, void* stream);
-int edgpu_spmv_paged_c64(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, const void* pages,
-                         int64_t n_pages, int page_entries, int unroll, const float* x, float* y, int R,
-                         void* stream);
+int edgpu_spmv_paged(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
+                     const double* x, double* y, int R, void* stream);
+int edgpu_spmv_paged_c64(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
+                         const float* x, float* y, int R, void* stream);
 
 /*
  * Batched Lanczos tridiagonalisation without reorthogonalisation, R independent runs on one
