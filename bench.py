@@ -358,7 +358,7 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     _, n_heavy = eng.spmv_plan(csr, mapping[1], mapping[2])
     return {
         "bound": "hbm",
-        "kernel": ("spmv_sched_kernel (heavy rows) + spmv_pages_kernel<float> (edgpu_spmv_paged_c64)"
+        "kernel": ("spmv_pages_kernel<float> (edgpu_spmv_paged_c64)"
                    if mapping[0] == "pages" else "spmv_sched_kernel<float> (edgpu_spmv_planned_c64)"),
         "achieved": round(achieved, 1),
         "peak": peak,

@@ -254,7 +254,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 constexpr int kPageWarps = 4;  // warps (pages) per block of the paged kernel
 
-template <typename T, bool VALC, int L, int U, int CH>
+template <typename T, bool VALC, int L, int U, int CH, bool PIPE>
 __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_pages,
                                                                      const Ent<T, VALC>* __restrict__ pages,
                                                                      const typename Pack16<T>::type* __restrict__ X,
@@ -308,37 +308,41 @@ __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_p
     for (int q = 0; q < RV; ++q) ar[q] = ai[q] = T(0);
   };
   const int ncols = pg[0].c;
-  for (int k = 1; k < ncols; k += U) {
-    E en[U];
-    P xv[U];
+  E en[U];
+  P xv[U];
+  // batch k: U columns from shared memory, then their gathers (issued before the previous
+  // batch is consumed when PIPE, so two batches of gathers are in flight)
+  auto fetch = [&](int k, E* e, P* x) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       if (k + u < ncols) {
-        en[u] = pg[(k + u) * C + grp];
+        e[u] = pg[(k + u) * C + grp];
       } else {
-        en[u] = E{};
-        en[u].c = -1;
+        e[u] = E{};
+        e[u].c = -1;
       }
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = en[u].c >= 0 ? __ldg(X + (int64_t)en[u].c * L + sub) : P{};
+    for (int u = 0; u < U; ++u) x[u] = e[u].c >= 0 ? __ldg(X + (int64_t)e[u].c * L + sub) : P{};
+  };
+  auto consume = [&](const E* e, const P* x) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int c = en[u].c;
+      const int c = e[u].c;
       if (c <= -2) {  // a slice header column (the same kind in every group)
         flush();
         row = c == INT_MIN ? -1 : (int64_t)(-2 - (int64_t)c);
-        heavy = en[u].flag() != 0;
+        heavy = e[u].flag() != 0;
         continue;
       }
       if (c < 0) continue;
-      const T* xs = reinterpret_cast<const T*>(&xv[u]);
+      const T* xs = reinterpret_cast<const T*>(&x[u]);
       T hr, hi = T(0);
       if constexpr (VALC) {
-        hr = en[u].vr;
-        hi = en[u].vi;
+        hr = e[u].vr;
+        hi = e[u].vi;
       } else {
-        hr = en[u].v;
+        hr = e[u].v;
       }
 #pragma unroll
       for (int q = 0; q < RV; ++q) {
@@ -350,6 +354,23 @@ __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_p
           ai[q] += hi * xr;
         }
       }
+    }
+  };
+  if constexpr (PIPE) {
+    E en2[U];
+    P xv2[U];
+    if (1 < ncols) fetch(1, en, xv);
+    for (int k = 1; k < ncols; k += 2 * U) {
+      if (k + U < ncols) fetch(k + U, en2, xv2);
+      consume(en, xv);
+      if (k + U >= ncols) break;
+      if (k + 2 * U < ncols) fetch(k + 2 * U, en, xv);
+      consume(en2, xv2);
+    }
+  } else {
+    for (int k = 1; k < ncols; k += U) {
+      fetch(k, en, xv);
+      consume(en, xv);
     }
   }
   flush();
@@ -444,10 +465,10 @@ __global__ void pages_fill_kernel(int64_t n_slices, int64_t n_heavy, int64_t n_r
 }
 
 template <typename T, bool VALC, int L, int U, int CH>
-int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, cudaStream_t s) {
+int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, cudaStream_t s, bool pipe) {
   using P = typename Pack16<T>::type;
   using E = Ent<T, VALC>;
-  auto kern = spmv_pages_kernel<T, VALC, L, U, CH>;
+  auto kern = pipe ? spmv_pages_kernel<T, VALC, L, U, CH, true> : spmv_pages_kernel<T, VALC, L, U, CH, false>;
   const size_t smem = (size_t)kPageWarps * CH * sizeof(E);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
@@ -462,14 +483,17 @@ int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, c
   return check_launch();
 }
 
+// unroll: 4 or 8 gathers per lane per batch; negative: the same with two batches in flight
 template <typename T, bool VALC, int L>
 int launch_pages_l(int64_t n_pages, const void* pages, int CH, int unroll, const void* x, void* y, cudaStream_t s) {
-  if (CH == 256 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 256>(n_pages, pages, x, y, s);
-  if (CH == 256 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 256>(n_pages, pages, x, y, s);
-  if (CH == 512 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 512>(n_pages, pages, x, y, s);
-  if (CH == 512 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 512>(n_pages, pages, x, y, s);
-  if (CH == 1024 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 1024>(n_pages, pages, x, y, s);
-  if (CH == 1024 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 1024>(n_pages, pages, x, y, s);
+  const bool pipe = unroll < 0;
+  const int u = pipe ? -unroll : unroll;
+  if (CH == 256 && u == 4) return launch_pages_t<T, VALC, L, 4, 256>(n_pages, pages, x, y, s, pipe);
+  if (CH == 256 && u == 8) return launch_pages_t<T, VALC, L, 8, 256>(n_pages, pages, x, y, s, pipe);
+  if (CH == 512 && u == 4) return launch_pages_t<T, VALC, L, 4, 512>(n_pages, pages, x, y, s, pipe);
+  if (CH == 512 && u == 8) return launch_pages_t<T, VALC, L, 8, 512>(n_pages, pages, x, y, s, pipe);
+  if (CH == 1024 && u == 4) return launch_pages_t<T, VALC, L, 4, 1024>(n_pages, pages, x, y, s, pipe);
+  if (CH == 1024 && u == 8) return launch_pages_t<T, VALC, L, 8, 1024>(n_pages, pages, x, y, s, pipe);
   return EDGPU_ERR_ARG;
 }
 
@@ -645,7 +669,7 @@ static int spmv_paged_impl(const edgpu_csr* h, const void* pages, int64_t n_page
                            const void* x, void* y, int R, cudaStream_t s) {
   if (!h || !x || !y || h->n < 1 || n_pages < 0) return EDGPU_ERR_ARG;
   if (n_pages > 0 && !pages) return EDGPU_ERR_ARG;
-  if (unroll != 4 && unroll != 8) return EDGPU_ERR_ARG;
+  if (unroll != 4 && unroll != 8 && unroll != -4 && unroll != -8) return EDGPU_ERR_ARG;
   constexpr int RV = Pack16<T>::runs;
   if (R % RV) return EDGPU_ERR_ARG;
   const int L = R / RV;

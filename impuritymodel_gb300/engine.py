@@ -687,8 +687,9 @@ class Engine:
         """Launch mappings of H.v that the autotuner chooses from, as tuples:
         ("sched", window, heavy_min, unroll, block): every row through the CSR, heavy rows
         one warp each, light rows in length-sorted windows;
-        ("pages", window, heavy_min, unroll, page_entries): the same heavy rows, the light
-        rows from a paged copy streamed through shared memory (real values, or complex64)."""
+        ("pages", window, heavy_min, unroll, page_entries): the same schedule packed into
+        pages that one warp each copies into shared memory (real values, or complex64);
+        a negative unroll keeps two batches of gathers in flight."""
         out = [("sched", w, hm, u, b) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY for u in self.SPMV_UNROLL
                for b in self.SPMV_BLOCK]
         lanes = R // (2 if precision else 1)
@@ -701,7 +702,8 @@ class Engine:
             for w in self.SPMV_WINDOWS:
                 for hm in self.SPMV_HEAVY:
                     need = groups * (max(hm, -(-max_len // groups)) + 2)
-                    out += [("pages", w, hm, u, ch) for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES if need <= ch]
+                    out += [("pages", w, hm, u, ch) for u in self.SPMV_UNROLL + tuple(-x for x in self.SPMV_UNROLL)
+                            for ch in self.SPMV_PAGES if need <= ch]
         return out
 
     @staticmethod

@@ -229,8 +229,9 @@ int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, int64_t n_h
 /*
  * y = H x from the pages of edgpu_spmv_pages_build, one launch: a warp copies one page into
  * shared memory with cp.async and gathers the x rows its columns name, unroll (4 or 8) per
- * lane in flight; heavy rows' partial sums are added across the warp's row groups with xor
- * shuffles.  Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4, 8,
+ * lane in flight (-4 or -8: the next batch's gathers are issued before the current batch is
+ * added up, so two batches are in flight); heavy rows' partial sums are added across the
+ * warp's row groups with xor shuffles.  Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4, 8,
  * 16} and equal to the lanes the pages were built for.  complex128 H values have no paged
  * form (EDGPU_ERR_ARG).  Replaces upstream's h.dot (finite.py:1946-1989).
  */
