@@ -369,7 +369,7 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
         "avg_launch_us": round(avg_s * 1e6, 2),
         "launches": launches,
         "mapping": {"kernel": mapping[0], "window": mapping[1], "heavy_min": mapping[2], "unroll": mapping[3],
-                    ("page_entries" if mapping[0] == "pages" else "block"): mapping[4],
+                    ("page_entries" if mapping[0] == "pages" else "block"): mapping[4], "flags": mapping[5],
                     "heavy_rows": int(n_heavy), "tune_s": round(tune_s, 3),
                     "candidates_us": get_tuner_report("spmv", eng.spmv_key(csr, R, 1))},
         "row_kernel_us": round(rows_s * 1e6, 2),

@@ -100,8 +100,8 @@ SIGNATURES = {
     "edgpu_spmv_planned_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P]),
     "edgpu_spmv_pages_workspace": (_SZ, [_I64, _I]),
     "edgpu_spmv_pages_build": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _I64, C.POINTER(_I64), _P, _SZ, _P]),
-    "edgpu_spmv_paged": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P]),
-    "edgpu_spmv_paged_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P]),
+    "edgpu_spmv_paged": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _P, _I, _P]),
+    "edgpu_spmv_paged_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _P, _I, _P]),
     "edgpu_lanczos_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_lanczos": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),

@@ -249,12 +249,42 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16_hint(void* smem, const void* gmem, uint64_t pol) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "l"(pol)
+               : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// L2 eviction-priority policies (PTX createpolicy): x rows are gathered nnz times and should
+// stay in L2; pages are read once.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float4 ldg_hint(const float4* ptr, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;\n"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(ptr), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ldg_hint(const double2* ptr, uint64_t pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;\n" : "=d"(v.x), "=d"(v.y) : "l"(ptr), "l"(pol));
+  return v;
+}
+
 constexpr int kPageWarps = 4;  // warps (pages) per block of the paged kernel
 
-template <typename T, bool VALC, int L, int U, int CH, bool PIPE>
+template <typename T, bool VALC, int L, int U, int CH, bool PIPE, bool HINT>
 __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_pages,
                                                                      const Ent<T, VALC>* __restrict__ pages,
                                                                      const typename Pack16<T>::type* __restrict__ X,
@@ -270,11 +300,19 @@ __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_p
   const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (p >= n_pages) return;  // warp-uniform
   E* pg = reinterpret_cast<E*>(page_raw) + (size_t)wib * CH;
+  uint64_t pol_x = 0;
   {
     const unsigned char* src = reinterpret_cast<const unsigned char*>(pages + p * CH);
     unsigned char* dst = reinterpret_cast<unsigned char*>(pg);
+    if constexpr (HINT) {
+      pol_x = l2_policy_evict_last();
+      const uint64_t pol_p = l2_policy_evict_first();
 #pragma unroll
-    for (int k = lane; k < CHUNKS; k += 32) cp_async16(dst + 16 * k, src + 16 * k);
+      for (int k = lane; k < CHUNKS; k += 32) cp_async16_hint(dst + 16 * k, src + 16 * k, pol_p);
+    } else {
+#pragma unroll
+      for (int k = lane; k < CHUNKS; k += 32) cp_async16(dst + 16 * k, src + 16 * k);
+    }
     cp_async_commit();
     cp_async_wait_all();
     __syncwarp();
@@ -323,7 +361,13 @@ __global__ void __launch_bounds__(32 * kPageWarps) spmv_pages_kernel(int64_t n_p
       }
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) x[u] = e[u].c >= 0 ? __ldg(X + (int64_t)e[u].c * L + sub) : P{};
+    for (int u = 0; u < U; ++u) {
+      if constexpr (HINT) {
+        x[u] = e[u].c >= 0 ? ldg_hint(X + (int64_t)e[u].c * L + sub, pol_x) : P{};
+      } else {
+        x[u] = e[u].c >= 0 ? __ldg(X + (int64_t)e[u].c * L + sub) : P{};
+      }
+    }
   };
   auto consume = [&](const E* e, const P* x) {
 #pragma unroll
@@ -465,10 +509,13 @@ __global__ void pages_fill_kernel(int64_t n_slices, int64_t n_heavy, int64_t n_r
 }
 
 template <typename T, bool VALC, int L, int U, int CH>
-int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, cudaStream_t s, bool pipe) {
+int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, cudaStream_t s, int flags) {
   using P = typename Pack16<T>::type;
   using E = Ent<T, VALC>;
-  auto kern = pipe ? spmv_pages_kernel<T, VALC, L, U, CH, true> : spmv_pages_kernel<T, VALC, L, U, CH, false>;
+  auto kern = (flags & 1) ? ((flags & 2) ? spmv_pages_kernel<T, VALC, L, U, CH, true, true>
+                                         : spmv_pages_kernel<T, VALC, L, U, CH, true, false>)
+                          : ((flags & 2) ? spmv_pages_kernel<T, VALC, L, U, CH, false, true>
+                                         : spmv_pages_kernel<T, VALC, L, U, CH, false, false>);
   const size_t smem = (size_t)kPageWarps * CH * sizeof(E);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
@@ -483,28 +530,28 @@ int launch_pages_t(int64_t n_pages, const void* pages, const void* x, void* y, c
   return check_launch();
 }
 
-// unroll: 4 or 8 gathers per lane per batch; negative: the same with two batches in flight
+// unroll: 4 or 8 gathers per lane per batch; flags bit 0: two batches in flight, bit 1: L2
+// eviction hints (x rows evict-last, pages evict-first)
 template <typename T, bool VALC, int L>
-int launch_pages_l(int64_t n_pages, const void* pages, int CH, int unroll, const void* x, void* y, cudaStream_t s) {
-  const bool pipe = unroll < 0;
-  const int u = pipe ? -unroll : unroll;
-  if (CH == 256 && u == 4) return launch_pages_t<T, VALC, L, 4, 256>(n_pages, pages, x, y, s, pipe);
-  if (CH == 256 && u == 8) return launch_pages_t<T, VALC, L, 8, 256>(n_pages, pages, x, y, s, pipe);
-  if (CH == 512 && u == 4) return launch_pages_t<T, VALC, L, 4, 512>(n_pages, pages, x, y, s, pipe);
-  if (CH == 512 && u == 8) return launch_pages_t<T, VALC, L, 8, 512>(n_pages, pages, x, y, s, pipe);
-  if (CH == 1024 && u == 4) return launch_pages_t<T, VALC, L, 4, 1024>(n_pages, pages, x, y, s, pipe);
-  if (CH == 1024 && u == 8) return launch_pages_t<T, VALC, L, 8, 1024>(n_pages, pages, x, y, s, pipe);
+int launch_pages_l(int64_t n_pages, const void* pages, int CH, int unroll, int flags, const void* x, void* y,
+                   cudaStream_t s) {
+  if (CH == 256 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 256>(n_pages, pages, x, y, s, flags);
+  if (CH == 256 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 256>(n_pages, pages, x, y, s, flags);
+  if (CH == 512 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 512>(n_pages, pages, x, y, s, flags);
+  if (CH == 512 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 512>(n_pages, pages, x, y, s, flags);
+  if (CH == 1024 && unroll == 4) return launch_pages_t<T, VALC, L, 4, 1024>(n_pages, pages, x, y, s, flags);
+  if (CH == 1024 && unroll == 8) return launch_pages_t<T, VALC, L, 8, 1024>(n_pages, pages, x, y, s, flags);
   return EDGPU_ERR_ARG;
 }
 
 template <typename T, bool VALC>
-int launch_pages(int64_t n_pages, const void* pages, int CH, int unroll, int L, const void* x, void* y,
+int launch_pages(int64_t n_pages, const void* pages, int CH, int unroll, int flags, int L, const void* x, void* y,
                  cudaStream_t s) {
   switch (L) {
-    case 2: return launch_pages_l<T, VALC, 2>(n_pages, pages, CH, unroll, x, y, s);
-    case 4: return launch_pages_l<T, VALC, 4>(n_pages, pages, CH, unroll, x, y, s);
-    case 8: return launch_pages_l<T, VALC, 8>(n_pages, pages, CH, unroll, x, y, s);
-    case 16: return launch_pages_l<T, VALC, 16>(n_pages, pages, CH, unroll, x, y, s);
+    case 2: return launch_pages_l<T, VALC, 2>(n_pages, pages, CH, unroll, flags, x, y, s);
+    case 4: return launch_pages_l<T, VALC, 4>(n_pages, pages, CH, unroll, flags, x, y, s);
+    case 8: return launch_pages_l<T, VALC, 8>(n_pages, pages, CH, unroll, flags, x, y, s);
+    case 16: return launch_pages_l<T, VALC, 16>(n_pages, pages, CH, unroll, flags, x, y, s);
     default: return EDGPU_ERR_ARG;
   }
 }
@@ -666,10 +713,10 @@ extern "C" int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, 
 
 template <typename T>
 static int spmv_paged_impl(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
-                           const void* x, void* y, int R, cudaStream_t s) {
+                           int flags, const void* x, void* y, int R, cudaStream_t s) {
   if (!h || !x || !y || h->n < 1 || n_pages < 0) return EDGPU_ERR_ARG;
   if (n_pages > 0 && !pages) return EDGPU_ERR_ARG;
-  if (unroll != 4 && unroll != 8 && unroll != -4 && unroll != -8) return EDGPU_ERR_ARG;
+  if ((unroll != 4 && unroll != 8) || flags < 0 || flags > 3) return EDGPU_ERR_ARG;
   constexpr int RV = Pack16<T>::runs;
   if (R % RV) return EDGPU_ERR_ARG;
   const int L = R / RV;
@@ -679,17 +726,17 @@ static int spmv_paged_impl(const edgpu_csr* h, const void* pages, int64_t n_page
   if (sizeof(T) == 8 && (h->val_c || !h->val_r)) return EDGPU_ERR_ARG;  // complex128 values: no paged form
   if (sizeof(T) == 4 && !h->val_cf && !h->val_rf) return EDGPU_ERR_ARG;
   if (n_pages == 0) return EDGPU_OK;
-  if (sizeof(T) == 8) return launch_pages<double, false>(n_pages, pages, page_entries, unroll, L, x, y, s);
-  if (h->val_cf) return launch_pages<float, true>(n_pages, pages, page_entries, unroll, L, x, y, s);
-  return launch_pages<float, false>(n_pages, pages, page_entries, unroll, L, x, y, s);
+  if (sizeof(T) == 8) return launch_pages<double, false>(n_pages, pages, page_entries, unroll, flags, L, x, y, s);
+  if (h->val_cf) return launch_pages<float, true>(n_pages, pages, page_entries, unroll, flags, L, x, y, s);
+  return launch_pages<float, false>(n_pages, pages, page_entries, unroll, flags, L, x, y, s);
 }
 
 extern "C" int edgpu_spmv_paged(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
-                                const double* x, double* y, int R, void* stream) {
-  return spmv_paged_impl<double>(h, pages, n_pages, page_entries, unroll, x, y, R, (cudaStream_t)stream);
+                                int flags, const double* x, double* y, int R, void* stream) {
+  return spmv_paged_impl<double>(h, pages, n_pages, page_entries, unroll, flags, x, y, R, (cudaStream_t)stream);
 }
 
 extern "C" int edgpu_spmv_paged_c64(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries,
-                                    int unroll, const float* x, float* y, int R, void* stream) {
-  return spmv_paged_impl<float>(h, pages, n_pages, page_entries, unroll, x, y, R, (cudaStream_t)stream);
+                                    int unroll, int flags, const float* x, float* y, int R, void* stream) {
+  return spmv_paged_impl<float>(h, pages, n_pages, page_entries, unroll, flags, x, y, R, (cudaStream_t)stream);
 }

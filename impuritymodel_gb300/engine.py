@@ -685,13 +685,13 @@ class Engine:
 
     def spmv_candidates(self, csr, R, precision):
         """Launch mappings of H.v that the autotuner chooses from, as tuples:
-        ("sched", window, heavy_min, unroll, block): every row through the CSR, heavy rows
+        ("sched", window, heavy_min, unroll, block, 0): every row through the CSR, heavy rows
         one warp each, light rows in length-sorted windows;
-        ("pages", window, heavy_min, unroll, page_entries): the same schedule packed into
-        pages that one warp each copies into shared memory (real values, or complex64);
-        a negative unroll keeps two batches of gathers in flight."""
-        out = [("sched", w, hm, u, b) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY for u in self.SPMV_UNROLL
-               for b in self.SPMV_BLOCK]
+        ("pages", window, heavy_min, unroll, page_entries, flags): the same schedule packed
+        into pages that one warp each copies into shared memory (real values, or complex64);
+        flags bit 0 keeps two batches of gathers in flight, bit 1 adds L2 eviction hints."""
+        out = [("sched", w, hm, u, b, 0) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY
+               for u in self.SPMV_UNROLL for b in self.SPMV_BLOCK]
         lanes = R // (2 if precision else 1)
         kind = self._pages_kind(csr, precision)
         if kind is not None and lanes in (2, 4, 8, 16):
@@ -702,8 +702,8 @@ class Engine:
             for w in self.SPMV_WINDOWS:
                 for hm in self.SPMV_HEAVY:
                     need = groups * (max(hm, -(-max_len // groups)) + 2)
-                    out += [("pages", w, hm, u, ch) for u in self.SPMV_UNROLL + tuple(-x for x in self.SPMV_UNROLL)
-                            for ch in self.SPMV_PAGES if need <= ch]
+                    out += [("pages", w, hm, u, ch, f) for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES
+                            for f in (0, 1, 2, 3) if need <= ch]
         return out
 
     @staticmethod
@@ -767,14 +767,14 @@ class Engine:
                                 lambda c: self._spmv_planned(csr, xr, yr, R, precision, c))
 
     def _spmv_planned(self, csr, xr, yr, R, precision, mapping):
-        kernel, w, hm, u, last = mapping
+        kernel, w, hm, u, last, flags = mapping
         sched, nh = self.spmv_plan(csr, w, hm)
         if kernel == "pages":
             lanes = R // (2 if precision else 1)
             buf, npg = self.spmv_pages(csr, w, hm, lanes, last, self._pages_kind(csr, precision))
             fn = self.lib.edgpu_spmv_paged_c64 if precision else self.lib.edgpu_spmv_paged
-            L.check(fn(C.byref(csr.struct()), _ptr(buf), npg, int(last), int(u), _ptr(xr), _ptr(yr), int(R),
-                       self.stream), "spmv_paged")
+            L.check(fn(C.byref(csr.struct()), _ptr(buf), npg, int(last), int(u), int(flags), _ptr(xr), _ptr(yr),
+                       int(R), self.stream), "spmv_paged")
             return
         fn = self.lib.edgpu_spmv_planned_c64 if precision else self.lib.edgpu_spmv_planned
         L.check(fn(C.byref(csr.struct()), _ptr(sched), nh, int(u), int(last), _ptr(xr), _ptr(yr), int(R), self.stream),

@@ -229,16 +229,17 @@ int edgpu_spmv_pages_build(const edgpu_csr* h, const int32_t* sched, int64_t n_h
 /*
  * y = H x from the pages of edgpu_spmv_pages_build, one launch: a warp copies one page into
  * shared memory with cp.async and gathers the x rows its columns name, unroll (4 or 8) per
- * lane in flight (-4 or -8: the next batch's gathers are issued before the current batch is
- * added up, so two batches are in flight); heavy rows' partial sums are added across the
- * warp's row groups with xor shuffles.  Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4, 8,
- * 16} and equal to the lanes the pages were built for.  complex128 H values have no paged
+ * lane in flight; heavy rows' partial sums are added across the warp's row groups with xor
+ * shuffles.  flags bit 0: the next batch's gathers are issued before the current batch is
+ * added up (two batches in flight); bit 1: L2 eviction hints (x rows evict-last, pages
+ * evict-first).  Vectors as edgpu_spmv_planned; R / (complex numbers per 16 bytes) in {2, 4,
+ * 8, 16} and equal to the lanes the pages were built for.  complex128 H values have no paged
  * form (EDGPU_ERR_ARG).  Replaces upstream's h.dot (finite.py:1946-1989).
  */
-int edgpu_spmv_paged(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
+int edgpu_spmv_paged(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll, int flags,
                      const double* x, double* y, int R, void* stream);
 int edgpu_spmv_paged_c64(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int unroll,
-                         const float* x, float* y, int R, void* stream);
+                         int flags, const float* x, float* y, int R, void* stream);
 
 /*
  * Batched Lanczos tridiagonalisation without reorthogonalisation, R independent runs on one
