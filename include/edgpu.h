@@ -352,6 +352,55 @@ void edgpu_set_small_reserve(int slots);
 void edgpu_set_reorth_fused(int enabled);
 
 /*
+ * Matrix-free H·v on a sorted sector basis (n states, n_words words each), for sectors whose
+ * CSR is not kept.  Upstream builds the same matrix elements column by column with applyOp
+ * (impurityModel/ed/finite.py:1514-1693) and multiplies with h.dot (finite.py:1946-1989).
+ * The operator comes split in two term tables (edgpu_terms encoding):
+ *   diagonal terms (those that map a product state onto itself): edgpu_hv_diag sums them per
+ *     basis state into d[n] (FP64, term order) once per sector;
+ *   off-diagonal terms, sorted by their key orbital (the first orbital a term creates without
+ *     annihilating it, which must be empty in the state it acts on); bucket[k]..bucket[k+1]
+ *     (host-built, device array of n_orb + 1 offsets) are the terms of key orbital k.
+ * edgpu_hv_matfree: y = (H - shift I) x for R vectors ([n][R], complex128, or complex64 with
+ * float32 accumulation for the _c64 form; 16-byte aligned; R / complex numbers per 16 bytes
+ * dividing 32).  Row i applies only the terms keyed on the empty orbitals of b_i, keeps the
+ * results inside ``restr`` and the basis (binary search), and adds conj(h) x_j; the diagonal
+ * (d_i - shift) x_i.  complex_terms = 0 when every coefficient is real.
+ */
+int edgpu_hv_diag(int n_words, const uint64_t* basis, int64_t n, const edgpu_terms* diag_terms, double* d,
+                  void* stream);
+int edgpu_hv_matfree(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
+                     const edgpu_terms* offdiag_terms, int complex_terms, const edgpu_restrictions* restr,
+                     const double* diag, double shift, const double* x, double* y, int R, void* stream);
+int edgpu_hv_matfree_c64(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
+                         const edgpu_terms* offdiag_terms, int complex_terms, const edgpu_restrictions* restr,
+                         const double* diag, double shift, const float* x, float* y, int R, void* stream);
+
+/*
+ * Pieces of a batched Lanczos with full reorthogonalisation for large sectors (R runs; a
+ * Krylov vector is [n][R] complex, the basis V[m][n][R] with `stride` complex numbers between
+ * consecutive vectors; precision 1: complex64 vectors, 0: complex128).  Reductions are
+ * accumulated in FP64 (each thread's partial over up to 8 rows in the vector type, then FP64,
+ * blocks summed in a fixed order).  Used as: w = H v_j; h = V[0..j]^H w; w -= V h (alpha_j =
+ * Re h_j); again; beta_j = |w|; v_{j+1} = w / beta_j.  Replaces upstream's recurrence
+ * (finite.py:1897-1995) where a complex64 recurrence without reorthogonalisation would lose
+ * orthogonality.
+ *   edgpu_krylov_dot:       h[k][r] = sum_i conj(V[k][i][r]) w[i][r], k < m (complex128 out).
+ *   edgpu_krylov_project:   w[i][r] -= sum_k h[k][r] V[k][i][r]; with_norm: leaves per-block
+ *                           |w|^2 partials in the workspace for edgpu_krylov_normalize.
+ *   edgpu_krylov_normalize: beta[r] = |w[.][r]| (FP64) and v = w / beta; beta == 0 sets
+ *                           *status_dev = EDGPU_ERR_BREAKDOWN and v = 0 for that run.
+ * R <= 256.  The workspace (edgpu_krylov_workspace for the largest m) is shared by the three.
+ */
+size_t edgpu_krylov_workspace(int64_t n, int R, int m_max);
+int edgpu_krylov_dot(int precision, const void* V, int64_t stride, int m, int64_t n, int R, const void* w, double* h,
+                     void* workspace, size_t workspace_bytes, void* stream);
+int edgpu_krylov_project(int precision, const void* V, int64_t stride, int m, int64_t n, int R, const double* h,
+                         void* w, int with_norm, void* workspace, size_t workspace_bytes, void* stream);
+int edgpu_krylov_normalize(int precision, int64_t n, int R, const void* w, void* v, double* beta, int32_t* status_dev,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Shifted solves X[r][z] = (zs[r][z] - H)^{-1} Y[r] for n_rhs right-hand sides (Y: [n_rhs][n]
  * complex128) and nz <= 512 complex shifts each, from one Krylov space per right-hand side
  * (Lanczos, FP64, CTA per right-hand side), iterated until every shift's residual estimate
