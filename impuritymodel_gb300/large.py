@@ -161,13 +161,29 @@ def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K
                 eng.spmv_into(csr, torch.view_as_real(x), torch.view_as_real(y), x.shape[1], precision=0)
             else:
                 y.copy_(eng.spmv(csr, x))
+    # the H.v kernels serve R / (complex numbers per 16 bytes) lanes per row, a divisor of
+    # 32: the run count is padded with empty runs (they stop at their first step)
+    R = v0.shape[1]
+    runs16 = 2 if precision else 1
+    if R > 32 * runs16:  # more runs than one H.v launch serves: in chunks
+        parts = [green_large(eng, dop, mop, restr, sector, v0[:, c:c + 32 * runs16], scale[c:c + 32 * runs16],
+                             e_runs[c:c + 32 * runs16], omega, delta, K, precision, matfree)
+                 for c in range(0, R, 32 * runs16)]
+        Kc = max(p[1].shape[1] for p in parts)
+        pad = lambda x: np.pad(x, ((0, 0), (0, Kc - x.shape[1])))  # noqa: E731
+        return (np.concatenate([p[0] for p in parts]), np.concatenate([pad(p[1]) for p in parts]),
+                np.concatenate([pad(p[2]) for p in parts]), np.concatenate([p[3] for p in parts]))
+    Rp = runs16
+    while Rp < R:
+        Rp *= 2
+    if Rp != R:
+        v0 = torch.cat([v0, torch.zeros((v0.shape[0], Rp - R), dtype=v0.dtype, device=v0.device)], 1)
     a, b, k_len = lanczos_reorth_batched(eng, apply_h, v0, K, precision, shift)
-    Kc = a.shape[1]
+    a, b, k_len = a[:R], b[:R], k_len[:R]
     at = torch.from_numpy(np.ascontiguousarray(a)).to(eng.device)
     bt = torch.from_numpy(np.ascontiguousarray(b)).to(eng.device)
     g = eng.cfrac(at, bt, k_len, omega, delta, np.asarray(e_runs, dtype=np.float64),
                   np.asarray(scale, dtype=np.float64))
-    del Kc
     return eng.to_host(g), a, b, k_len
 
 
