@@ -603,7 +603,7 @@ def large_config(eng, K=150, n_states=1):
 
     from impuritymodel_gb300 import finite, models
     from impuritymodel_gb300.engine import DeviceOp, make_restrictions
-    from impuritymodel_gb300.large import MatfreeOp, hv_diag, hv_matfree_into, spectra_large
+    from impuritymodel_gb300.large import MatfreeOp, hv_diag, hv_matfree_into, spectra_large, state_hash
 
     mod = models.make_model("config4")
     n = mod.n_spin_orbitals
@@ -644,13 +644,14 @@ def large_config(eng, K=150, n_states=1):
         while R < info["runs"]:
             R *= 2
         d = hv_diag(eng, sector.basis, mop)
+        table = state_hash(eng, sector.basis)
         x = torch.randn((sector.n, R), dtype=torch.complex64, device=eng.device)
         y = torch.empty_like(x)
-        hv_matfree_into(eng, sector.basis, mop, restr, d, x, y)
+        hv_matfree_into(eng, sector.basis, mop, restr, d, x, y, 0.0, table)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         for _ in range(5):
-            hv_matfree_into(eng, sector.basis, mop, restr, d, x, y)
+            hv_matfree_into(eng, sector.basis, mop, restr, d, x, y, 0.0, table)
         b.record()
         torch.cuda.synchronize()
         hv_us = a.elapsed_time(b) * 1e3 / 5

@@ -37,10 +37,13 @@ constexpr int kKmChunk = 8;  // products summed in the vector type before an FP6
 
 inline int rows_per_block(int R) { return kKmThreads / R; }
 
-// partial[k][b][r] = sum over this block's rows of conj(V[k][i][r]) * w[i][r]
+// partial[k][b][r] = sum over this block's rows of conj(V[k][i][r]) * w[i][r], for the KD
+// vectors k = blockIdx.y * KD + kk (w is read once for all of them)
+constexpr int KD = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(kKmThreads) krylov_dot_kernel(const typename Cplx<T>::type* __restrict__ V,
-                                                               int64_t stride, int64_t n, int R,
+                                                               int64_t stride, int m, int64_t n, int R,
                                                                const typename Cplx<T>::type* __restrict__ w,
                                                                double2* __restrict__ partial) {
   using CT = typename Cplx<T>::type;
@@ -48,40 +51,55 @@ __global__ void __launch_bounds__(kKmThreads) krylov_dot_kernel(const typename C
   const int rpb = kKmThreads / R;
   const int tid = threadIdx.x;
   const int r = tid % R, rr = tid / R;
-  const int k = blockIdx.y;
-  const CT* vk = V + (int64_t)k * stride;
-  double sr = 0.0, si = 0.0;
+  const int k0 = blockIdx.y * KD;
+  const int kn = m - k0 < KD ? m - k0 : KD;
+  double sr[KD], si[KD];
+#pragma unroll
+  for (int kk = 0; kk < KD; ++kk) sr[kk] = si[kk] = 0.0;
   if (rr < rpb) {
     const int64_t step = (int64_t)gridDim.x * rpb;
     int64_t i = (int64_t)blockIdx.x * rpb + rr;
     while (i < n) {
-      T cr = T(0), ci = T(0);
+      T cr[KD], ci[KD];
 #pragma unroll
+      for (int kk = 0; kk < KD; ++kk) cr[kk] = ci[kk] = T(0);
+#pragma unroll 1
       for (int c = 0; c < kKmChunk; ++c) {
         if (i < n) {
-          const CT a = vk[i * R + r];
           const CT b = w[i * R + r];
-          cr += a.x * b.x + a.y * b.y;
-          ci += a.x * b.y - a.y * b.x;
+#pragma unroll
+          for (int kk = 0; kk < KD; ++kk) {
+            if (kk < kn) {
+              const CT a = V[(int64_t)(k0 + kk) * stride + i * R + r];
+              cr[kk] += a.x * b.x + a.y * b.y;
+              ci[kk] += a.x * b.y - a.y * b.x;
+            }
+          }
         }
         i += step;
       }
-      sr += (double)cr;
-      si += (double)ci;
+#pragma unroll
+      for (int kk = 0; kk < KD; ++kk) {
+        sr[kk] += (double)cr[kk];
+        si[kk] += (double)ci[kk];
+      }
     }
   }
-  red[tid] = make_double2(sr, si);
-  __syncthreads();
-  // rows of the block: fixed tree over rr for each r
-  for (int h = (rpb + 1) / 2, len = rpb; len > 1; len = h, h = (h + 1) / 2) {
-    if (rr < len - h && rr + h < len) {
-      const double2 o = red[(rr + h) * R + r];
-      red[tid].x += o.x;
-      red[tid].y += o.y;
+  for (int kk = 0; kk < kn; ++kk) {
+    red[tid] = make_double2(sr[kk], si[kk]);
+    __syncthreads();
+    // rows of the block: fixed tree over rr for each r
+    for (int h = (rpb + 1) / 2, len = rpb; len > 1; len = h, h = (h + 1) / 2) {
+      if (rr < len - h && rr + h < len) {
+        const double2 o = red[(rr + h) * R + r];
+        red[tid].x += o.x;
+        red[tid].y += o.y;
+      }
+      __syncthreads();
     }
+    if (rr == 0) partial[((int64_t)(k0 + kk) * gridDim.x + blockIdx.x) * R + r] = red[r];
     __syncthreads();
   }
-  if (rr == 0) partial[((int64_t)k * gridDim.x + blockIdx.x) * R + r] = red[r];
 }
 
 // h[k][r] = sum over blocks of partial[k][b][r] (block order)
@@ -204,12 +222,12 @@ extern "C" int edgpu_krylov_dot(int precision, const void* V, int64_t stride, in
   cudaStream_t s = (cudaStream_t)stream;
   const int nb = km_blocks(n, R);
   double2* partial = reinterpret_cast<double2*>(workspace);
-  dim3 grid(nb, m);
+  dim3 grid(nb, (m + KD - 1) / KD);
   if (precision == 1)
-    krylov_dot_kernel<float><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const float2*>(V), stride, n, R,
+    krylov_dot_kernel<float><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const float2*>(V), stride, m, n, R,
                                                          reinterpret_cast<const float2*>(w), partial);
   else
-    krylov_dot_kernel<double><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const double2*>(V), stride, n, R,
+    krylov_dot_kernel<double><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const double2*>(V), stride, m, n, R,
                                                           reinterpret_cast<const double2*>(w), partial);
   note_launch();
   const int64_t t = (int64_t)m * R;

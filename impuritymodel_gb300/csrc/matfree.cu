@@ -32,6 +32,48 @@ struct MfPack<double> {
   static constexpr int runs = 1;
 };
 
+// Open-addressing hash of product states (edgpu_state_hash_build): slot -> basis index or -1,
+// linear probing in a power-of-two table at most half full, so a lookup is one or two table
+// reads and one basis read instead of ~log2(n) dependent basis reads of a binary search.
+template <int W>
+__device__ __forceinline__ uint64_t state_hash(const uint64_t (&s)[W]) {
+  uint64_t h = 0x243F6A8885A308D3ull;
+#pragma unroll
+  for (int q = 0; q < W; ++q) {
+    h ^= s[q] + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 31;
+  }
+  return h;
+}
+
+template <int W>
+__global__ void state_hash_insert_kernel(const uint64_t* __restrict__ basis, int64_t n, int32_t* table,
+                                         uint64_t mask) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t s[W];
+  load_state<W>(basis + i * W, s);
+  uint64_t slot = state_hash<W>(s) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    if (atomicCAS(reinterpret_cast<int*>(table + slot), -1, (int)i) == -1) return;
+    slot = (slot + 1) & mask;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ int64_t hash_find(const uint64_t* __restrict__ basis, const int32_t* __restrict__ table,
+                                             uint64_t mask, const uint64_t (&key)[W]) {
+  uint64_t slot = state_hash<W>(key) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    const int32_t idx = __ldg(table + slot);
+    if (idx < 0) return -1;
+    if (state_eq<W>(key, basis + (int64_t)idx * W)) return idx;
+    slot = (slot + 1) & mask;
+  }
+  return -1;
+}
+
 constexpr int kMfWarps = 8;      // warps (rows in flight) per block
 constexpr int kMfList = 256;     // (column, value) pairs buffered per warp
 
@@ -59,7 +101,8 @@ __global__ void hv_diag_kernel(int64_t n, const uint64_t* __restrict__ basis, in
 
 template <int W, typename T, bool CPLX, int L>
 __global__ void __launch_bounds__(32 * kMfWarps)
-    hv_matfree_kernel(int64_t n, const uint64_t* __restrict__ basis, int n_orb, const int32_t* __restrict__ bucket,
+    hv_matfree_kernel(int64_t n, const uint64_t* __restrict__ basis, const int32_t* __restrict__ table,
+                      uint64_t table_mask, int n_orb, const int32_t* __restrict__ bucket,
                       const uint64_t* __restrict__ ops, const double2* __restrict__ coeff, Restr restr,
                       const double* __restrict__ diag, double shift, const typename MfPack<T>::type* __restrict__ X,
                       typename MfPack<T>::type* __restrict__ Y) {
@@ -132,7 +175,7 @@ __global__ void __launch_bounds__(32 * kMfWarps)
             for (int w = 0; w < W; ++w) s[w] = s0[w];
             int parity = 0;
             if (apply_term<W>(s, __ldg(ops + t), parity) && restr_ok<W>(restr, s)) {
-              j = find_state<W>(basis, n, s);
+              j = table ? hash_find<W>(basis, table, table_mask, s) : find_state<W>(basis, n, s);
               if (j >= 0) {
                 const double2 c = coeff[t];
                 const double sg = (parity & 1) ? -1.0 : 1.0;
@@ -177,7 +220,8 @@ __global__ void __launch_bounds__(32 * kMfWarps)
 }
 
 template <int W, typename T, bool CPLX>
-int launch_matfree_l(int L, int64_t n, const uint64_t* basis, int n_orb, const int32_t* bucket, const uint64_t* ops,
+int launch_matfree_l(int L, int64_t n, const uint64_t* basis, const int32_t* table, uint64_t table_mask, int n_orb,
+                     const int32_t* bucket, const uint64_t* ops,
                      const double2* coeff, const Restr& r, const double* diag, double shift, const void* x, void* y,
                      cudaStream_t s) {
   using P = typename MfPack<T>::type;
@@ -188,7 +232,8 @@ int launch_matfree_l(int L, int64_t n, const uint64_t* basis, int n_orb, const i
   P* Y = reinterpret_cast<P*>(y);
 #define EDGPU_MF_CASE(LL)                                                                                  \
   case LL:                                                                                                 \
-    hv_matfree_kernel<W, T, CPLX, LL><<<(unsigned)blocks, 32 * kMfWarps, 0, s>>>(n, basis, n_orb, bucket, \
+    hv_matfree_kernel<W, T, CPLX, LL><<<(unsigned)blocks, 32 * kMfWarps, 0, s>>>(n, basis, table, table_mask, \
+                                                                                 n_orb, bucket,            \
                                                                                  ops, coeff, r, diag,      \
                                                                                  shift, X, Y);             \
     break;
@@ -208,11 +253,14 @@ int launch_matfree_l(int L, int64_t n, const uint64_t* basis, int n_orb, const i
 }
 
 template <typename T>
-int hv_matfree_impl(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
+int hv_matfree_impl(int n_words, const uint64_t* basis, int64_t n, const int32_t* table, int64_t table_size,
+                    int n_orb, const int32_t* bucket,
                     const edgpu_terms* terms, int complex_terms, const edgpu_restrictions* restr, const double* diag,
                     double shift, const void* x, void* y, int R, cudaStream_t s) {
   if (!basis || n < 1 || !bucket || !terms || !diag || !x || !y || R < 1) return EDGPU_ERR_ARG;
   if (n_orb < 1 || n_orb > 64 * n_words || n_words < 1 || n_words > EDGPU_MAX_WORDS) return EDGPU_ERR_ARG;
+  if (table && (table_size < 2 * n || (table_size & (table_size - 1)))) return EDGPU_ERR_ARG;
+  const uint64_t mask = table ? (uint64_t)table_size - 1 : 0;
   if (terms->n_terms > 0 && (!terms->ops || !terms->coeff)) return EDGPU_ERR_ARG;
   constexpr int RV = MfPack<T>::runs;
   if (R % RV) return EDGPU_ERR_ARG;
@@ -222,10 +270,10 @@ int hv_matfree_impl(int n_words, const uint64_t* basis, int64_t n, int n_orb, co
   const Restr r = make_restr(restr);
   const double2* coeff = reinterpret_cast<const double2*>(terms->coeff);
   EDGPU_DISPATCH_W(n_words, return complex_terms
-                                ? launch_matfree_l<W, T, true>(L, n, basis, n_orb, bucket, terms->ops, coeff, r, diag,
-                                                               shift, x, y, s)
-                                : launch_matfree_l<W, T, false>(L, n, basis, n_orb, bucket, terms->ops, coeff, r, diag,
-                                                                shift, x, y, s));
+                                ? launch_matfree_l<W, T, true>(L, n, basis, table, mask, n_orb, bucket, terms->ops,
+                                                               coeff, r, diag, shift, x, y, s)
+                                : launch_matfree_l<W, T, false>(L, n, basis, table, mask, n_orb, bucket, terms->ops,
+                                                                coeff, r, diag, shift, x, y, s));
   return EDGPU_ERR_ARG;
 }
 
@@ -247,18 +295,33 @@ extern "C" int edgpu_hv_diag(int n_words, const uint64_t* basis, int64_t n, cons
   return check_launch();
 }
 
-extern "C" int edgpu_hv_matfree(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
+extern "C" int edgpu_state_hash_build(int n_words, const uint64_t* basis, int64_t n, int32_t* table,
+                                      int64_t table_size, void* stream) {
+  if (!basis || !table || n < 1 || n >= (1ll << 31) || table_size < 2 * n || (table_size & (table_size - 1)))
+    return EDGPU_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(table, 0xFF, sizeof(int32_t) * (size_t)table_size, s) != cudaSuccess) return EDGPU_ERR_CUDA;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  EDGPU_DISPATCH_W(n_words, state_hash_insert_kernel<W><<<blocks, 256, 0, s>>>(basis, n, table,
+                                                                               (uint64_t)table_size - 1));
+  note_launch();
+  return check_launch();
+}
+
+extern "C" int edgpu_hv_matfree(int n_words, const uint64_t* basis, int64_t n, const int32_t* table,
+                                int64_t table_size, int n_orb, const int32_t* bucket,
                                 const edgpu_terms* offdiag_terms, int complex_terms,
                                 const edgpu_restrictions* restr, const double* diag, double shift, const double* x,
                                 double* y, int R, void* stream) {
-  return hv_matfree_impl<double>(n_words, basis, n, n_orb, bucket, offdiag_terms, complex_terms, restr, diag, shift,
-                                 x, y, R, (cudaStream_t)stream);
+  return hv_matfree_impl<double>(n_words, basis, n, table, table_size, n_orb, bucket, offdiag_terms, complex_terms,
+                                 restr, diag, shift, x, y, R, (cudaStream_t)stream);
 }
 
-extern "C" int edgpu_hv_matfree_c64(int n_words, const uint64_t* basis, int64_t n, int n_orb,
-                                    const int32_t* bucket, const edgpu_terms* offdiag_terms, int complex_terms,
+extern "C" int edgpu_hv_matfree_c64(int n_words, const uint64_t* basis, int64_t n, const int32_t* table,
+                                    int64_t table_size, int n_orb, const int32_t* bucket,
+                                    const edgpu_terms* offdiag_terms, int complex_terms,
                                     const edgpu_restrictions* restr, const double* diag, double shift,
                                     const float* x, float* y, int R, void* stream) {
-  return hv_matfree_impl<float>(n_words, basis, n, n_orb, bucket, offdiag_terms, complex_terms, restr, diag, shift,
-                                x, y, R, (cudaStream_t)stream);
+  return hv_matfree_impl<float>(n_words, basis, n, table, table_size, n_orb, bucket, offdiag_terms, complex_terms,
+                                restr, diag, shift, x, y, R, (cudaStream_t)stream);
 }

@@ -70,8 +70,19 @@ def hv_diag(eng, basis_sorted, mop):
     return d
 
 
-def hv_matfree_into(eng, basis_sorted, mop, restr, diag, x, y, shift=0.0):
-    """y = (H - shift I) x for x, y [n, R] complex (complex64 or complex128), matrix-free."""
+def state_hash(eng, basis_sorted):
+    """Hash table of the basis states (int32 slots, a power of two >= 2n) for matrix-free
+    lookups."""
+    n, w = basis_sorted.shape
+    size = 1 << max(4, int(2 * n - 1).bit_length())
+    table = torch.empty(size, dtype=torch.int32, device=eng.device)
+    L.check(eng.lib.edgpu_state_hash_build(w, _ptr(basis_sorted), n, _ptr(table), size, eng.stream), "state_hash")
+    return table
+
+
+def hv_matfree_into(eng, basis_sorted, mop, restr, diag, x, y, shift=0.0, table=None):
+    """y = (H - shift I) x for x, y [n, R] complex (complex64 or complex128), matrix-free;
+    ``table`` (from :func:`state_hash`) replaces the binary searches by hash lookups."""
     n, w = basis_sorted.shape
     R = x.shape[1]
     rp = C.byref(restr) if restr is not None else None
@@ -79,7 +90,8 @@ def hv_matfree_into(eng, basis_sorted, mop, restr, diag, x, y, shift=0.0):
         fn = eng.lib.edgpu_hv_matfree_c64
     else:
         fn = eng.lib.edgpu_hv_matfree
-    L.check(fn(w, _ptr(basis_sorted), n, mop.n_orb, _ptr(mop.bucket), C.byref(mop.off.terms),
+    tsize = 0 if table is None else int(table.numel())
+    L.check(fn(w, _ptr(basis_sorted), n, _ptr(table), tsize, mop.n_orb, _ptr(mop.bucket), C.byref(mop.off.terms),
                0 if mop.off.is_real else 1, rp, _ptr(diag), float(shift), _ptr(torch.view_as_real(x)),
                _ptr(torch.view_as_real(y)), R, eng.stream), "hv_matfree")
     return y
@@ -146,9 +158,10 @@ def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K
         if matfree:
             diag = hv_diag(eng, sector.basis, mop)
             shift = float(diag.mean().item())
+            table = state_hash(eng, sector.basis)
 
             def apply_h(x, y):
-                hv_matfree_into(eng, sector.basis, mop, restr, diag, x, y, shift)
+                hv_matfree_into(eng, sector.basis, mop, restr, diag, x, y, shift, table)
         else:
             csr.mixed()
             shift = csr.mixed_shift

@@ -369,12 +369,21 @@ void edgpu_set_reorth_fused(int enabled);
  */
 int edgpu_hv_diag(int n_words, const uint64_t* basis, int64_t n, const edgpu_terms* diag_terms, double* d,
                   void* stream);
-int edgpu_hv_matfree(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
-                     const edgpu_terms* offdiag_terms, int complex_terms, const edgpu_restrictions* restr,
-                     const double* diag, double shift, const double* x, double* y, int R, void* stream);
-int edgpu_hv_matfree_c64(int n_words, const uint64_t* basis, int64_t n, int n_orb, const int32_t* bucket,
-                         const edgpu_terms* offdiag_terms, int complex_terms, const edgpu_restrictions* restr,
-                         const double* diag, double shift, const float* x, float* y, int R, void* stream);
+/* Open-addressing hash of the basis states for the lookups of edgpu_hv_matfree: table
+ * (device int32, table_size a power of two >= 2 n) receives basis indices (-1 = empty);
+ * replaces upstream's basis_index dict (finite.py:1613-1693). */
+int edgpu_state_hash_build(int n_words, const uint64_t* basis, int64_t n, int32_t* table, int64_t table_size,
+                           void* stream);
+/* table: the hash of edgpu_state_hash_build (lookups by one or two probes), or NULL (binary
+ * search in the sorted basis). */
+int edgpu_hv_matfree(int n_words, const uint64_t* basis, int64_t n, const int32_t* table, int64_t table_size,
+                     int n_orb, const int32_t* bucket, const edgpu_terms* offdiag_terms, int complex_terms,
+                     const edgpu_restrictions* restr, const double* diag, double shift, const double* x, double* y,
+                     int R, void* stream);
+int edgpu_hv_matfree_c64(int n_words, const uint64_t* basis, int64_t n, const int32_t* table, int64_t table_size,
+                         int n_orb, const int32_t* bucket, const edgpu_terms* offdiag_terms, int complex_terms,
+                         const edgpu_restrictions* restr, const double* diag, double shift, const float* x, float* y,
+                         int R, void* stream);
 
 /*
  * Pieces of a batched Lanczos with full reorthogonalisation for large sectors (R runs; a

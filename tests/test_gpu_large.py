@@ -35,10 +35,11 @@ def small316(eng):
 
 
 def _check_hv(eng, basis, csr, mop, restr, widths):
-    from impuritymodel_gb300.large import hv_diag, hv_matfree_into
+    from impuritymodel_gb300.large import hv_diag, hv_matfree_into, state_hash
 
     n = basis.shape[0]
     d = hv_diag(eng, basis, mop)
+    table = state_hash(eng, basis)
     rng = np.random.default_rng(4)
     rows = torch.repeat_interleave(torch.arange(n, device=eng.device), csr.row_ptr[1:] - csr.row_ptr[:-1])
     vals = csr.val_r.abs() if csr.val_r is not None else torch.view_as_complex(csr.val_c).abs()
@@ -48,10 +49,10 @@ def _check_hv(eng, basis, csr, mop, restr, widths):
             ref = eng.spmv(csr, x)
             scale = float(torch.zeros(n, dtype=torch.float64, device=eng.device).index_add_(
                 0, rows, vals * x.abs().max()).max())
-            for shift in (0.0, 3.0):
+            for shift, tab in ((0.0, None), (3.0, None), (0.0, table)):
                 xt = x.to(torch.complex64) if precision else x
                 y = torch.empty_like(xt)
-                hv_matfree_into(eng, basis, mop, restr, d, xt, y, shift)
+                hv_matfree_into(eng, basis, mop, restr, d, xt, y, shift, tab)
                 err = float((y.to(torch.complex128) + shift * xt.to(torch.complex128) - ref).abs().max()) / scale
                 tol = 2e-6 if precision else 1e-13
                 assert err < tol, (precision, R, shift, err)
