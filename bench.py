@@ -594,8 +594,8 @@ def equal_error(pipe, forms, members=3, eps_list=PERTURB_EPS):
 
 def large_config(eng, K=150, n_states=1):
     """The 316-spin-orbital model (30 bath levels per 3d spin-orbital, seed 3, at most two
-    bath holes): ground state on its 47 895-state sector, then PS (10 photoemission operators)
-    and XAS (3 dipole polarisations) of the lowest eigenstate, each family one batched
+    bath holes): ground state on its 47 895-state sector, then PS (10 photoemission operators
+    on 3d), XPS (6 on 2p) and XAS (3 dipole polarisations) of the lowest eigenstate, each family one batched
     reorthogonalised Lanczos (K steps) on its sector: complex64 vectors, matrix-free H·v and
     FP64 reductions, against the complex128 recurrence on the FP64 CSR Hamiltonian; the
     per-spectrum relative L1 error is reported."""
@@ -620,6 +620,7 @@ def large_config(eng, K=150, n_states=1):
     out["gs"] = {"sector": len(basis), "s": round(time.perf_counter() - t0, 3), "e0": float(es[0])}
     w = np.linspace(-25.0, 25.0, 2000)
     fams = {"PS": ([DeviceOp(t, eng.device) for t in mod.ps_ops()], -w, -0.2),
+            "XPS": ([DeviceOp(t, eng.device) for t in mod.ps_ops(l=1)], -w, -0.2),
             "XAS": ([DeviceOp(t, eng.device) for t in mod.xas_ops()], w, 0.2)}
     for name, (tops, mesh, delta) in fams.items():
         torch.cuda.synchronize()
