@@ -112,6 +112,15 @@ SIGNATURES = {
     "edgpu_krylov_dot": (_I, [_I, _P, _I64, _I, _I64, _I, _P, _P, _P, _SZ, _P]),
     "edgpu_krylov_project": (_I, [_I, _P, _I64, _I, _I64, _I, _P, _P, _I, _P, _SZ, _P]),
     "edgpu_krylov_normalize": (_I, [_I, _I64, _I, _P, _P, _P, _P, _P, _SZ, _P]),
+    "edgpu_build_csr_workspace": (_SZ, [_I, _I64, _I64]),
+    "edgpu_build_csr": (_I, [_I, C.POINTER(Terms), C.POINTER(Restrictions), _D, _P, _I64, _I, _P, _P, _P, _I64,
+                             C.POINTER(_I64), _P, _P, _SZ, _P]),
+    "edgpu_expand_workspace": (_SZ, [_I, _I64, _I64]),
+    "edgpu_expand": (_I, [_I, C.POINTER(Terms), C.POINTER(Restrictions), _D, _P, _I64, _I64, _I64, _P, _P,
+                          C.POINTER(_I64), _P, _P, _SZ, _P]),
+    "edgpu_eig_lowest_workspace": (_SZ, [_I64, _I]),
+    "edgpu_eig_lowest": (_I, [C.POINTER(CSR), _I, _D, _I, C.c_uint64, C.POINTER(_D), _P, C.POINTER(_I), _P, _P,
+                              _SZ, _P]),
     "edgpu_lanczos_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_lanczos": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_lanczos_timed": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _P, _P, _P, _P, _SZ, _P, C.POINTER(_D)]),

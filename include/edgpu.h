@@ -520,6 +520,56 @@ int edgpu_density_matrix(int n_words, const uint64_t* states, const double* amps
                          const uint64_t* pair_ops, int P, double* out, void* stream);
 
 /*
+ * Single-call sector and ground-state construction, for hosts that drive the engine without
+ * the Python layer.  Each is synchronous on `stream` (sizes are read back between phases) and
+ * takes all scratch from the workspace of its *_workspace query.
+ *
+ * edgpu_build_csr: the sector Hamiltonian on a SORTED basis (n states), replacing upstream
+ * get_hamiltonian_matrix / get_hamiltonian_matrix_from_h_dict (finite.py:1514-1693): row j
+ * holds H|b_j> conjugated (= row j of the Hermitian H), outputs outside the basis or the
+ * restrictions dropped, duplicates summed in term order, |v|^2 < weight_min dropped.
+ * row_ptr[n + 1] is always written; *nnz_out receives the entry count, and when it exceeds
+ * nnz_cap (or col/val is NULL) the call returns EDGPU_ERR_OVERFLOW without writing entries:
+ * call again with nnz_cap >= *nnz_out.  real_values != 0: val is float64 [nnz] (the real
+ * parts); else complex128 [nnz][2].
+ */
+size_t edgpu_build_csr_workspace(int n_words, int64_t n, int64_t nnz_cap);
+int edgpu_build_csr(int n_words, const edgpu_terms* terms, const edgpu_restrictions* restr, double weight_min,
+                    const uint64_t* basis, int64_t n, int real_values, int64_t* row_ptr, int32_t* col, double* val,
+                    int64_t nnz_cap, int64_t* nnz_out, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                    void* stream);
+/*
+ * edgpu_expand: closure of basis0 (n0 states) under the restricted operator, replacing
+ * upstream expand_basis (finite.py:1696-1803): breadth-first layers, each layer the sorted
+ * new states.  out_sorted[capacity] receives the closure sorted (lexicographic word order =
+ * upstream bytes order); out_layered (optional, [capacity]) upstream's basis order (basis0
+ * as given, then each layer sorted); *n_out its size.  Candidates are generated at most
+ * emit_cap at a time (the frontier is split).  EDGPU_ERR_OVERFLOW with *n_out a lower bound
+ * when the closure exceeds capacity.
+ */
+size_t edgpu_expand_workspace(int n_words, int64_t capacity, int64_t emit_cap);
+int edgpu_expand(int n_words, const edgpu_terms* terms, const edgpu_restrictions* restr, double weight_min,
+                 const uint64_t* basis0, int64_t n0, int64_t capacity, int64_t emit_cap, uint64_t* out_sorted,
+                 uint64_t* out_layered, int64_t* n_out, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                 void* stream);
+/*
+ * edgpu_eig_lowest: the k lowest eigenpairs of a Hermitian CSR H by Lanczos with full
+ * reorthogonalisation from a seeded random start vector (edgpu_lanczos_reorth, chunks of 32
+ * steps), replacing upstream eigensystem's eigsh(k, which="SA") (finite.py:58-118).  Ritz
+ * values of the Krylov tridiagonal come from bisection on Sturm counts and its eigenvectors
+ * from inverse iteration; the run stops when every wanted residual beta |s_last| is below
+ * tol_rel * max(1, |theta|), when the Krylov space is exhausted, or at k_cap steps
+ * (EDGPU_ERR_NOCONV, best pairs still written).  evals (host, k) ascending, evecs (device,
+ * [k][n] complex128), *k_found the pairs written.  One Krylov space holds one vector of each
+ * eigenspace: the copies of an exactly degenerate eigenvalue beyond the first are found by
+ * further deflated runs, which the Python layer adds (finite.eig_lowest).
+ */
+size_t edgpu_eig_lowest_workspace(int64_t n, int k_cap);
+int edgpu_eig_lowest(const edgpu_csr* h, int k, double tol_rel, int k_cap, uint64_t seed, double* evals,
+                     double* evecs, int* k_found, int32_t* status_dev, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
+/*
  * Connected components of a sector's (symmetric) sparsity pattern: label[i] = smallest state
  * index of i's component, for n <= 65536 in one launch (one CTA iterating minimum-label
  * propagation with pointer jumping on chip until a round changes nothing; *rounds receives
