@@ -190,11 +190,13 @@ class Pipeline:
         return es, g_xas, g_rixs
 
     def e2e_step(self, precision=0):
-        """The same pipeline through the drop-in dict API (host inputs, host outputs)."""
+        """The same pipeline through the drop-in dict API (host inputs, host outputs).  Each
+        step starts a fresh session: no sector kept by an earlier step is reused."""
         from impuritymodel_gb300 import finite, spectra
 
         W = WORKLOAD
         m = self.mod
+        finite.clear_sector_cache()
         es, psis = finite.eigensystem(self.n, m.hOp, self.basis, W["n_psi"], precision=precision)
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psis = es[:ne], psis[:ne]

@@ -91,6 +91,12 @@ def make_restrictions(restrictions, n_spin_orbitals):
     return r
 
 
+def _restr_key(restr):
+    if restr is None:
+        return None
+    return tuple((int(restr.lo[k]), int(restr.hi[k]), tuple(int(x) for x in restr.mask[k])) for k in range(restr.n))
+
+
 class CsrMatrix:
     """CSR Hamiltonian on the device (row j holds <j|H|k> for the sector basis)."""
 
@@ -213,6 +219,24 @@ class Engine:
         # bytes moved across the host<->device boundary by the drop-in API (inputs/results)
         self.h2d_bytes = 0
         self.d2h_bytes = 0
+        # sectors built by the drop-in API calls of a session (see remember_sector)
+        self.sectors = []
+
+    # -- session sector cache (the role of upstream's h_dict memo across calls) ------------
+    def remember_sector(self, kind, dop, restr, item, keep=8):
+        """Keep a sector built by a drop-in call: ``kind`` "closure" (a Sector closed under the
+        restricted operator) or "basis" (an eigensystem basis with its Hamiltonian)."""
+        rkey = _restr_key(restr)
+        self.sectors = [e for e in self.sectors if e[3] is not item][-(keep - 1):] + [(kind, dop, rkey, item)]
+
+    def sectors_for(self, kind, dop, restr):
+        """Sectors of this kind kept for the same operator object and restrictions, newest
+        first."""
+        rkey = _restr_key(restr)
+        return [e[3] for e in reversed(self.sectors) if e[0] == kind and e[1] is dop and e[2] == rkey]
+
+    def clear_sectors(self):
+        self.sectors = []
 
     # -- plumbing -------------------------------------------------------------------------
     def _stream_handle(self):

@@ -54,6 +54,13 @@ def assert_hermitian(op):
     assert daggerOp(op) == op
 
 
+def clear_sector_cache():
+    """Forget the sectors that drop-in calls of this process kept for later calls (the
+    ground-state basis of ``eigensystem``, the closures built by ``getSpectra`` and
+    ``getRIXSmap``).  Call it when a new model starts or to time calls independently."""
+    get_engine().clear_sectors()
+
+
 def get_job_tasks(rank, ranks, tasks_tot):
     """Split task indices over ranks (upstream finite.py:27-55)."""
     n_tot = len(tasks_tot)
@@ -648,7 +655,11 @@ def eigensystem(n_spin_orbitals, hOp, basis, nPsiMax, groundDiagMode="Lanczos", 
     words_for(n)
     basis = list(basis)
     sb = _SortedBasis(eng, basis, n)
-    csr = _device_hamiltonian(eng, _device_op(hOp, eng), sb)
+    dop = _device_op(hOp, eng)
+    csr = _device_hamiltonian(eng, dop, sb)
+    # kept for the spectra calls of the same session: RIXS final states run on this sector
+    # when it is closed under the restricted H (spectra.getRIXSmap)
+    eng.remember_sector("basis", dop, None, (sb, csr))
     if groundDiagMode == "full":
         h = _csr_to_scipy_given_order(csr, sb.perm).toarray()
         es, vecs = np.linalg.eigh(h)

@@ -34,7 +34,7 @@ import torch
 
 from . import _lib as L
 from . import codec
-from .engine import get_engine, make_restrictions, words_for
+from .engine import _restr_key, get_engine, make_restrictions, words_for
 from .finite import _device_op
 from .models import (  # noqa: F401  (upstream names re-exported)
     K_B,
@@ -308,11 +308,14 @@ def green_batch(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, kry
 
 def _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, omega, delta, krylovSize=150, precision=0,
                        sector=None, return_coeffs=False, normalize=True, scales=None, timing=None, capture=None,
-                       perturb=None, stages=None, sector_hint=None):
-    """green_batch as a step generator: yields once, after the Lanczos launch."""
+                       perturb=None, stages=None, sector_hint=None, sector_out=None):
+    """green_batch as a step generator: yields once, after the Lanczos launch.  ``sector_out``
+    (a dict) receives the sector the runs used under "sector"."""
     omega = np.asarray(omega, dtype=np.float64)
     st = green_setup(eng, dop, restr, run_states, run_amps, krylovSize, precision, sector, normalize, scales,
                      perturb, stages, sector_hint)
+    if sector_out is not None and st is not None:
+        sector_out["sector"] = st.sector
     runs = len(run_states) if run_amps is not None else run_states[3]
     g = torch.zeros((runs, len(omega)), dtype=torch.complex128, device=eng.device)
     if st is None:
@@ -433,7 +436,7 @@ def spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150,
 
 
 def spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, slaterWeightMin=1e-7, precision=0,
-                  capture=None, perturb=None, batched=True, t_outs=None, sector_hint=None):
+                  capture=None, perturb=None, batched=True, t_outs=None, sector_hint=None, sector_out=None):
     """spectra_device as a step generator for :func:`run_concurrently`.  ``t_outs``: the
     result of ``eng.apply_vectors_multi`` for these operators and states when the caller
     has it already; ``sector_hint``: a sector closed under the restricted H that may hold
@@ -451,7 +454,8 @@ def spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize=150, 
             e_runs.append(es[i])
     if batched:
         g = yield from _green_batch_steps(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize,
-                                          precision, capture=capture, perturb=perturb, sector_hint=sector_hint)
+                                          precision, capture=capture, perturb=perturb, sector_hint=sector_hint,
+                                          sector_out=sector_out)
     else:
         g = green_runs_one_by_one(eng, dop, restr, run_states, run_amps, e_runs, w, delta, krylovSize, precision)
     return g.view(len(t_dops), ne, len(w)).permute(1, 0, 2)
@@ -473,7 +477,14 @@ def getSpectra(n_spin_orbitals, hOp, tOps, psis, es, w, delta, restrictions=None
     restr = make_restrictions(restrictions, n)
     psi_t = [_psi_tensors(eng, psis[i], n) for i in range(len(es))]
     t_dops = [_device_op(top, eng) for top in tOps]
-    g = spectra_device(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision)
+    # a closure kept from an earlier call of this session serves as the sector when it holds
+    # every start state (the role of upstream's h_dict memo); the sector used is kept
+    hints = eng.sectors_for("closure", dop, restr)
+    used = {}
+    g = _drive(spectra_steps(eng, dop, restr, t_dops, psi_t, es, w, delta, krylovSize, slaterWeightMin, precision,
+                             sector_hint=hints[0] if hints else None, sector_out=used))
+    if "sector" in used:
+        eng.remember_sector("closure", dop, restr, used["sector"])
     return eng.to_host(g.contiguous())
 
 
@@ -534,9 +545,26 @@ def getRIXSmap(n_spin_orbitals, hOp, tOpsIn, tOpsOut, psis, es, wIns, wLoss, del
     dop = _device_op(hOp, eng)
     restr = make_restrictions(restrictions, n)
     psi_t = [_psi_tensors(eng, psis[i], n) for i in range(len(es))]
-    g = rixs_device(eng, dop, restr, [_device_op(t, eng) for t in tOpsIn], [_device_op(t, eng) for t in tOpsOut],
-                    psi_t, es, wIns, wLoss, delta1, delta2, krylovSize, slaterWeightMin, precision, solve_tol,
-                    share_out_memo, max_krylov)
+    # sectors kept from earlier calls of this session: a closure that holds T_in psi serves as
+    # the core-hole sector, and an eigensystem basis closed under the restricted H as the
+    # final-state sector (the roles of upstream's h_dict memos across calls)
+    hints = eng.sectors_for("closure", dop, restr)
+    final = None
+    for sb, csr in eng.sectors_for("basis", dop, None):
+        cache = sb.__dict__.setdefault("_closed", {})
+        rkey = _restr_key(restr)
+        if rkey not in cache:
+            cache[rkey] = closed_sector(eng, dop, restr, sb.sorted, csr, sb.words)
+        if cache[rkey] is not None:
+            final = cache[rkey]
+            break
+    share = {}
+    g = _drive(rixs_steps(eng, dop, restr, [_device_op(t, eng) for t in tOpsIn], [_device_op(t, eng) for t in tOpsOut],
+                          psi_t, es, wIns, wLoss, delta1, delta2, krylovSize, slaterWeightMin, precision, solve_tol,
+                          share_out_memo, max_krylov, final_sector=final, share=share,
+                          core_hint=hints[0] if hints else None))
+    if "sector" in share:
+        eng.remember_sector("closure", dop, restr, share["sector"])
     return eng.to_host(g)
 
 
@@ -554,10 +582,13 @@ def rixs_device(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, de
 
 def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, delta1, delta2, krylovSize=150,
                slaterWeightMin=1e-7, precision=0, solve_tol=1e-10, share_out_memo=True, max_krylov=2000,
-               timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None, share=None):
+               timing=None, capture=None, perturb=None, stages=None, batched=True, final_sector=None, share=None,
+               core_hint=None):
     """rixs_device as a step generator for :func:`run_concurrently` (yields after the launch
     of the shifted solves and after the launch of the final-state Lanczos).  ``final_sector``:
     a sector from :func:`closed_sector` (the ground-state sector) used for the final states
+    (``core_hint``: a closure under the restricted H used as the core-hole sector when it holds
+    every T_in psi state)
     when it holds them all, instead of expanding their closure.  ``share``: a dict that
     receives ``t_outs`` (T_in applied to the eigenstates, as ``eng.apply_vectors_multi``
     returns it), ``sector`` (the core-hole sector, the closure of those states) and
@@ -580,7 +611,14 @@ def rixs_steps(eng, dop, restr, tin_dops, tout_dops, psi_t, es, wIns, wLoss, del
         return gs
     _mark(stages, "rixs:psi1")
     # 2. core-hole sector
-    core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
+    core = None
+    if core_hint is not None:
+        # a closure under the restricted H that holds every T_in psi state holds their closure
+        rows = eng.lookup(core_hint.basis, torch.cat(nonempty, 0))
+        if bool((rows >= 0).all().item()):
+            core = core_hint
+    if core is None:
+        core = Sector(eng, dop, restr, torch.cat(nonempty, 0))
     if share is not None:
         share.update(t_outs=t_outs, sector=core, ready=torch.cuda.current_stream(eng.device).record_event())
     _mark(stages, "rixs:core_sector")

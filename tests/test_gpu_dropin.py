@@ -88,3 +88,29 @@ def test_eigensystem_returns_every_copy_of_degenerate_levels(eng, precision):
     Xh = X.cpu().numpy()
     g2 = Xh.conj() @ Xh.T
     assert np.abs(g2 - np.eye(k)).max() < 1e-8
+
+
+def test_session_sectors_give_the_same_spectra(eng):
+    """eigensystem -> getSpectra -> getRIXSmap through the dict API with the sectors kept by
+    the session (XAS closure reused as the RIXS core-hole sector, the ground-state basis as the
+    final-state sector) equals the same calls with the cache cleared before each."""
+    mod = M.make_model("config1")
+    n = mod.n_spin_orbitals
+    basis = finite.get_basis(*mod.basis_args())
+    w = np.linspace(-10, 20, 200)
+    wl = np.linspace(-2, 12, 150)
+    finite.clear_sector_cache()
+    es, psis = finite.eigensystem(n, mod.hOp, basis, 3)
+    g1 = spectra.getSpectra(n, mod.hOp, mod.xas_ops(), psis, es, w, 0.2, mod.restrictions)
+    r1 = spectra.getRIXSmap(n, mod.hOp, mod.xas_ops(), mod.rixs_out_ops(), psis, es, w[::40], wl, 0.2, 0.05,
+                            mod.restrictions)
+    assert len(eng.sectors) >= 2
+    finite.clear_sector_cache()
+    g2 = spectra.getSpectra(n, mod.hOp, mod.xas_ops(), psis, es, w, 0.2, mod.restrictions)
+    finite.clear_sector_cache()
+    r2 = spectra.getRIXSmap(n, mod.hOp, mod.xas_ops(), mod.rixs_out_ops(), psis, es, w[::40], wl, 0.2, 0.05,
+                            mod.restrictions)
+    assert np.abs(g1 - g2).max() <= 1e-10 * np.abs(g2).max()
+    # the final states run on the ground-state sector or on their own closure: the same
+    # Krylov spaces (closures are unions of components)
+    assert np.abs(r1 - r2).max() <= 1e-6 * np.abs(r2).max()
