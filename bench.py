@@ -386,12 +386,16 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     }
 
 
-def get_tuner_report(kind, key):
+def get_tuner_report(kind, key, top=6):
+    """The autotuner's measurements for this bucket: the fastest ``top`` mappings and the
+    number of mappings timed."""
     from impuritymodel_gb300.tuner import get_tuner
 
     rep = get_tuner().report(kind)
     name = "%s|%s" % (kind, ",".join(str(k) for k in key))
-    return rep.get(name, {}).get("times_us")
+    times = rep.get(name, {}).get("times_us") or {}
+    best = sorted(times.items(), key=lambda t: t[1])[:top]
+    return {"timed": len(times), "fastest_us": dict(best)}
 
 
 def pruning_setup(eng, n_train=1000, n_held=200, keeps=(0.5, 0.75), epochs=10):

@@ -485,7 +485,8 @@ def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=Non
     ``r_i <= tol_rel * max(1, |theta_i|)``.  Without ``thr`` the lowest ``k`` pairs are
     wanted.  With ``thr`` (a deflated run) the pairs below ``thr`` are wanted, at most
     ``k``: the run stops once every Ritz pair up to the first one that lies above ``thr``
-    by more than its residual (and beyond the tolerance) has converged.  The Krylov space
+    has converged; a pair lies above when its Ritz value minus min(residual, residual^2 /
+    gap to the next Ritz value) exceeds ``thr`` plus the tolerance.  The Krylov space
     grows (its cap doubling) until then or until it spans the sector (or, with ``locked``
     vectors, their orthogonal complement).  Returns (theta [q] ascending, Ritz vectors
     [q, N] complex128 device tensor) of the q wanted pairs."""
@@ -519,7 +520,12 @@ def _ritz_run(eng, csr, v0, k, k_cap, tol_rel, precision=0, locked=None, thr=Non
             return bool(np.all(ratio <= 1.0)), float(ratio.max())
         worst = 0.0
         for i in range(len(th)):
-            if th[i] - res[i] > thr + tol_thr:
+            # lower estimate of the eigenvalue this Ritz value approaches: the residual bound,
+            # sharpened to res^2 / gap (Kato-Temple) with the gap to the next Ritz value
+            drop = res[i]
+            if i + 1 < len(th) and th[i + 1] > th[i]:
+                drop = min(drop, res[i] * res[i] / (th[i + 1] - th[i]))
+            if th[i] - drop > thr + tol_thr:
                 return True, worst  # this pair and the ones above it lie above the threshold
             if i >= k:
                 return True, worst
