@@ -133,6 +133,7 @@ SIGNATURES = {
     "edgpu_lanczos_reorth_df": (_I, [C.POINTER(CSR), _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_set_reorth_fused": (None, [_I]),
     "edgpu_set_small_reserve": (None, [_I]),
+    "edgpu_set_lanczos_cta": (None, [_I]),
     "edgpu_shifted_solve_workspace": (_SZ, [_I64, _I, _I, _I]),
     "edgpu_shifted_solve": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),
     "edgpu_shifted_solve_df": (_I, [C.POINTER(CSR), _P, _I, _P, _I, _I, _D, _P, _P, _P, _P, _SZ, _P]),

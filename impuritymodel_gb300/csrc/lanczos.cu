@@ -1453,8 +1453,24 @@ using SlicedDfKern = void (*)(int64_t, const int32_t*, const int32_t*, const int
                               const double2*, const int32_t*, int, double*, double*, int32_t*, float4*);
 static const int kDfThreads[5] = {512, 256, 192, 160, 128};
 
+// Process-wide CTA-size choice for the double-float one-CTA-per-run Lanczos (index into
+// kDfThreads, or -1 for the rule below); set by the engine's autotuner around a call.
+static std::atomic<int> g_df_cta{-1};
+extern "C" void edgpu_set_lanczos_cta(int index) { g_df_cta.store(index >= 0 && index < 5 ? index : -1); }
+
 static int pick_df_config(const void* const* kerns, size_t smem, int R, int* per_sm_out) {
   const int nsm = grid_cap();
+  const int forced = g_df_cta.load();
+  if (forced >= 0) {
+    cudaFuncSetAttribute(kerns[forced], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[forced], kDfThreads[forced], smem);
+    if (per_sm >= 1) {
+      *per_sm_out = per_sm;
+      return forced;
+    }
+    cudaGetLastError();
+  }
   int best = -1, best_waves = 0;
   for (int c = 0; c < 5; ++c) {
     cudaFuncSetAttribute(kerns[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -216,6 +216,8 @@ class Engine:
         self._lanes = {}
         self._side = []
         self.scratch_entries = 256
+        # time the CTA sizes of the batched double-float Lanczos once per problem bucket
+        self.tune_lanczos = True
         # bytes moved across the host<->device boundary by the drop-in API (inputs/results)
         self.h2d_bytes = 0
         self.d2h_bytes = 0
@@ -641,11 +643,16 @@ class Engine:
             raise ValueError("lanczos: precision must be 0, 1 or 3")
         v0r = torch.view_as_real(v0.contiguous()) if v0.is_complex() else v0
         ws, wsn = self.workspace(self.lib.edgpu_lanczos_workspace(n, r, K, precision))
+        cta = self._lanczos_cta(csr, v0r, r, kmax, K, precision, ws, wsn) if self.tune_lanczos else -1
         self.reset_status()
         if timing is None:
-            L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
-                                           _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
-                    "lanczos")
+            self.lib.edgpu_set_lanczos_cta(cta)
+            try:
+                L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
+                                               _ptr(alpha), _ptr(beta), _ptr(self.status), ws, wsn, self.stream),
+                        "lanczos")
+            finally:
+                self.lib.edgpu_set_lanczos_cta(-1)
         else:
             ms = (C.c_double * 3)()
             L.check(self.lib.edgpu_lanczos_timed(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
@@ -660,6 +667,35 @@ class Engine:
         if precision == 1 and csr.mixed_shift:
             alpha += csr.mixed_shift  # Lanczos ran on H - shift*I
         return alpha, beta
+
+    # CTA sizes of the double-float one-CTA-per-run Lanczos (index into the library's list)
+    LANCZOS_CTAS = (-1, 0, 1, 2, 3, 4)
+    LANCZOS_SMALL_ROWS = 32767  # sectors served by that kernel
+
+    def _lanczos_cta(self, csr, v0r, r, kmax, K, precision, ws, wsn):
+        """The CTA size the autotuner picked for the double-float one-CTA-per-run Lanczos in
+        this (n, R, K) bucket, timed on this call's own inputs on first use; -1 (the built-in
+        rule) for every other form."""
+        if precision != 3 or csr.val_df is None or csr.n > self.LANCZOS_SMALL_ROWS or r < 64:
+            return -1
+        key = (bucket(csr.n), bucket(r), bucket(K))
+        tuner = get_tuner()
+        hit = tuner.lookup("lanczos_cta", key)
+        if hit is not None:
+            return int(hit[0])
+        a_s = torch.empty((r, K), dtype=torch.float64, device=self.device)
+        b_s = torch.empty_like(a_s)
+        st = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+        def run(c):
+            self.lib.edgpu_set_lanczos_cta(c[0])
+            try:
+                L.check(self.lib.edgpu_lanczos(C.byref(csr.struct()), _ptr(v0r), r, _ptr(kmax), K, precision,
+                                               _ptr(a_s), _ptr(b_s), _ptr(st), ws, wsn, self.stream), "lanczos")
+            finally:
+                self.lib.edgpu_set_lanczos_cta(-1)
+
+        return int(tuner.pick("lanczos_cta", key, [(c,) for c in self.LANCZOS_CTAS], run, reps=2, warmup=1)[0])
 
     def spmv(self, csr, x, precision=0, mapping=None):
         """y [csr.n, R] = csr @ x for x [csr.ncols, R].

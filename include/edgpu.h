@@ -346,6 +346,13 @@ int edgpu_lanczos_reorth_df(const edgpu_csr* h, const double* v0, int j0, int j1
  * one-CTA-per-run Lanczos of edgpu_lanczos (precision 3, small sectors) leaves free, so that
  * work on another stream can run beside it.  No counterpart in upstream impurityModel. */
 void edgpu_set_small_reserve(int slots);
+/* Process-wide launch choice (default -1): the CTA size of the double-float one-CTA-per-run
+ * Lanczos of edgpu_lanczos (precision 3, small sectors) as an index into {512, 256, 192, 160,
+ * 128} threads, or -1 for the built-in rule (fewest waves with a slot per SM kept back).  The
+ * engine's autotuner times the choices per problem bucket and sets the fastest around each
+ * call; the size changes the order of the block reductions, not the recurrence.  No
+ * counterpart in upstream impurityModel. */
+void edgpu_set_lanczos_cta(int index);
 /* Process-wide switch (default 1): 0 sends every edgpu_lanczos_reorth call to the
  * per-step kernels (both paths compute the same recurrence; used to test one against the
  * other).  No counterpart in upstream impurityModel. */
