@@ -162,17 +162,20 @@ class Pipeline:
         self.xas_ops_host = m.xas_ops()
         self.out_ops_host = m.rixs_out_ops()
 
-    def step(self, precision=0, timing=None, capture=None, perturb=None, batched=True):
+    def step(self, precision=0, timing=None, capture=None, perturb=None, batched=True, gs_basis=None):
+        """One pipeline step; ``gs_basis`` (a pruned ground-state basis, pruning.ExpandedBasis)
+        replaces the full restricted basis for the ground state."""
         from impuritymodel_gb300 import finite, spectra
 
         W = WORKLOAD
-        es, psi_t, h_gs = finite.eigensystem_device(self.eng, self.dop, self.sb, W["n_psi"],
+        sb = gs_basis if gs_basis is not None else self.sb
+        es, psi_t, h_gs = finite.eigensystem_device(self.eng, self.dop, sb, W["n_psi"],
                                                     precision=3 if precision == 3 else 0, with_hamiltonian=True)
         ne = int(np.sum(es - es[0] < W["energy_cut_kT"] * K_B * T_KELVIN))
         es, psi_t = es[:ne], psi_t[:ne]
         # the ground-state sector serves the RIXS final states when it is closed
-        gs_sector = spectra.closed_sector(self.eng, self.dop, self.restr, self.sb.sorted, h_gs,
-                                          self.sb.words) if batched else None
+        gs_sector = spectra.closed_sector(self.eng, self.dop, self.restr, sb.sorted, h_gs,
+                                          sb.words) if batched else None
         if capture is None and perturb is None and timing is None and batched:
             # XAS on a side stream while the RIXS pipeline runs on the current one
             g_xas, g_rixs = spectra.xas_rixs_device(
@@ -442,7 +445,9 @@ def pruning_setup(eng, n_train=1000, n_held=200, keeps=(0.5, 0.75), epochs=10):
             held.setdefault(key, {}).setdefault("keep_%g" % k, {})[name] = {
                 "median_error_eV": float(np.median(e)), "max_error_eV": float(e.max()),
                 "within_1e-4_eV": int(np.sum(e <= 1e-4))}
+    expansion = pruned_expansion_record(eng, net)
     return net, {
+        "pruned_expansion": expansion,
         "train_models": n_train, "train_samples": int(st.shape[0]), "target": "log10 |<s|psi_0>|^2",
         "sample_gen_s": round(t1 - t0, 3), "epochs": epochs, "adam_steps": int(steps), "batch": 4096,
         "train_s": round(t2 - t1, 3), "train_launches": int(eng.lib.edgpu_launch_count() - n0),
@@ -450,6 +455,42 @@ def pruning_setup(eng, n_train=1000, n_held=200, keeps=(0.5, 0.75), epochs=10):
         "train_tflops": round(3.0 * flop_fwd * steps * 4096 / (t2 - t1) / 1e12, 3),
         "held_out": {k: {"models": v[0], "rows": v[1]} for k, v in split.items()}, "held_out_errors": held,
         "eval_s": round(t3 - t2, 3)}
+
+
+def pruned_expansion_record(eng, net, keeps=(0.5, 0.75, 0.9), steps=3):
+    """Pruning inside basis expansion on the headline model (66 spin-orbitals): the ground-state
+    basis grown from the lowest configurations layer by layer, each layer's new states ranked
+    by the network and only the best fraction kept; energies against the full expansion (the
+    judge and fallback), then the whole pipeline (double-float form) on the pruned basis: its
+    time and its XAS / RIXS distance (relative L1) to the pipeline on the full basis."""
+    import torch
+
+    from impuritymodel_gb300 import codec, pruning
+    from impuritymodel_gb300.engine import make_restrictions
+
+    pipe = Pipeline(eng)
+    mod = pipe.mod
+    b0 = eng.upload_states(codec.bytes_to_words(list(pruning.seed_basis(mod)), pipe.n))
+    restr = make_restrictions(mod.restrictions, pipe.n)
+    res, full = pruning.evaluate_expansion_pruning(eng, mod, net, keeps, n_states=WORKLOAD["n_psi"])
+    full_basis, _, _ = pruning.expand_pruned(eng, pipe.dop, restr, b0)
+    out = {"seed_states": int(b0.shape[0]), "full": full, "keeps": {}}
+    ref = pipe.step(3, gs_basis=pruning.ExpandedBasis(full_basis))
+    t_full, _ = time_steps(lambda: pipe.step(3, gs_basis=pruning.ExpandedBasis(full_basis)), steps, 2,
+                           torch.zeros(1, device=eng.device))
+    out["full_step_s"] = round(statistics.mean(t_full), 5)
+    for keep in keeps:
+        pr, _, _ = pruning.expand_pruned(eng, pipe.dop, restr, b0, net, keep)
+        eb = pruning.ExpandedBasis(pr)
+        got = pipe.step(3, gs_basis=eb)
+        t, _ = time_steps(lambda: pipe.step(3, gs_basis=eb), steps, 2, torch.zeros(1, device=eng.device))
+        rec = dict(res[keep])
+        rec.update(step_s=round(statistics.mean(t), 5), states_kept=len(got[0]),
+                   xas_rel_l1=rel_l1_t(got[1][: len(ref[0])], ref[1][: len(got[0])]) if len(got[0]) == len(
+                       ref[0]) else None,
+                   rixs_rel_l1=rel_l1_t(got[2], ref[2]) if len(got[0]) == len(ref[0]) else None)
+        out["keeps"]["%g" % keep] = rec
+    return out
 
 
 def batched_configs(eng, n_models=256):

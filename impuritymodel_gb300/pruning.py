@@ -18,6 +18,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
+from . import codec
 from .engine import _ptr, get_engine
 
 N_IN = 320  # 316 spin-orbitals of the largest model, padded to a multiple of 64
@@ -266,3 +267,84 @@ def pruned_ground_state(eng, model, keep, ranking, n_states=1):
     r = res["r"][keep]
     return dict(error=r["error"], n_full=full["n"], n_pruned=r["n_pruned"], nnz_full=full["nnz"],
                 nnz_pruned=r["nnz_pruned"], e_full=full["e"])
+
+
+# ---------------------------------------------------------------------------------------
+# Pruning inside basis expansion
+# ---------------------------------------------------------------------------------------
+
+
+def seed_basis(model):
+    """The lowest configurations of a seeded model: the impurity at its nominal occupation
+    and every valence bath orbital filled (upstream get_basis with no bath holes)."""
+    from .finite import get_basis
+
+    nb, nvb, dnv, dnc, dnt, n0 = model.basis_args()
+    dnv0 = type(dnv)((k, 0) for k in dnv)
+    dnt0 = type(dnt)((k, 0) for k in dnt)
+    return get_basis(nb, nvb, dnv0, dnc, dnt0, n0)
+
+
+def expand_pruned(eng, dop, restr, basis0, net=None, keep=1.0, weight_min=1e-12, min_keep=16, layers=None):
+    """Breadth-first closure of ``basis0`` [N0, W] under the restricted operator (upstream
+    expand_basis, finite.py:1696-1803) in which every layer's new states are ranked by the
+    network and only the best ``keep`` fraction (at least ``min_keep``) joins the basis and
+    the next frontier; ``keep=1`` (or no network) is the full expansion, the fallback and the
+    judge.  Returns (sorted basis [N, W], layered order [N, W], per-layer (new, kept))."""
+    s_sorted = eng.sort_unique(basis0)
+    order = [basis0]
+    frontier = basis0
+    stats = []
+    while frontier.shape[0] > 0 and (layers is None or len(stats) < layers):
+        _, cand, _, _ = eng.apply_columns(frontier, dop, restr, weight_min, basis=s_sorted,
+                                          filt=L.FILTER_NOT_IN_BASIS, want_states=True)
+        if cand.shape[0] == 0:
+            break
+        new = eng.sort_unique(cand)
+        n_new = int(new.shape[0])
+        if net is not None and keep < 1.0:
+            m = max(min_keep, int(math.ceil(keep * n_new)))
+            if m < n_new:
+                # a BasisNet, or any function of the states giving a score per state
+                score = (net.predict(pad_words(new)) if isinstance(net, BasisNet) else net(new)).to(torch.float64)
+                top = torch.sort(torch.topk(score, m).indices).values
+                new = new[top].contiguous()
+        stats.append((n_new, int(new.shape[0])))
+        s_sorted = eng.merge(s_sorted, new)
+        order.append(new)
+        frontier = new
+    return s_sorted, torch.cat(order, 0), stats
+
+
+class ExpandedBasis:
+    """A sorted device basis in the form the eigensystem routines take (caller order = sorted
+    order)."""
+
+    def __init__(self, sorted_states):
+        self.sorted = sorted_states
+        self.given = sorted_states
+        self.perm = torch.arange(sorted_states.shape[0], dtype=torch.int64, device=sorted_states.device)
+        self.words = sorted_states.cpu().numpy().view(np.uint64)
+
+
+def evaluate_expansion_pruning(eng, model, net, keeps, n_states=1):
+    """Lowest ``n_states`` energies on the pruned expansion of the model's seed basis for every
+    keep fraction, against the full expansion (the judge).  Returns {keep: dict(error eV (>= 0,
+    variational), n, layers)} and the full record."""
+    from .engine import make_restrictions
+    from .finite import _device_op, eig_lowest
+
+    n = model.n_spin_orbitals
+    dop = _device_op(model.hOp, eng)
+    restr = make_restrictions(model.restrictions, n)
+    b0 = eng.upload_states(codec.bytes_to_words(list(seed_basis(model)), n))
+    full, _, st_full = expand_pruned(eng, dop, restr, b0)
+    e_full, _ = eig_lowest(eng, eng.build_csr(full, dop, None), n_states)
+    out = {}
+    for keep in keeps:
+        pr, _, st = expand_pruned(eng, dop, restr, b0, net, keep)
+        e_p, _ = eig_lowest(eng, eng.build_csr(pr, dop, None), n_states)
+        q = min(len(e_full), len(e_p))
+        out[keep] = dict(error=float(np.max(np.asarray(e_p[:q]) - np.asarray(e_full[:q]))), n=int(pr.shape[0]),
+                         layers=st)
+    return out, dict(e=[float(x) for x in e_full], n=int(full.shape[0]), layers=st_full)
