@@ -289,14 +289,15 @@ def expand_pruned(eng, dop, restr, basis0, net=None, keep=1.0, weight_min=1e-12,
     """Breadth-first closure of ``basis0`` [N0, W] under the restricted operator (upstream
     expand_basis, finite.py:1696-1803) in which every layer's new states are ranked by the
     network and only the best ``keep`` fraction (at least ``min_keep``) joins the basis and
-    the next frontier; ``keep=1`` (or no network) is the full expansion, the fallback and the
-    judge.  Returns (sorted basis [N, W], layered order [N, W], per-layer (new, kept))."""
+    the next frontier; the states it drops are remembered and not offered again by later
+    layers.  ``keep=1`` (or no network) is the full expansion, the fallback and the judge.  Returns (sorted basis [N, W], layered order [N, W], per-layer (new, kept))."""
     s_sorted = eng.sort_unique(basis0)
+    seen = s_sorted  # basis states and the states pruned so far (never offered again)
     order = [basis0]
     frontier = basis0
     stats = []
     while frontier.shape[0] > 0 and (layers is None or len(stats) < layers):
-        _, cand, _, _ = eng.apply_columns(frontier, dop, restr, weight_min, basis=s_sorted,
+        _, cand, _, _ = eng.apply_columns(frontier, dop, restr, weight_min, basis=seen,
                                           filt=L.FILTER_NOT_IN_BASIS, want_states=True)
         if cand.shape[0] == 0:
             break
@@ -307,10 +308,13 @@ def expand_pruned(eng, dop, restr, basis0, net=None, keep=1.0, weight_min=1e-12,
             if m < n_new:
                 # a BasisNet, or any function of the states giving a score per state
                 score = (net.predict(pad_words(new)) if isinstance(net, BasisNet) else net(new)).to(torch.float64)
-                top = torch.sort(torch.topk(score, m).indices).values
-                new = new[top].contiguous()
+                mask = torch.zeros(n_new, dtype=torch.bool, device=new.device)
+                mask[torch.topk(score, m).indices] = True
+                seen = eng.merge(seen, new[~mask].contiguous())
+                new = new[mask].contiguous()
         stats.append((n_new, int(new.shape[0])))
         s_sorted = eng.merge(s_sorted, new)
+        seen = eng.merge(seen, new)
         order.append(new)
         frontier = new
     return s_sorted, torch.cat(order, 0), stats
