@@ -275,8 +275,9 @@ def time_steps(fn, steps, warmup, flush_buf):
     return times, out
 
 
-def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
-    """H·v on the 316-orbital model's photoemission sector (complex64, R vectors)."""
+def hv_roofline(eng, peaks, R=16, launches=30, warmup=3, orders=("sorted", "locality")):
+    """H·v on the 316-orbital model's photoemission sector (complex64, R vectors), in the
+    sorted row order and in the locality order; the faster one is the roofline's launch."""
     import torch
 
     from impuritymodel_gb300 import finite, models
@@ -298,32 +299,29 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     sec = Sector(eng, dop, restr, st, precision=1)
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
-    csr = sec.csr
+    from impuritymodel_gb300.large import locality_order
+
+    # the sector in its sorted order and in the locality order (bath configuration major,
+    # impurity orbitals minor): the same operator with its rows and columns relabelled
+    t0 = time.perf_counter()
+    perm = locality_order(sec.basis, dop)
+    mats = {}
+    if "sorted" in orders:
+        mats["sorted"] = sec.csr
+    if perm is not None and "locality" in orders:
+        mats["locality"] = sec.csr.permuted(perm, "locality").mixed()
+    torch.cuda.synchronize()
+    order_s = time.perf_counter() - t0
     g = torch.Generator(device=eng.device)
     g.manual_seed(0)
-    x = torch.randn((csr.n, R), dtype=torch.complex64, device=eng.device, generator=g)
+    x_sorted = torch.randn((sec.csr.n, R), dtype=torch.complex64, device=eng.device, generator=g)
     import ctypes
 
     from impuritymodel_gb300 import _lib
 
     lib = _lib.load()
     stream = torch.cuda.current_stream()
-    y = torch.empty_like(x)
-    xr, yr = torch.view_as_real(x), torch.view_as_real(y)
     st = ctypes.c_void_p(stream.cuda_stream)
-    # the autotuner measures every launch mapping of the row-scheduled kernel on this matrix
-    # once (first call), then the chosen one is timed
-    t0 = time.perf_counter()
-    mapping = eng.spmv_into(csr, xr, yr, R, precision=1)
-    torch.cuda.synchronize()
-    tune_s = time.perf_counter() - t0
-
-    def launch():
-        eng.spmv_into(csr, xr, yr, R, precision=1, mapping=mapping)
-
-    def launch_rows():
-        _lib.check(lib.edgpu_spmv_c64(ctypes.byref(csr.struct()), ctypes.c_void_p(xr.data_ptr()),
-                                      ctypes.c_void_p(yr.data_ptr()), R, st), "spmv_c64")
 
     def timed(fn, count):
         """Mean device time per launch: the launches are queued back to back between one
@@ -338,13 +336,38 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / 1e3 / count
 
-    avg_s = timed(launch, launches)
+    runs = {}
+    for name, c in mats.items():
+        x = x_sorted if name == "sorted" else x_sorted[perm].contiguous()
+        y = torch.empty_like(x)
+        xr, yr = torch.view_as_real(x), torch.view_as_real(y)
+        # the autotuner measures every launch mapping on this matrix once (first call), then
+        # the chosen one is timed
+        t0 = time.perf_counter()
+        mp = eng.spmv_into(c, xr, yr, R, precision=1)
+        torch.cuda.synchronize()
+        tune_s = time.perf_counter() - t0
+        avg = timed(lambda: eng.spmv_into(c, xr, yr, R, precision=1, mapping=mp), launches)
+        runs[name] = dict(csr=c, x=x, y=y, mapping=mp, avg=avg, tune_s=tune_s)
+    best = min(runs, key=lambda k: runs[k]["avg"])
+    csr, x, y, mapping, avg_s, tune_s = (runs[best][k] for k in ("csr", "x", "y", "mapping", "avg", "tune_s"))
+    # both orders compute the same product (rows relabelled, each row's terms in one order)
+    order_agree = None
+    if "locality" in runs and "sorted" in runs:
+        ys, yl = runs["sorted"]["y"], runs["locality"]["y"]
+        order_agree = float((yl - ys[perm]).abs().max() / ys.abs().max().clamp_min(1e-30))
+    xr, yr = torch.view_as_real(x), torch.view_as_real(y)
+
+    def launch_rows():
+        _lib.check(lib.edgpu_spmv_c64(ctypes.byref(csr.struct()), ctypes.c_void_p(xr.data_ptr()),
+                                      ctypes.c_void_p(yr.data_ptr()), R, st), "spmv_c64")
+
     rows_s = timed(launch_rows, 10)
     # the same product from the row kernel: the schedule changes only the addition order
     y_rows = torch.empty_like(y)
     _lib.check(lib.edgpu_spmv_c64(ctypes.byref(csr.struct()), ctypes.c_void_p(xr.data_ptr()),
                                   ctypes.c_void_p(torch.view_as_real(y_rows).data_ptr()), R, st), "spmv_c64")
-    launch()
+    eng.spmv_into(csr, xr, yr, R, precision=1, mapping=mapping)
     torch.cuda.synchronize()
     agree = float((y - y_rows).abs().max() / y_rows.abs().max().clamp_min(1e-30))
     val_b = 4 if csr.val_cf is None else 8
@@ -358,7 +381,7 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
     avg64 = timed(lambda: eng.spmv_into(csr, x64r, y64r, R, precision=0, mapping=map64), 10)
     val64 = 8 if csr.val_c is None else 16
     alg64 = csr.nnz * (val64 + 4) + (csr.n + 1) * 8 + 2 * csr.n * R * 16
-    del y64, y, y_rows
+    del y64, y_rows
     peak = peaks.get("hbm_gbs")
     _, n_heavy = eng.spmv_plan(csr, mapping[1], mapping[2])
     return {
@@ -379,6 +402,11 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3):
                     "candidates_us": get_tuner_report("spmv", eng.spmv_key(csr, R, 1))},
         "row_kernel_us": round(rows_s * 1e6, 2),
         "vs_row_kernel_max_rel": agree,
+        "row_order": {"timed": best, "order_s": round(order_s, 3), "vs_sorted_max_rel": order_agree,
+                      "avg_launch_us": {k: round(v["avg"] * 1e6, 2) for k, v in runs.items()},
+                      "mapping": {k: list(v["mapping"]) for k, v in runs.items()},
+                      "note": ("locality: rows ordered by bath configuration, impurity spin-orbitals last; "
+                               "sorted: upstream's basis order")},
         "sector": {"n": int(csr.n), "nnz": int(csr.nnz), "R": R, "build_s": round(build_s, 3),
                    "model": "316 spin-orbitals, 30 bath levels, seed 3, <=2 bath holes; PS sector"},
         "fp64": {"achieved": round(alg64 / avg64 / 1e9, 1), "avg_launch_us": round(avg64 * 1e6, 2),
@@ -677,15 +705,21 @@ def large_config(eng, K=150, n_states=1):
         t64 = time.perf_counter() - t0
         sector = info.pop("sector_obj")
         t0 = time.perf_counter()
+        g64c, _ = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=1, matfree=False,
+                                sector=sector)
+        torch.cuda.synchronize()
+        t64c = time.perf_counter() - t0
+        t0 = time.perf_counter()
         g128, _ = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=0, sector=sector)
         torch.cuda.synchronize()
         t128 = time.perf_counter() - t0
-        errs = []
+        errs, errs_c = [], []
         for i in range(g128.shape[0]):
             for o in range(g128.shape[1]):
                 ref = g128[i, o].imag
                 if np.abs(ref).sum() > 0:
                     errs.append(float(np.abs(g64[i, o].imag - ref).sum() / np.abs(ref).sum()))
+                    errs_c.append(float(np.abs(g64c[i, o].imag - ref).sum() / np.abs(ref).sum()))
         # matrix-free H.v on this sector, R = the family's runs padded to a width the kernel
         # serves (as the recurrence does), complex64
         R = 2
@@ -704,10 +738,13 @@ def large_config(eng, K=150, n_states=1):
         torch.cuda.synchronize()
         hv_us = a.elapsed_time(b) * 1e3 / 5
         out[name] = {"sector": info["sector"], "runs": info["runs"], "hv_width": R, "k_len_min": min(info["k_len"]),
-                     "c64_matfree_s": round(t64, 3), "c128_csr_s": round(t128, 3),
+                     "sector_build_s": round(info["sector_s"], 3), "dgks_second_passes": info["second_passes"],
+                     "c64_matfree_s": round(t64 - info["sector_s"], 3), "c64_csr_s": round(t64c, 3),
+                     "c128_csr_s": round(t128, 3),
                      "rel_l1_vs_c128": {"max": max(errs), "median": float(np.median(errs))},
+                     "csr_rel_l1_vs_c128": {"max": max(errs_c), "median": float(np.median(errs_c))},
                      "matfree_hv_us": round(hv_us, 1), "csr_nnz": int(sector.csr.nnz)}
-        del sector, g64, g128
+        del sector, g64, g64c, g128
         torch.cuda.empty_cache()
     return out
 
@@ -865,7 +902,7 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-def run_hv_only():
+def run_hv_only(args):
     import torch
 
     import __graft_entry__
@@ -874,7 +911,8 @@ def run_hv_only():
     from impuritymodel_gb300.engine import get_engine
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    roof = hv_roofline(get_engine(), read_peaks(), launches=5, warmup=3)
+    orders = ("sorted", "locality") if args.hv_order == "both" else (args.hv_order,)
+    roof = hv_roofline(get_engine(), read_peaks(), launches=5, warmup=3, orders=orders)
     roof["traffic"] = traffic_scaled(roof)
     print(json.dumps({"roofline": roof}))
 
@@ -909,12 +947,13 @@ def run_profile_step(args):
 
 # DRAM bytes (read + write) per launch of the H.v kernel over its algorithmic bytes, from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on the same
-# 462 120-state sector; the bench line scales it to the launch it times.
-HV_DRAM_OVER_ALGORITHMIC = 1.103
+# 462 120-state sector in each row order; the bench line scales it to the launch it times.
+HV_DRAM_OVER_ALGORITHMIC = {"sorted": 1.103, "locality": None}
 
 
 def traffic_scaled(roof):
-    return int(HV_DRAM_OVER_ALGORITHMIC * roof["algorithmic_bytes_per_launch"])
+    ratio = HV_DRAM_OVER_ALGORITHMIC.get(roof.get("row_order", {}).get("timed", "sorted"))
+    return int(ratio * roof["algorithmic_bytes_per_launch"]) if ratio else None
 
 
 # ---------------------------------------------------------------------------------------
@@ -1140,6 +1179,8 @@ def main():
     ap.add_argument("--large-only", action="store_true", help="only the 316-spin-orbital large-sector line")
     ap.add_argument("--hv-only", action="store_true",
                     help="only the H.v roofline measurement (the case profiled under ncu)")
+    ap.add_argument("--hv-order", choices=["both", "sorted", "locality"], default="both",
+                    help="row orders of the sector timed by --hv-only")
     ap.add_argument("--profile-step", action="store_true",
                     help="warm up, then run one pipeline step inside the NVTX range 'pipeline_step'")
     ap.add_argument("--form", choices=list(FORMS),
@@ -1150,7 +1191,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.hv_only:
-        run_hv_only()
+        run_hv_only(args)
     elif args.large_only:
         run_large_only()
     elif args.profile_step:

@@ -11,196 +11,343 @@
 // for sectors of 1e5..1e6 states, where a complex64 recurrence without reorthogonalisation
 // loses orthogonality within a few dozen steps.
 //
+// Every pass streams V once from HBM, so the kernels are built for bandwidth: each thread
+// moves 16 bytes per access (two complex64 runs, or one complex128); the dot streams its
+// lanes through a cp.async ring in shared memory (several row steps in flight per thread
+// without holding them in registers), and the projection loads V with the streaming
+// (evict-first) policy, unrolled over vectors so that several 16-byte loads are in flight.
+//
 // Reductions: each thread sums its products over up to 8 rows in the vector type, then adds
 // that partial into an FP64 accumulator; blocks reduce in shared memory in a fixed tree and a
-// second launch adds the per-block partials in block order (deterministic, FP64 throughout
+// second launch adds the per-block partials in a fixed order (deterministic, FP64 throughout
 // above the first eight products).  Projections and scalings run in the vector type with the
-// FP64 coefficients rounded to it.  All passes are bound by HBM reads of V.
+// FP64 coefficients rounded to it.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace edgpu {
 namespace {
 
-template <typename T>
-struct Cplx;
+constexpr int kKmThreads = 256;
+constexpr int kKmChunk = 8;  // products summed in the vector type before an FP64 add
+constexpr int KD = 4;        // Krylov vectors per dot block (w is read once for all of them)
+constexpr int KB = 2048;     // projection coefficients staged in shared memory per round
+
+// One thread's lane: VW complex numbers of one row (consecutive runs).
+template <typename T, int VW>
+struct Lane;
 template <>
-struct Cplx<float> {
+struct Lane<float, 2> {
+  using type = float4;
+};
+template <>
+struct Lane<float, 1> {
   using type = float2;
 };
 template <>
-struct Cplx<double> {
+struct Lane<double, 1> {
   using type = double2;
 };
 
-constexpr int kKmThreads = 256;
-constexpr int kKmChunk = 8;  // products summed in the vector type before an FP64 add
+__device__ __forceinline__ void unpack(const float4& u, float (&re)[2], float (&im)[2]) {
+  re[0] = u.x;
+  im[0] = u.y;
+  re[1] = u.z;
+  im[1] = u.w;
+}
+__device__ __forceinline__ void unpack(const float2& u, float (&re)[1], float (&im)[1]) {
+  re[0] = u.x;
+  im[0] = u.y;
+}
+__device__ __forceinline__ void unpack(const double2& u, double (&re)[1], double (&im)[1]) {
+  re[0] = u.x;
+  im[0] = u.y;
+}
+__device__ __forceinline__ float4 pack(const float (&re)[2], const float (&im)[2]) {
+  return make_float4(re[0], im[0], re[1], im[1]);
+}
+__device__ __forceinline__ float2 pack(const float (&re)[1], const float (&im)[1]) {
+  return make_float2(re[0], im[0]);
+}
+__device__ __forceinline__ double2 pack(const double (&re)[1], const double (&im)[1]) {
+  return make_double2(re[0], im[0]);
+}
 
-inline int rows_per_block(int R) { return kKmThreads / R; }
+__device__ __forceinline__ void add_to(double& a, const double& b) { a += b; }
+__device__ __forceinline__ void add_to(double2& a, const double2& b) {
+  a.x += b.x;
+  a.y += b.y;
+}
 
-// partial[k][b][r] = sum over this block's rows of conj(V[k][i][r]) * w[i][r], for the KD
-// vectors k = blockIdx.y * KD + kk (w is read once for all of them)
-constexpr int KD = 4;
-
-template <typename T>
-__global__ void __launch_bounds__(kKmThreads) krylov_dot_kernel(const typename Cplx<T>::type* __restrict__ V,
-                                                               int64_t stride, int m, int64_t n, int R,
-                                                               const typename Cplx<T>::type* __restrict__ w,
-                                                               double2* __restrict__ partial) {
-  using CT = typename Cplx<T>::type;
-  __shared__ double2 red[kKmThreads];
-  const int rpb = kKmThreads / R;
-  const int tid = threadIdx.x;
-  const int r = tid % R, rr = tid / R;
-  const int k0 = blockIdx.y * KD;
-  const int kn = m - k0 < KD ? m - k0 : KD;
-  double sr[KD], si[KD];
-#pragma unroll
-  for (int kk = 0; kk < KD; ++kk) sr[kk] = si[kk] = 0.0;
-  if (rr < rpb) {
-    const int64_t step = (int64_t)gridDim.x * rpb;
-    int64_t i = (int64_t)blockIdx.x * rpb + rr;
-    while (i < n) {
-      T cr[KD], ci[KD];
-#pragma unroll
-      for (int kk = 0; kk < KD; ++kk) cr[kk] = ci[kk] = T(0);
-#pragma unroll 1
-      for (int c = 0; c < kKmChunk; ++c) {
-        if (i < n) {
-          const CT b = w[i * R + r];
-#pragma unroll
-          for (int kk = 0; kk < KD; ++kk) {
-            if (kk < kn) {
-              const CT a = V[(int64_t)(k0 + kk) * stride + i * R + r];
-              cr[kk] += a.x * b.x + a.y * b.y;
-              ci[kk] += a.x * b.y - a.y * b.x;
-            }
-          }
-        }
-        i += step;
-      }
-#pragma unroll
-      for (int kk = 0; kk < KD; ++kk) {
-        sr[kk] += (double)cr[kk];
-        si[kk] += (double)ci[kk];
-      }
-    }
-  }
-  for (int kk = 0; kk < kn; ++kk) {
-    red[tid] = make_double2(sr[kk], si[kk]);
-    __syncthreads();
-    // rows of the block: fixed tree over rr for each r
-    for (int h = (rpb + 1) / 2, len = rpb; len > 1; len = h, h = (h + 1) / 2) {
-      if (rr < len - h && rr + h < len) {
-        const double2 o = red[(rr + h) * R + r];
-        red[tid].x += o.x;
-        red[tid].y += o.y;
-      }
-      __syncthreads();
-    }
-    if (rr == 0) partial[((int64_t)(k0 + kk) * gridDim.x + blockIdx.x) * R + r] = red[r];
+// Fixed-order tree over the index rr of the values red[rr * width + c], rr < rows; every
+// thread of the block calls it (it synchronises).
+template <typename A>
+__device__ __forceinline__ void tree_rows(A* red, int tid, int rr, int rows, int width) {
+  for (int h = (rows + 1) / 2, len = rows; len > 1; len = h, h = (h + 1) / 2) {
+    if (rr + h < len) add_to(red[tid], red[tid + h * width]);
     __syncthreads();
   }
 }
 
-// h[k][r] = sum over blocks of partial[k][b][r] (block order)
-__global__ void krylov_dot_reduce_kernel(const double2* __restrict__ partial, int nb, int m, int R, double2* h) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)m * R) return;
-  const int k = (int)(t / R), r = (int)(t % R);
-  double sr = 0.0, si = 0.0;
-  for (int b = 0; b < nb; ++b) {
-    const double2 p = partial[((int64_t)k * nb + b) * R + r];
-    sr += p.x;
-    si += p.y;
+// Asynchronous 16- or 8-byte copies global -> shared (the thread's own lane of a stage).
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int kDotStages = 3;  // row steps of (w, KD vectors) in flight per thread
+
+// Shared memory of the dot kernel: [stage][KD + 1][thread] lanes.
+template <typename T, int VW>
+constexpr size_t dot_smem_bytes() {
+  return sizeof(typename Lane<T, VW>::type) * (size_t)kDotStages * (KD + 1) * kKmThreads;
+}
+
+// partial[k][b][r] = sum over block b's rows of conj(V[k][i][r]) * w[i][r], for the KD
+// vectors k = blockIdx.y * KD + kk.  Lanes: tpr = R / VW threads per row.  Each thread
+// streams its own lanes of w and of the KD vectors through a kDotStages-deep cp.async ring
+// in shared memory (a thread reads back only what it copied itself, so no block barrier is
+// needed inside the loop), which keeps kDotStages row steps of loads in flight per thread
+// without holding them in registers.
+template <typename T, int VW>
+__global__ void __launch_bounds__(kKmThreads)
+    krylov_dot_kernel(const typename Lane<T, VW>::type* __restrict__ V, int64_t stride_l, int m, int64_t n, int R,
+                      const typename Lane<T, VW>::type* __restrict__ w, double2* __restrict__ partial) {
+  using LT = typename Lane<T, VW>::type;
+  extern __shared__ __align__(16) unsigned char km_smem[];
+  LT* ring = reinterpret_cast<LT*>(km_smem);  // [kDotStages][KD + 1][kKmThreads]
+  __shared__ double2 red[kKmThreads];
+  const int tpr = R / VW, rpb = kKmThreads / tpr;
+  const int tid = threadIdx.x;
+  const int c = tid % tpr, rr = tid / tpr;
+  const int k0 = blockIdx.y * KD;
+  const int kn = m - k0 < KD ? m - k0 : KD;
+  double sr[KD][VW], si[KD][VW];
+#pragma unroll
+  for (int kk = 0; kk < KD; ++kk)
+#pragma unroll
+    for (int v = 0; v < VW; ++v) sr[kk][v] = si[kk][v] = 0.0;
+  const int64_t step = (int64_t)gridDim.x * rpb;
+  const int64_t i0 = (int64_t)blockIdx.x * rpb + rr;
+  const int64_t ns = (rr < rpb && i0 < n) ? (n - i0 + step - 1) / step : 0;  // this thread's row steps
+  auto issue = [&](int64_t s) {
+    if (s < ns) {
+      const int64_t e = (i0 + s * step) * tpr + c;
+      LT* slot = ring + (size_t)(s % kDotStages) * (KD + 1) * kKmThreads + tid;
+      cp_async<sizeof(LT)>(slot, w + e);
+#pragma unroll
+      for (int kk = 0; kk < KD; ++kk)
+        if (kk < kn) cp_async<sizeof(LT)>(slot + (kk + 1) * kKmThreads, V + (int64_t)(k0 + kk) * stride_l + e);
+    }
+    cp_async_commit();  // one group per step, empty past the end, so the wait count holds
+  };
+#pragma unroll
+  for (int s = 0; s < kDotStages - 1; ++s) issue(s);
+  for (int64_t s0 = 0; s0 < ns; s0 += kKmChunk) {
+    T cr[KD][VW], ci[KD][VW];
+#pragma unroll
+    for (int kk = 0; kk < KD; ++kk)
+#pragma unroll
+      for (int v = 0; v < VW; ++v) cr[kk][v] = ci[kk][v] = T(0);
+    const int64_t s1 = s0 + kKmChunk < ns ? s0 + kKmChunk : ns;
+    for (int64_t s = s0; s < s1; ++s) {
+      issue(s + kDotStages - 1);
+      cp_async_wait<kDotStages - 1>();  // step s has landed
+      const LT* slot = ring + (size_t)(s % kDotStages) * (KD + 1) * kKmThreads + tid;
+      T br[VW], bi[VW];
+      unpack(slot[0], br, bi);
+#pragma unroll
+      for (int kk = 0; kk < KD; ++kk) {
+        if (kk < kn) {
+          T ar[VW], ai[VW];
+          unpack(slot[(kk + 1) * kKmThreads], ar, ai);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) {
+            cr[kk][v] += ar[v] * br[v] + ai[v] * bi[v];
+            ci[kk][v] += ar[v] * bi[v] - ai[v] * br[v];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < KD; ++kk)
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        sr[kk][v] += (double)cr[kk][v];
+        si[kk][v] += (double)ci[kk][v];
+      }
   }
-  h[t] = make_double2(sr, si);
+  cp_async_wait<0>();
+#pragma unroll
+  for (int kk = 0; kk < KD; ++kk) {
+    if (kk < kn) {  // kn is the same for the whole block
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        red[tid] = make_double2(sr[kk][v], si[kk][v]);
+        __syncthreads();
+        tree_rows(red, tid, rr, rpb, tpr);
+        if (rr == 0) partial[((int64_t)(k0 + kk) * gridDim.x + blockIdx.x) * R + c * VW + v] = red[c];
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// h[k][r] = sum over blocks b of partial[k][b][r]: one block per k; the blocks are split
+// into kKmThreads / R interleaved slices summed in order, the slices added in a fixed tree.
+__global__ void __launch_bounds__(kKmThreads) krylov_dot_reduce_kernel(const double2* __restrict__ partial, int nb,
+                                                                      int R, double2* __restrict__ h) {
+  __shared__ double2 red[kKmThreads];
+  const int k = blockIdx.x, tid = threadIdx.x;
+  const int r = tid % R, s = tid / R, S = kKmThreads / R;
+  double2 acc = make_double2(0.0, 0.0);
+  if (s < S)
+    for (int b = s; b < nb; b += S) add_to(acc, partial[((int64_t)k * nb + b) * R + r]);
+  red[tid] = acc;
+  __syncthreads();
+  tree_rows(red, tid, s, S, R);
+  if (s == 0) h[(int64_t)k * R + r] = red[r];
 }
 
 // w[i][r] -= sum_k h[k][r] V[k][i][r]; with norms: per-block FP64 partials of |w[.][r]|^2
-template <typename T, int KB>
-__global__ void __launch_bounds__(kKmThreads) krylov_project_kernel(const typename Cplx<T>::type* __restrict__ V,
-                                                                   int64_t stride, int m, int64_t n, int R,
-                                                                   const double2* __restrict__ h,
-                                                                   typename Cplx<T>::type* __restrict__ w,
-                                                                   double* __restrict__ npart) {
-  using CT = typename Cplx<T>::type;
-  __shared__ CT hs[KB];
+template <typename T, int VW>
+__global__ void __launch_bounds__(kKmThreads)
+    krylov_project_kernel(const typename Lane<T, VW>::type* __restrict__ V, int64_t stride_l, int m, int64_t n, int R,
+                          const double2* __restrict__ h, typename Lane<T, VW>::type* __restrict__ w,
+                          double* __restrict__ npart) {
+  __shared__ T hre[KB], him[KB];
   __shared__ double red[kKmThreads];
-  const int rpb = kKmThreads / R;
+  const int tpr = R / VW, rpb = kKmThreads / tpr;
   const int tid = threadIdx.x;
-  const int r = tid % R, rr = tid / R;
-  double nacc = 0.0;
+  const int c = tid % tpr, rr = tid / tpr;
+  const int kpr = KB / R;  // vectors per staging round
+  double nacc[VW];
+#pragma unroll
+  for (int v = 0; v < VW; ++v) nacc[v] = 0.0;
   const int64_t step = (int64_t)gridDim.x * rpb;
-  for (int k0 = 0; k0 < m; k0 += KB / R) {
-    const int kc = (m - k0) < KB / R ? (m - k0) : KB / R;
+  for (int k0 = 0; k0 < m; k0 += kpr) {
+    const int kc = (m - k0) < kpr ? (m - k0) : kpr;
     __syncthreads();
     for (int t = tid; t < kc * R; t += kKmThreads) {
-      const double2 c = h[(int64_t)k0 * R + t];
-      hs[t] = CT{(T)c.x, (T)c.y};
+      const double2 cf = h[(int64_t)k0 * R + t];
+      hre[t] = (T)cf.x;
+      him[t] = (T)cf.y;
     }
     __syncthreads();
     if (rr < rpb) {
       for (int64_t i = (int64_t)blockIdx.x * rpb + rr; i < n; i += step) {
-        CT acc = w[i * R + r];
+        T wr[VW], wi[VW];
+        unpack(w[i * tpr + c], wr, wi);
+        const typename Lane<T, VW>::type* vp = V + (int64_t)k0 * stride_l + i * tpr + c;
+#pragma unroll 8
         for (int k = 0; k < kc; ++k) {
-          const CT c = hs[k * R + r];
-          const CT v = V[(int64_t)(k0 + k) * stride + i * R + r];
-          acc.x -= c.x * v.x - c.y * v.y;
-          acc.y -= c.x * v.y + c.y * v.x;
+          T vr[VW], vi[VW];
+          unpack(__ldcs(vp + (int64_t)k * stride_l), vr, vi);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) {
+            const T hr = hre[k * R + c * VW + v], hi = him[k * R + c * VW + v];
+            wr[v] -= hr * vr[v] - hi * vi[v];
+            wi[v] -= hr * vi[v] + hi * vr[v];
+          }
         }
-        w[i * R + r] = acc;
-        if (npart && k0 + kc >= m) nacc += (double)acc.x * acc.x + (double)acc.y * acc.y;
+        w[i * tpr + c] = pack(wr, wi);
+        if (npart && k0 + kc >= m) {
+#pragma unroll
+          for (int v = 0; v < VW; ++v) nacc[v] += (double)wr[v] * wr[v] + (double)wi[v] * wi[v];
+        }
       }
     }
   }
-  if (!npart) return;
-  red[tid] = nacc;
-  __syncthreads();
-  for (int hh = (rpb + 1) / 2, len = rpb; len > 1; len = hh, hh = (hh + 1) / 2) {
-    if (rr < len - hh && rr + hh < len) red[tid] += red[(rr + hh) * R + r];
+  if (!npart) return;  // the same for every thread of the launch
+#pragma unroll
+  for (int v = 0; v < VW; ++v) {
+    red[tid] = nacc[v];
+    __syncthreads();
+    tree_rows(red, tid, rr, rpb, tpr);
+    if (rr == 0) npart[(int64_t)blockIdx.x * R + c * VW + v] = red[c];
     __syncthreads();
   }
-  if (rr == 0 && tid < R) npart[(int64_t)blockIdx.x * R + r] = red[r];
 }
 
-// beta[r] = sqrt(sum_b npart[b][r]); v[i][r] = w[i][r] / beta[r] (0 when beta[r] == 0, and
-// the run's status flag set)
-template <typename T>
-__global__ void __launch_bounds__(kKmThreads) krylov_normalize_kernel(const double* __restrict__ npart, int nb,
-                                                                     int64_t n, int R,
-                                                                     const typename Cplx<T>::type* __restrict__ w,
-                                                                     typename Cplx<T>::type* __restrict__ v,
-                                                                     double* __restrict__ beta, int32_t* status) {
-  using CT = typename Cplx<T>::type;
-  __shared__ double sb[kKmThreads];
+// beta[r] = sqrt(sum_b npart[b][r]) in a fixed order (one block); beta == 0 sets the status
+__global__ void __launch_bounds__(kKmThreads) krylov_norm_reduce_kernel(const double* __restrict__ npart, int nb,
+                                                                       int R, double* __restrict__ beta,
+                                                                       int32_t* status) {
+  __shared__ double red[kKmThreads];
   const int tid = threadIdx.x;
-  if (tid < R) {
-    double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += npart[(int64_t)b * R + tid];
-    sb[tid] = sqrt(s);
-    if (blockIdx.x == 0) {
-      beta[tid] = sb[tid];
-      if (!(sb[tid] > 0.0) && status) atomicExch(status, (int32_t)EDGPU_ERR_BREAKDOWN);
-    }
-  }
+  const int r = tid % R, s = tid / R, S = kKmThreads / R;
+  double acc = 0.0;
+  if (s < S)
+    for (int b = s; b < nb; b += S) acc += npart[(int64_t)b * R + r];
+  red[tid] = acc;
   __syncthreads();
-  const int rpb = kKmThreads / R;
-  const int r = tid % R, rr = tid / R;
+  tree_rows(red, tid, s, S, R);
+  if (s == 0) {
+    const double b = sqrt(red[r]);
+    beta[r] = b;
+    if (!(b > 0.0) && status) atomicExch(status, (int32_t)EDGPU_ERR_BREAKDOWN);
+  }
+}
+
+// v[i][r] = w[i][r] / beta[r] (0 for a run whose beta is 0)
+template <typename T, int VW>
+__global__ void __launch_bounds__(kKmThreads) krylov_scale_kernel(const double* __restrict__ beta, int64_t n, int R,
+                                                                 const typename Lane<T, VW>::type* __restrict__ w,
+                                                                 typename Lane<T, VW>::type* __restrict__ v) {
+  const int tpr = R / VW, rpb = kKmThreads / tpr;
+  const int tid = threadIdx.x;
+  const int c = tid % tpr, rr = tid / tpr;
   if (rr >= rpb) return;
-  const double b = sb[r];
-  const T inv = b > 0.0 ? (T)(1.0 / b) : T(0);
+  T inv[VW];
+#pragma unroll
+  for (int q = 0; q < VW; ++q) {
+    const double b = beta[c * VW + q];
+    inv[q] = b > 0.0 ? (T)(1.0 / b) : T(0);
+  }
   for (int64_t i = (int64_t)blockIdx.x * rpb + rr; i < n; i += (int64_t)gridDim.x * rpb) {
-    const CT a = w[i * R + r];
-    v[i * R + r] = CT{a.x * inv, a.y * inv};
+    T re[VW], im[VW];
+    unpack(__ldcs(w + i * tpr + c), re, im);
+#pragma unroll
+    for (int q = 0; q < VW; ++q) {
+      re[q] *= inv[q];
+      im[q] *= inv[q];
+    }
+    v[i * tpr + c] = pack(re, im);
   }
 }
 
 inline int km_blocks(int64_t n, int R) {
-  const int rpb = rows_per_block(R);
+  const int rpb = kKmThreads / R;
   int64_t b = (n + rpb - 1) / rpb;
   const int64_t cap = (int64_t)grid_cap() * 4;
   if (b > cap) b = cap;
   return (int)(b > 0 ? b : 1);
+}
+
+inline bool a16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename T, int VW>
+void launch_dot(dim3 grid, cudaStream_t s, const typename Lane<T, VW>::type* V, int64_t stride_l, int m, int64_t n,
+                int R, const typename Lane<T, VW>::type* w, double2* partial) {
+  constexpr size_t smem = dot_smem_bytes<T, VW>();
+  // the ring is above the 48 KB default for 16-byte lanes (set on every call: per device)
+  cudaFuncSetAttribute(krylov_dot_kernel<T, VW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  krylov_dot_kernel<T, VW><<<grid, kKmThreads, smem, s>>>(V, stride_l, m, n, R, w, partial);
+}
+
+// complex64 pairs per thread when every access of the call is a 16-byte one
+inline bool pairs_ok(int R, int64_t stride, const void* a, const void* b) {
+  return (R % 2) == 0 && (stride % 2) == 0 && a16(a) && a16(b);
 }
 
 }  // namespace
@@ -220,19 +367,24 @@ extern "C" int edgpu_krylov_dot(int precision, const void* V, int64_t stride, in
   if (precision != 0 && precision != 1) return EDGPU_ERR_ARG;
   if (workspace_bytes < edgpu_krylov_workspace(n, R, m)) return EDGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  const int nb = km_blocks(n, R);
+  // row blocks: enough blocks for ~4 waves of 3 resident blocks per SM over all vector
+  // groups, so that each block streams many row steps through its ring (its fill and its
+  // reduction tree are paid once per block), at most the workspace's km_blocks
+  const int ny = (m + KD - 1) / KD;
+  const int nb = (int)std::min<int64_t>(km_blocks(n, R), std::max<int64_t>(1, ((int64_t)grid_cap() * 12 + ny - 1) / ny));
   double2* partial = reinterpret_cast<double2*>(workspace);
-  dim3 grid(nb, (m + KD - 1) / KD);
-  if (precision == 1)
-    krylov_dot_kernel<float><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const float2*>(V), stride, m, n, R,
-                                                         reinterpret_cast<const float2*>(w), partial);
+  dim3 grid(nb, ny);
+  if (precision == 1 && pairs_ok(R, stride, V, w))
+    launch_dot<float, 2>(grid, s, reinterpret_cast<const float4*>(V), stride / 2, m, n, R,
+                         reinterpret_cast<const float4*>(w), partial);
+  else if (precision == 1)
+    launch_dot<float, 1>(grid, s, reinterpret_cast<const float2*>(V), stride, m, n, R,
+                         reinterpret_cast<const float2*>(w), partial);
   else
-    krylov_dot_kernel<double><<<grid, kKmThreads, 0, s>>>(reinterpret_cast<const double2*>(V), stride, m, n, R,
-                                                          reinterpret_cast<const double2*>(w), partial);
+    launch_dot<double, 1>(grid, s, reinterpret_cast<const double2*>(V), stride, m, n, R,
+                          reinterpret_cast<const double2*>(w), partial);
   note_launch();
-  const int64_t t = (int64_t)m * R;
-  krylov_dot_reduce_kernel<<<(unsigned)((t + 255) / 256), 256, 0, s>>>(partial, nb, m, R,
-                                                                       reinterpret_cast<double2*>(h));
+  krylov_dot_reduce_kernel<<<m, kKmThreads, 0, s>>>(partial, nb, R, reinterpret_cast<double2*>(h));
   note_launch();
   return check_launch();
 }
@@ -247,14 +399,15 @@ extern "C" int edgpu_krylov_project(int precision, const void* V, int64_t stride
   const int nb = km_blocks(n, R);
   double* npart = with_norm ? reinterpret_cast<double*>(workspace) : nullptr;
   const double2* hc = reinterpret_cast<const double2*>(h);
-  constexpr int KB = 1024;  // coefficients staged per round (KB / R vectors)
-  if (R > KB) return EDGPU_ERR_ARG;
-  if (precision == 1)
-    krylov_project_kernel<float, KB><<<nb, kKmThreads, 0, s>>>(reinterpret_cast<const float2*>(V), stride, m, n, R,
-                                                               hc, reinterpret_cast<float2*>(w), npart);
+  if (precision == 1 && pairs_ok(R, stride, V, w))
+    krylov_project_kernel<float, 2><<<nb, kKmThreads, 0, s>>>(reinterpret_cast<const float4*>(V), stride / 2, m, n,
+                                                              R, hc, reinterpret_cast<float4*>(w), npart);
+  else if (precision == 1)
+    krylov_project_kernel<float, 1><<<nb, kKmThreads, 0, s>>>(reinterpret_cast<const float2*>(V), stride, m, n, R,
+                                                              hc, reinterpret_cast<float2*>(w), npart);
   else
-    krylov_project_kernel<double, KB><<<nb, kKmThreads, 0, s>>>(reinterpret_cast<const double2*>(V), stride, m, n,
-                                                                R, hc, reinterpret_cast<double2*>(w), npart);
+    krylov_project_kernel<double, 1><<<nb, kKmThreads, 0, s>>>(reinterpret_cast<const double2*>(V), stride, m, n,
+                                                               R, hc, reinterpret_cast<double2*>(w), npart);
   note_launch();
   return check_launch();
 }
@@ -267,12 +420,17 @@ extern "C" int edgpu_krylov_normalize(int precision, int64_t n, int R, const voi
   cudaStream_t s = (cudaStream_t)stream;
   const int nb = km_blocks(n, R);
   const double* npart = reinterpret_cast<const double*>(workspace);
-  if (precision == 1)
-    krylov_normalize_kernel<float><<<nb, kKmThreads, 0, s>>>(npart, nb, n, R, reinterpret_cast<const float2*>(w),
-                                                             reinterpret_cast<float2*>(v), beta, status_dev);
+  krylov_norm_reduce_kernel<<<1, kKmThreads, 0, s>>>(npart, nb, R, beta, status_dev);
+  note_launch();
+  if (precision == 1 && pairs_ok(R, R, w, v))
+    krylov_scale_kernel<float, 2><<<nb, kKmThreads, 0, s>>>(beta, n, R, reinterpret_cast<const float4*>(w),
+                                                            reinterpret_cast<float4*>(v));
+  else if (precision == 1)
+    krylov_scale_kernel<float, 1><<<nb, kKmThreads, 0, s>>>(beta, n, R, reinterpret_cast<const float2*>(w),
+                                                            reinterpret_cast<float2*>(v));
   else
-    krylov_normalize_kernel<double><<<nb, kKmThreads, 0, s>>>(npart, nb, n, R, reinterpret_cast<const double2*>(w),
-                                                              reinterpret_cast<double2*>(v), beta, status_dev);
+    krylov_scale_kernel<double, 1><<<nb, kKmThreads, 0, s>>>(beta, n, R, reinterpret_cast<const double2*>(w),
+                                                             reinterpret_cast<double2*>(v));
   note_launch();
   return check_launch();
 }

@@ -10,7 +10,8 @@
 //     it can act on b_i only when orbital k is empty in b_i.  The off-diagonal terms come
 //     bucketed by that key orbital; a warp serves one row, finds the empty orbitals of b_i
 //     (a few of several hundred in these models) and applies only the terms of their buckets,
-//     looks each result up in the sorted basis (binary search) and collects (column, conj(h))
+//     looks each result up in an open-addressing hash of the basis (edgpu_state_hash_build;
+//     binary search of the sorted basis when no table is given) and collects (column, conj(h))
 //     pairs in shared memory; then its lanes gather the x rows of the pairs, L lanes per pair
 //     (16 bytes each), and the partial sums of the row groups are added with xor shuffles.
 // The matrix-free product therefore costs term applications and L2 gathers, no CSR traffic.

@@ -40,6 +40,7 @@ class DeviceOp:
         flags = np.zeros(t, dtype=np.uint32)
         coeff = np.zeros((t, 2), dtype=np.float64)
         max_orb = -1
+        moved = []  # orbitals whose occupation an off-diagonal term changes
         for k, key in enumerate(keys):
             if len(key) > 4:
                 raise ValueError("terms with more than four operators are not supported")
@@ -56,10 +57,14 @@ class DeviceOp:
                 (cre if a == "c" else ann).append(i)
             ops[k] = packed
             flags[k] = (1 if sorted(cre) == sorted(ann) else 0) | (len(key) << 8)
+            if sorted(cre) != sorted(ann):
+                moved += sorted(set(cre) ^ set(ann))
             v = complex(op[key])
             coeff[k] = (v.real, v.imag)
         self.n_terms = t
         self.max_orbital = max_orb
+        # off-diagonal terms moving each orbital (host; orders sector rows for locality)
+        self.moves = np.bincount(np.array(moved, dtype=np.int64), minlength=max_orb + 1)
         self.is_real = bool(np.all(coeff[:, 1] == 0.0))
         self.nbytes = ops.nbytes + coeff.nbytes + flags.nbytes
         self.ops = torch.from_numpy(ops.view(np.int64)).to(device)
@@ -113,6 +118,7 @@ class CsrMatrix:
         self.ncols = self.n if ncols is None else int(ncols)
         self.nnz = col.numel()
         self._struct = None
+        self.order_tag = "sorted"  # row order (autotuner bucket): "sorted" basis or a permutation's tag
 
     def mixed(self):
         """Add the float32 / complex64 copy of H - shift*I used by the mixed-precision form.
@@ -176,6 +182,29 @@ class CsrMatrix:
 
     def value_bytes(self):
         return 16 if self.val_c is not None else 8
+
+    def permuted(self, perm, tag="permuted"):
+        """The same operator on the basis reordered by ``perm`` (new position -> old index):
+        P H P^T, row k' = old row perm[k'] with its columns renumbered and its entries kept in
+        their stored order (so every row sums its terms in the same order as before).  FP64
+        values only; call ``mixed()`` / ``double_float()`` on the result for the copies."""
+        n = self.n
+        if perm.numel() != n or self.ncols != n:
+            raise ValueError("permuted: square operator and a permutation of its rows needed")
+        dev = self.row_ptr.device
+        inv = torch.empty_like(perm)
+        inv[perm] = torch.arange(n, dtype=perm.dtype, device=dev)
+        lens = self.row_ptr[1:] - self.row_ptr[:-1]
+        rows = torch.repeat_interleave(torch.arange(n, device=dev), lens, output_size=self.nnz)
+        # entries grouped by new row; a stable sort keeps each row's stored order
+        idx = torch.sort(inv[rows], stable=True).indices
+        row_ptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        row_ptr[1:] = torch.cumsum(lens[perm], 0)
+        col = inv[self.col.to(torch.int64)[idx]].to(torch.int32)
+        out = CsrMatrix(row_ptr, col, val_c=None if self.val_c is None else self.val_c[idx].contiguous(),
+                        val_r=None if self.val_r is None else self.val_r[idx].contiguous())
+        out.order_tag = tag
+        return out
 
 
 COMPONENTS_KERNEL_MAX_ROWS = 1 << 16  # single-CTA label propagation of edgpu_components
@@ -817,8 +846,10 @@ class Engine:
 
     def spmv_key(self, csr, R, precision):
         """Autotuner bucket of an H.v launch: sizes as powers of two, vector width, types."""
-        return (bucket(csr.n), bucket(max(1, csr.nnz // max(csr.n, 1))), int(R), "c64" if precision else "c128",
-                "c" if (csr.val_c is not None or csr.val_cf is not None) else "r")
+        key = (bucket(csr.n), bucket(max(1, csr.nnz // max(csr.n, 1))), int(R), "c64" if precision else "c128",
+               "c" if (csr.val_c is not None or csr.val_cf is not None) else "r")
+        tag = getattr(csr, "order_tag", "sorted")
+        return key if tag == "sorted" else key + (tag,)
 
     def spmv_mapping(self, csr, xr, yr, R, precision):
         """The launch mapping the autotuner picked for this shape bucket, measured on this

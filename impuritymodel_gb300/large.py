@@ -23,6 +23,7 @@ reorthogonalisation.
 from __future__ import annotations
 
 import ctypes as C
+import time
 
 import numpy as np
 import torch
@@ -62,6 +63,50 @@ class MatfreeOp:
         self.is_real = self.diag.is_real and self.off.is_real
 
 
+LEAD_RATIO = 4.0  # an orbital moved by this many times the median count of terms is a lead orbital
+
+
+def locality_order(basis, dop, ratio=LEAD_RATIO):
+    """Row order of a sector in which states linked by the Hamiltonian sit near each other.
+
+    The lead orbitals (those that far more off-diagonal terms move than the median orbital:
+    the impurity's, in these models, where a 3d spin-orbital appears in hundreds of Coulomb
+    and hybridisation terms and a bath spin-orbital in its hybridisation pair) become the
+    least significant part of the sort key.  States that agree on every other orbital (one
+    bath configuration) then form one contiguous block of rows; a term that moves only lead
+    orbitals links rows of the same block, and a hybridisation term links two blocks whose
+    rows it pairs up in order.  The product H·x then gathers each x row for many entries of
+    nearby rows (cache reuse) instead of once per entry from far apart.
+
+    ``basis`` [n, W] int64 sorted product states.  Returns the permutation (new position ->
+    sorted index, int64 on the basis' device) or None when no orbital stands out (the sorted
+    order is kept)."""
+    moves = np.asarray(dop.moves)
+    nz = moves[moves > 0]
+    if nz.size == 0:
+        return None
+    lead = np.nonzero(moves > ratio * np.median(nz))[0]
+    if lead.size == 0 or lead.size == nz.size:
+        return None
+    n, W = basis.shape
+    mask = np.zeros(W, dtype=np.uint64)
+    for o in lead:
+        if o // 64 < W:
+            mask[o // 64] |= np.uint64(1) << np.uint64(63 - o % 64)
+    m = torch.from_numpy(mask.view(np.int64)).to(basis.device)
+    top = torch.tensor(-(1 << 63), dtype=torch.int64, device=basis.device)  # unsigned order as signed
+    major = torch.bitwise_xor(torch.bitwise_and(basis, torch.bitwise_not(m)), top)
+    minor = torch.bitwise_xor(torch.bitwise_and(basis, m), top)
+    order = torch.arange(n, dtype=torch.int64, device=basis.device)
+    # lexicographic on (major words, minor words): stable sorts from the least significant word
+    for key, skip in ((minor, mask == 0), (major, mask == np.uint64(0xFFFFFFFFFFFFFFFF))):
+        for q in reversed(range(W)):
+            if skip[q]:
+                continue
+            order = order[torch.sort(key[order, q], stable=True).indices]
+    return order
+
+
 def hv_diag(eng, basis_sorted, mop):
     """Diagonal of H on a sorted basis (FP64, [n])."""
     n, w = basis_sorted.shape
@@ -97,14 +142,24 @@ def hv_matfree_into(eng, basis_sorted, mop, restr, diag, x, y, shift=0.0, table=
     return y
 
 
-def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0):
-    """Batched Lanczos with two classical Gram-Schmidt passes per step against the whole
-    basis, for R runs at once.
+def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0, reorth="dgks"):
+    """Batched Lanczos with full reorthogonalisation against the whole basis, for R runs at
+    once.
+
+    ``reorth="dgks"`` (default): each step first takes the three-term recurrence (alpha'_j =
+    v_j^H w, w -= alpha'_j v_j + beta_{j-1} v_{j-1}), then one classical Gram-Schmidt pass
+    against every basis vector, and a second pass only for a step where the first removed
+    more than half of |w|^2 (the criterion of Daniel, Gragg, Kaufman and Stewart, 1976, with
+    eta = 1/sqrt(2); by Pythagoras |w_before|^2 = beta^2 + |h|^2, so the test is |h|^2 >
+    beta^2 for some run); the basis is read twice per step.  ``reorth="cgs2"``: two full
+    classical Gram-Schmidt passes every step (the basis read four times per step).
 
     ``v0`` [n, R] complex128, each column normalised; ``apply_h(x, y)`` writes y = (H - shift)
     x for [n, R] vectors of the run dtype (complex64 for ``precision=1``, complex128 for 0).
     Returns (alpha [R, K], beta [R, K] host float64 with ``shift`` added back to alpha,
     k_len [R]: the Krylov size of each run, cut at its first zero beta)."""
+    if reorth not in ("dgks", "cgs2"):
+        raise ValueError("reorth must be 'dgks' or 'cgs2'")
     n, R = v0.shape
     dt = torch.complex64 if precision else torch.complex128
     K = int(min(K, n))
@@ -113,28 +168,59 @@ def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0):
     w = torch.empty((n, R), dtype=dt, device=eng.device)
     h1 = torch.zeros((K, K, R), dtype=torch.complex128, device=eng.device)
     h2 = torch.zeros((K, K, R), dtype=torch.complex128, device=eng.device)
+    ha = torch.zeros((K, R), dtype=torch.complex128, device=eng.device)  # three-term alpha'
+    h3 = torch.zeros((2, R), dtype=torch.complex128, device=eng.device)  # [beta_{j-1}, alpha'_j]
     beta = torch.zeros((K, R), dtype=torch.float64, device=eng.device)
     scratch = torch.empty((n, R), dtype=dt, device=eng.device)
     ws, wsn = eng.workspace(eng.lib.edgpu_krylov_workspace(n, R, K))
     eng.reset_status()
     stride = n * R
-    Vp = torch.view_as_real(V)
     lib = eng.lib
+    wr = _ptr(torch.view_as_real(w))
+
+    def vp(k):
+        return _ptr(torch.view_as_real(V[k]))
+
+    def dot(k0, m, hrow):
+        L.check(lib.edgpu_krylov_dot(precision, vp(k0), stride, m, n, R, wr, _ptr(torch.view_as_real(hrow)), ws, wsn,
+                                     eng.stream), "krylov_dot")
+
+    def project(k0, m, hrows, with_norm):
+        L.check(lib.edgpu_krylov_project(precision, vp(k0), stride, m, n, R, _ptr(torch.view_as_real(hrows)), wr,
+                                         with_norm, ws, wsn, eng.stream), "krylov_project")
+
+    def normalize(dst, j):
+        L.check(lib.edgpu_krylov_normalize(precision, n, R, wr, _ptr(torch.view_as_real(dst)), _ptr(beta[j]),
+                                           _ptr(eng.status), ws, wsn, eng.stream), "krylov_normalize")
+
+    second = 0
     for j in range(K):
         apply_h(V[j], w)
         m = j + 1
-        for hbuf, last in ((h1, False), (h2, True)):
-            L.check(lib.edgpu_krylov_dot(precision, _ptr(Vp), stride, m, n, R, _ptr(torch.view_as_real(w)),
-                                         _ptr(torch.view_as_real(hbuf[j])), ws, wsn, eng.stream), "krylov_dot")
-            L.check(lib.edgpu_krylov_project(precision, _ptr(Vp), stride, m, n, R,
-                                             _ptr(torch.view_as_real(hbuf[j])), _ptr(torch.view_as_real(w)),
-                                             1 if last else 0, ws, wsn, eng.stream), "krylov_project")
         dst = V[j + 1] if j + 1 < K else scratch
-        L.check(lib.edgpu_krylov_normalize(precision, n, R, _ptr(torch.view_as_real(w)),
-                                           _ptr(torch.view_as_real(dst)), _ptr(beta[j]), _ptr(eng.status), ws, wsn,
-                                           eng.stream), "krylov_normalize")
+        if reorth == "cgs2":
+            for hbuf, last in ((h1, 0), (h2, 1)):
+                dot(0, m, hbuf[j])
+                project(0, m, hbuf[j], last)
+            normalize(dst, j)
+            continue
+        dot(j, 1, ha[j])
+        if j == 0:
+            project(0, 1, ha[0:1], 0)
+        else:
+            h3[0].copy_(beta[j - 1])
+            h3[1].copy_(ha[j])
+            project(j - 1, 2, h3, 0)
+        dot(0, m, h1[j])
+        project(0, m, h1[j], 1)
+        normalize(dst, j)
+        if bool(((h1[j].real ** 2 + h1[j].imag ** 2).sum(0) > beta[j] ** 2).any()):
+            dot(0, m, h2[j])
+            project(0, m, h2[j], 1)
+            normalize(dst, j)
+            second += 1
     idx = torch.arange(K, device=eng.device)
-    alpha = (h1[idx, idx].real + h2[idx, idx].real).t().contiguous() + shift
+    alpha = (ha.real + h1[idx, idx].real + h2[idx, idx].real).t().contiguous() + shift
     a = alpha.cpu().numpy()
     b = beta.t().contiguous().cpu().numpy()
     k_len = np.full(R, K, dtype=np.int32)
@@ -142,45 +228,86 @@ def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0):
         z = np.nonzero(b[r] == 0.0)[0]
         if z.size:
             k_len[r] = int(z[0]) + 1
+    lanczos_reorth_batched.second_passes = second
     return a, b, k_len
 
 
-def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K=150, precision=1, matfree=True):
+def ordered_sector(eng, sector, dop, order=True):
+    """(basis [n, W] in the row order the recurrence runs in, the permutation new -> sorted
+    index or None) of a sector; the locality order of :func:`locality_order` when ``order``,
+    else the sorted order.  Cached on the sector."""
+    cache = sector.__dict__.setdefault("_large", {})
+    key = ("order", bool(order))
+    if key not in cache:
+        perm = locality_order(sector.basis, dop) if order else None
+        basis = sector.basis if perm is None else sector.basis[perm].contiguous()
+        cache[key] = (basis, perm)
+    return cache[key]
+
+
+def _sector_operator(eng, sector, dop, mop, order, precision, matfree):
+    """apply_h(x, y) writing (H - shift) x in the sector's run order, and the shift; the
+    pieces (diagonal, hash table, reordered CSR and its float copies) are cached on the
+    sector."""
+    basis, perm = ordered_sector(eng, sector, dop, order)
+    cache = sector.__dict__["_large"]
+    if precision and matfree:
+        key = ("matfree", perm is not None, id(mop))
+        if key not in cache:
+            diag = hv_diag(eng, basis, mop)
+            cache[key] = (diag, float(diag.mean().item()), state_hash(eng, basis))
+        diag, shift, table = cache[key]
+        restr = cache.get("restr")
+
+        def apply_h(x, y):
+            hv_matfree_into(eng, basis, mop, restr, diag, x, y, shift, table)
+        return apply_h, shift
+    key = ("csr", perm is not None)
+    if key not in cache:
+        cache[key] = sector.csr if perm is None else sector.csr.permuted(perm, "locality")
+    csr = cache[key]
+    if precision:
+        csr.mixed()
+
+        def apply_h(x, y):
+            eng.spmv_into(csr, torch.view_as_real(x), torch.view_as_real(y), x.shape[1], precision=1)
+        return apply_h, csr.mixed_shift
+
+    def apply_h(x, y):
+        if eng.spmv_planned_ok(x.shape[1], 0):
+            eng.spmv_into(csr, torch.view_as_real(x), torch.view_as_real(y), x.shape[1], precision=0)
+        else:
+            y.copy_(eng.spmv(csr, x))
+    return apply_h, 0.0
+
+
+def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K=150, precision=1, matfree=True,
+                order=True):
     """Continued-fraction Green's functions of R normalised start vectors ``v0`` [n, R] on a
     large ``sector`` (its sorted basis and, for the CSR path, its Hamiltonian).
 
     ``precision=1``: complex64 vectors, H matrix-free (or the complex64 CSR copy), FP64
-    reductions; ``precision=0``: complex128 vectors on the FP64 CSR (the reference).  Returns
-    (g [R, n_omega] complex128 host, alpha, beta, k_len)."""
-    csr = sector.csr
-    shift = 0.0
-    if precision:
-        if matfree:
-            diag = hv_diag(eng, sector.basis, mop)
-            shift = float(diag.mean().item())
-            table = state_hash(eng, sector.basis)
+    reductions; ``precision=0``: complex128 vectors on the FP64 CSR (the reference).
+    ``order``: the recurrence runs on the rows in :func:`locality_order` (v0 is permuted in,
+    the coefficients do not depend on the row order).  Returns (g [R, n_omega] complex128
+    host, alpha, beta, k_len)."""
+    sector.__dict__.setdefault("_large", {})["restr"] = restr
+    apply_h, shift = _sector_operator(eng, sector, dop, mop, order, precision, matfree)
+    _, perm = ordered_sector(eng, sector, dop, order)
+    if perm is not None:
+        v0 = v0[perm]
+    return _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision)
 
-            def apply_h(x, y):
-                hv_matfree_into(eng, sector.basis, mop, restr, diag, x, y, shift, table)
-        else:
-            csr.mixed()
-            shift = csr.mixed_shift
 
-            def apply_h(x, y):
-                eng.spmv_into(csr, torch.view_as_real(x), torch.view_as_real(y), x.shape[1], precision=1)
-    else:
-        def apply_h(x, y):
-            if eng.spmv_planned_ok(x.shape[1], 0):
-                eng.spmv_into(csr, torch.view_as_real(x), torch.view_as_real(y), x.shape[1], precision=0)
-            else:
-                y.copy_(eng.spmv(csr, x))
+def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision):
+    """green_large after the row order and the operator are fixed."""
     # the H.v kernels serve R / (complex numbers per 16 bytes) lanes per row, a divisor of
     # 32: the run count is padded with empty runs (they stop at their first step)
     R = v0.shape[1]
     runs16 = 2 if precision else 1
     if R > 32 * runs16:  # more runs than one H.v launch serves: in chunks
-        parts = [green_large(eng, dop, mop, restr, sector, v0[:, c:c + 32 * runs16], scale[c:c + 32 * runs16],
-                             e_runs[c:c + 32 * runs16], omega, delta, K, precision, matfree)
+        parts = [_green_ordered(eng, apply_h, shift, v0[:, c:c + 32 * runs16], scale[c:c + 32 * runs16],
+                                e_runs[c:c + 32 * runs16], omega, delta, K, precision)
                  for c in range(0, R, 32 * runs16)]
         Kc = max(p[1].shape[1] for p in parts)
         pad = lambda x: np.pad(x, ((0, 0), (0, Kc - x.shape[1])))  # noqa: E731
@@ -201,7 +328,7 @@ def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K
 
 
 def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, precision=1, matfree=True,
-                  slaterWeightMin=1e-7, sector=None):
+                  slaterWeightMin=1e-7, sector=None, order=True):
     """Spectra ``g[n_states, n_ops, n_w]`` of transition operators on large sectors (upstream
     getSpectra, impurityModel/ed/spectra.py:684-806: T psi, normalised, Green's function
     scaled by the squared norm), every (operator, state) run in one batched recurrence on the
@@ -221,8 +348,12 @@ def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, prec
     g = np.zeros((ne, no, len(w)), dtype=np.complex128)
     if not runs:
         return g, {"runs": 0}
+    sector_s = 0.0
     if sector is None:
+        t0 = time.perf_counter()
         sector = Sector(eng, dop, restr, torch.cat(states, 0))
+        torch.cuda.synchronize(eng.device)
+        sector_s = time.perf_counter() - t0
     n = sector.n
     R = len(runs)
     v0 = torch.zeros((n, R), dtype=torch.complex128, device=eng.device)
@@ -234,7 +365,9 @@ def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, prec
         scale[r] = nrm * nrm
         v0[rows, r] = vals / nrm
     e_runs = [es[i] for i, _ in runs]
-    gr, a, b, k_len = green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, w, delta, K, precision, matfree)
+    gr, a, b, k_len = green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, w, delta, K, precision, matfree,
+                                  order)
     for r, (i, o) in enumerate(runs):
         g[i, o] = gr[r]
-    return g, {"runs": R, "sector": int(n), "k_len": [int(x) for x in k_len], "sector_obj": sector}
+    return g, {"runs": R, "sector": int(n), "k_len": [int(x) for x in k_len], "sector_obj": sector,
+               "sector_s": sector_s, "second_passes": getattr(lanczos_reorth_batched, "second_passes", None)}
