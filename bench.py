@@ -749,6 +749,80 @@ def large_config(eng, K=150, n_states=1):
     return out
 
 
+def krylov_roofline(eng, peaks, n=462120, R=16, K=150, ms=(1, 16, 75, 150), precision=1, reps=5):
+    """The large-sector Krylov kernels (edgpu_krylov_dot / _project / _normalize) on random
+    complex64 (or complex128) vectors of the 316-orbital PS sector's shape: n rows, R runs, a
+    basis of K vectors; per m (vectors in the pass) the mean CUDA-event time of back-to-back
+    calls and the algorithmic bytes over it (dot: m + 1 vectors read; projection: m read, w
+    read and written; normalisation: w read, v written), against the measured HBM copy peak."""
+    import ctypes as C
+
+    import torch
+
+    from impuritymodel_gb300 import _lib as L
+    from impuritymodel_gb300.engine import _ptr
+
+    lib = eng.lib
+    dt = torch.complex64 if precision else torch.complex128
+    esz = 8 if precision else 16
+    g = torch.Generator(device=eng.device).manual_seed(0)
+    V = torch.randn((K, n, R), dtype=dt, device=eng.device, generator=g)
+    w = torch.randn((n, R), dtype=dt, device=eng.device, generator=g)
+    h = torch.zeros((K, R), dtype=torch.complex128, device=eng.device)
+    beta = torch.zeros(R, dtype=torch.float64, device=eng.device)
+    out = torch.empty_like(w)
+    wsn = lib.edgpu_krylov_workspace(n, R, K)
+    ws = torch.empty(wsn, dtype=torch.uint8, device=eng.device)
+    wsp = C.c_void_p(ws.data_ptr())
+    Vp, wp, hp = _ptr(torch.view_as_real(V)), _ptr(torch.view_as_real(w)), _ptr(torch.view_as_real(h))
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps * 1e3
+
+    peak = peaks.get("hbm_gbs")
+    vb = n * R * esz
+    res = {}
+    for m in ms:
+        d = timed(lambda: L.check(lib.edgpu_krylov_dot(precision, Vp, n * R, m, n, R, wp, hp, wsp, wsn, eng.stream),
+                                  "krylov_dot"))
+        p = timed(lambda: L.check(lib.edgpu_krylov_project(precision, Vp, n * R, m, n, R, hp, wp, 1, wsp, wsn,
+                                                           eng.stream), "krylov_project"))
+        z = timed(lambda: L.check(lib.edgpu_krylov_normalize(precision, n, R, wp, _ptr(torch.view_as_real(out)),
+                                                             _ptr(beta), _ptr(eng.status), wsp, wsn, eng.stream),
+                                  "krylov_normalize"))
+        row = {}
+        for name, us, nbytes in (("dot", d, (m + 1) * vb), ("project", p, (m + 2) * vb), ("normalize", z, 2 * vb)):
+            gbs = nbytes / us / 1e3
+            row[name] = {"us": round(us, 1), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3) if peak else None}
+        res[str(m)] = row
+    del V
+    torch.cuda.empty_cache()
+    return {"n": n, "R": R, "K": K, "dtype": "c64" if precision else "c128", "by_m": res,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+
+def run_krylov_only(args):
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from impuritymodel_gb300.engine import get_engine
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ms = tuple(int(x) for x in args.krylov_m.split(","))
+    print(json.dumps({"krylov_kernels": krylov_roofline(get_engine(), read_peaks(), K=args.krylov_k, ms=ms)}))
+
+
 def run_large_only():
     import torch
 
@@ -758,7 +832,10 @@ def run_large_only():
     from impuritymodel_gb300.engine import get_engine
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps({"large_316orb": large_config(get_engine())}))
+    eng = get_engine()
+    out = large_config(eng)
+    out["krylov_kernels"] = krylov_roofline(eng, read_peaks())
+    print(json.dumps({"large_316orb": out}))
 
 
 def run_gpu(args):
@@ -863,6 +940,8 @@ def run_gpu(args):
     batched = batched_configs(eng) if (rank == 0 and not args.skip_batched) else None
     prune_info = pruning_setup(eng)[1] if (rank == 0 and not args.skip_batched) else None
     large = large_config(eng) if (rank == 0 and not args.skip_batched) else None
+    if large is not None:
+        large["krylov_kernels"] = krylov_roofline(eng, peaks)
     cpu = cpu_baseline() if (rank == 0 and not args.skip_cpu) else None
     if rank == 0:
         line = {
@@ -1179,6 +1258,10 @@ def main():
     ap.add_argument("--large-only", action="store_true", help="only the 316-spin-orbital large-sector line")
     ap.add_argument("--hv-only", action="store_true",
                     help="only the H.v roofline measurement (the case profiled under ncu)")
+    ap.add_argument("--krylov-only", action="store_true",
+                    help="only the large-sector Krylov kernel timings (the case profiled under ncu)")
+    ap.add_argument("--krylov-k", type=int, default=150, help="basis vectors held by --krylov-only")
+    ap.add_argument("--krylov-m", default="1,16,75,150", help="vectors per pass timed by --krylov-only")
     ap.add_argument("--hv-order", choices=["both", "sorted", "locality"], default="both",
                     help="row orders of the sector timed by --hv-only")
     ap.add_argument("--profile-step", action="store_true",
@@ -1192,6 +1275,8 @@ def main():
         run_reference(args)
     elif args.hv_only:
         run_hv_only(args)
+    elif args.krylov_only:
+        run_krylov_only(args)
     elif args.large_only:
         run_large_only()
     elif args.profile_step:

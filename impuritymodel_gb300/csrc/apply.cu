@@ -8,6 +8,8 @@
 //   warp-wide sum of one state's hundreds of diagonal terms kept the FP64 pipe busy); the
 //   off-diagonal emissions go to a per-warp shared-memory buffer where equal output states
 //   are merged in term order.  This reproduces upstream's sequential dict sums bit for bit.
+//   Operators whose bucket index fits in shared memory run apply_columns_bucket_kernel
+//   instead (same outputs): each state tries only the terms that can act on it.
 // apply_vector: raw emissions of an operator on a weighted multi-state psi, in (state, term)
 //   order, for a later stable sort + segmented sum.
 #include "common.cuh"
@@ -268,6 +270,280 @@ __global__ void __launch_bounds__(256) apply_columns_kernel(ColParams p) {
   }
 }
 
+// Bucketed form of apply_columns_kernel for operators with many terms (same outputs, bit for
+// bit).  A term can act on a state only if every orbital it creates without annihilating is
+// empty there, so the off-diagonal terms are bucketed by one such key orbital (the lowest) and
+// a state tries only the buckets of its empty orbitals (plus the terms without a key orbital);
+// the diagonal terms form one bucket tried in term order.  Each block builds the buckets of the
+// term table in shared memory once (stable: term order within a bucket); warps then run their
+// states independently (no block barrier per state):
+//   * diagonal sum: lanes test 32 diagonal terms at a time, and the valid signed coefficients
+//     are broadcast in term order (shuffles) into one FP64 chain that every lane runs, so the
+//     sum is upstream's sequential one;
+//   * off-diagonal emissions from the buckets land in the per-warp buffer in bucket order and
+//     are put back into term order by a rank sort on the term index before the merge, which is
+//     the one of apply_columns_kernel.
+constexpr int kBucketWarps = 4;
+
+template <int W>
+__device__ __forceinline__ int term_bucket(uint64_t ops, uint32_t flags) {
+  constexpr int NKEY = 64 * W;  // key orbitals; NKEY: no key orbital; NKEY + 1: diagonal
+  if (flags & 1u) return NKEY + 1;
+  int cre[4], ann[4], nc = 0, na = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t op = (uint32_t)(ops >> (16 * k)) & 0xFFFFu;
+    if (!(op & 0x8000u)) continue;
+    const int orb = (int)(op & 0x3FFu);
+    if (op & 0x4000u)
+      cre[nc++] = orb;
+    else
+      ann[na++] = orb;
+  }
+  int key = NKEY;
+  for (int a = 0; a < nc; ++a) {
+    bool annihilated = false;
+    for (int b = 0; b < na; ++b) annihilated |= ann[b] == cre[a];
+    if (!annihilated && cre[a] < key) key = cre[a];
+  }
+  return key;  // orbitals at or beyond NKEY (outside the state) also fall in bucket NKEY
+}
+
+template <int W>
+__global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel(ColParams p) {
+  constexpr int NB = 64 * W + 2;
+  constexpr int NOKEY = 64 * W, DIAG = 64 * W + 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int T = p.n_terms;
+  int* bptr = reinterpret_cast<int*>(smem);  // [NB + 1]
+  int* cursor = bptr + NB + 1;               // [NB]
+  int* blist = cursor + NB;                  // [T]
+  const size_t index_bytes = ((size_t)4 * (2 * NB + 1 + T) + 15) & ~(size_t)15;
+  // bucket sizes, their scan, then a stable fill by warp 0 (term order within a bucket)
+  for (int b = threadIdx.x; b < NB; b += blockDim.x) cursor[b] = 0;
+  __syncthreads();
+  int cplx = 0;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    atomicAdd(&cursor[term_bucket<W>(__ldg(p.ops + t), __ldg(p.flags + t))], 1);
+    cplx |= __ldg(&p.coeff[t].y) != 0.0;
+  }
+  cplx = __syncthreads_or(cplx);
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < NB; ++b) {
+      bptr[b] = acc;
+      acc += cursor[b];
+      cursor[b] = bptr[b];
+    }
+    bptr[NB] = acc;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    for (int base = 0; base < T; base += 32) {
+      const int t = base + lane;
+      const int k = t < T ? term_bucket<W>(__ldg(p.ops + t), __ldg(p.flags + t)) : -1;
+      const unsigned peers = __match_any_sync(FULL, k);
+      if (t < T) blist[cursor[k] + __popc(peers & ((1u << lane) - 1u))] = t;
+      __syncwarp();
+      if (t < T && (peers & ((1u << lane) - 1u)) == 0) cursor[k] += __popc(peers);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+
+  const int cap = p.cap;
+  const size_t per_warp = ((size_t)cap * (24 + 8 * W) + 15) & ~(size_t)15;
+  unsigned char* wbase = smem + index_bytes + per_warp * warp;
+  double2* wvals = reinterpret_cast<double2*>(wbase);
+  uint64_t* wkeys = reinterpret_cast<uint64_t*>(wbase + 16 * (size_t)cap);
+  int* wtidx = reinterpret_cast<int*>(wbase + (16 + 8 * W) * (size_t)cap);
+  int* wperm = wtidx + cap;
+  const bool fill = p.offsets != nullptr;
+  const int wpb = blockDim.x >> 5;
+  const int64_t nwarps = (int64_t)gridDim.x * wpb;
+  for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += nwarps) {
+    uint64_t s0[W];
+    load_state<W>(p.states + j * W, s0);
+    // diagonal entry: the valid diagonal terms summed in term order
+    double dre = 0.0, dim = 0.0;
+    int dfirst = -1;
+    for (int b = bptr[DIAG]; b < bptr[DIAG + 1]; b += 32) {
+      const int i = b + lane;
+      bool valid = false;
+      double cx = 0.0, cy = 0.0;
+      int t = 0;
+      if (i < bptr[DIAG + 1]) {
+        t = blist[i];
+        uint64_t s[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) s[q] = s0[q];
+        int par = 0;
+        valid = apply_term<W>(s, __ldg(p.ops + t), par);
+        if (valid) {
+          double2 c = __ldg(&p.coeff[t]);
+          if (par & 1) {
+            c.x = neg_bits(c.x);
+            c.y = neg_bits(c.y);
+          }
+          cx = c.x;
+          cy = c.y;
+        }
+      }
+      unsigned vm = __ballot_sync(FULL, valid);
+      while (vm) {
+        const int src = __ffs(vm) - 1;
+        vm &= vm - 1;
+        const double x = __shfl_sync(FULL, cx, src), y = __shfl_sync(FULL, cy, src);
+        const int ts = __shfl_sync(FULL, t, src);
+        if (dfirst < 0) {
+          dre = x;
+          dim = y;
+          dfirst = ts;
+        } else {
+          dre = __dadd_rn(dre, x);
+          // real operator: every imaginary part is a signed zero, and the sum of signed zeros
+          // is -0 only when all of them are -0 (IEEE round to nearest)
+          dim = cplx ? __dadd_rn(dim, y) : __longlong_as_double(__double_as_longlong(dim) & __double_as_longlong(y));
+        }
+      }
+    }
+    // off-diagonal emissions from the buckets of the empty orbitals and the keyless terms
+    int m = 0;
+    auto run_bucket = [&](int lo, int hi) {
+      for (int b = lo; b < hi; b += 32) {
+        const int i = b + lane;
+        bool valid = false;
+        uint64_t s[W];
+        double2 c = make_double2(0.0, 0.0);
+        int t = 0;
+        if (i < hi) {
+          t = blist[i];
+#pragma unroll
+          for (int q = 0; q < W; ++q) s[q] = s0[q];
+          int par = 0;
+          valid = apply_term<W>(s, __ldg(p.ops + t), par);
+          if (valid) {
+            c = __ldg(&p.coeff[t]);
+            if (par & 1) {
+              c.x = neg_bits(c.x);
+              c.y = neg_bits(c.y);
+            }
+          }
+        }
+        const unsigned bo = __ballot_sync(FULL, valid);
+        if (bo) {
+          const int pos = m + __popc(bo & ((1u << lane) - 1u));
+          if (valid && pos < cap) {
+#pragma unroll
+            for (int q = 0; q < W; ++q) wkeys[(size_t)pos * W + q] = s[q];
+            wvals[pos] = c;
+            wtidx[pos] = t;
+          }
+          m += __popc(bo);
+        }
+      }
+    };
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+      uint64_t bits = ~s0[q];
+      while (bits) {
+        const int z = __clzll(bits);  // orbital q * 64 + z (most significant bit first)
+        bits &= ~(1ull << (63 - z));
+        const int orb = q * 64 + z;
+        const int lo = bptr[orb], hi = bptr[orb + 1];
+        if (hi > lo) run_bucket(lo, hi);
+      }
+    }
+    run_bucket(bptr[NOKEY], bptr[NOKEY + 1]);
+    __syncwarp();  // the emission buffer is complete before other lanes read it
+    if (m > cap) {
+      if (lane == 0) {
+        atomicExch(p.status, (int32_t)EDGPU_ERR_OVERFLOW);
+        if (!fill) p.counts[j] = 0;
+      }
+      __syncwarp();
+      continue;
+    }
+    // term order: rank of each emission by its term index (a term emits once per state)
+    for (int k = lane; k < m; k += 32) {
+      const int tk = wtidx[k];
+      int r = 0;
+      for (int e = 0; e < m; ++e) r += wtidx[e] < tk;
+      wperm[r] = k;
+    }
+    __syncwarp();
+    // Diagonal entry (output == input state).
+    bool dkeep = false;
+    int64_t didx = -1;
+    if (dfirst >= 0) {
+      dkeep = abs2_py(dre, dim) >= p.weight_min && restr_ok<W>(p.restr, s0);
+      if (dkeep) dkeep = filter_pass<W>(p, s0, didx);
+    }
+    int kept = 0;     // kept off-diagonal heads so far (warp uniform)
+    int dbefore = 0;  // kept heads with first term index < dfirst
+    const int64_t obase = fill ? p.offsets[j] : 0;
+    for (int c0 = 0; c0 < m; c0 += 32) {
+      const int k = c0 + lane;
+      bool keep = false;
+      double sre = 0.0, sim = 0.0;
+      int64_t idx = -1;
+      uint64_t key[W];
+      int tk = 0x7fffffff;
+      if (k < m) {
+        const int pk = wperm[k];
+#pragma unroll
+        for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)pk * W + q];
+        bool head = true;
+        for (int e = 0; e < k; ++e) {
+          if (state_eq<W>(key, wkeys + (size_t)wperm[e] * W)) {
+            head = false;
+            break;
+          }
+        }
+        if (head) {
+          double2 v = wvals[pk];
+          sre = v.x;
+          sim = v.y;
+          for (int e = k + 1; e < m; ++e) {
+            const int pe = wperm[e];
+            if (state_eq<W>(key, wkeys + (size_t)pe * W)) {
+              double2 u = wvals[pe];
+              sre = __dadd_rn(sre, u.x);
+              sim = __dadd_rn(sim, u.y);
+            }
+          }
+          keep = abs2_py(sre, sim) >= p.weight_min && restr_ok<W>(p.restr, key);
+          if (keep) keep = filter_pass<W>(p, key, idx);
+          tk = wtidx[pk];
+        }
+      }
+      const unsigned bk = __ballot_sync(FULL, keep);
+      const unsigned bb = __ballot_sync(FULL, keep && dkeep && tk < dfirst);
+      if (fill && keep) {
+        const int rank = kept + __popc(bk & ((1u << lane) - 1u)) + ((dkeep && dfirst < tk) ? 1 : 0);
+        const int64_t o = obase + rank;
+        if (p.out_states) store_state<W>(p.out_states + o * W, key);
+        if (p.out_index) p.out_index[o] = idx;
+        if (p.out_vals) p.out_vals[o] = make_double2(sre, p.conj_vals ? neg_bits(sim) : sim);
+      }
+      kept += __popc(bk);
+      dbefore += __popc(bb);
+    }
+    if (!fill) {
+      if (lane == 0) p.counts[j] = kept + (dkeep ? 1 : 0);
+    } else if (dkeep && lane == 0) {
+      const int64_t o = obase + dbefore;
+      if (p.out_states) store_state<W>(p.out_states + o * W, s0);
+      if (p.out_index) p.out_index[o] = didx;
+      if (p.out_vals) p.out_vals[o] = make_double2(dre, p.conj_vals ? neg_bits(dim) : dim);
+    }
+    __syncwarp();
+  }
+}
+
 struct VecParams {
   const uint64_t* states;
   const double2* amps;
@@ -379,6 +655,25 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
     warps = 8;
     while (warps > 1 && per_warp * warps > smem_max) warps >>= 1;
     if (per_warp * warps > smem_max) return EDGPU_ERR_ARG;
+  }
+  // the bucketed kernel when its term index and four warps' emission buffers fit
+  const int nb_keys = 64 * n_words + 2;
+  const size_t index_bytes = ((size_t)4 * (2 * nb_keys + 1 + p.n_terms) + 15) & ~(size_t)15;
+  const size_t bucket_warp = (((size_t)p.cap * (24 + 8 * (size_t)n_words)) + 15) & ~(size_t)15;
+  int bwarps = kBucketWarps;
+  while (bwarps > 1 && index_bytes + bucket_warp * bwarps > smem_max) bwarps >>= 1;
+  const size_t bucket_smem = index_bytes + bucket_warp * bwarps;
+  if (bucket_smem <= smem_max) {
+    int64_t blocks = (n_states + bwarps - 1) / bwarps;
+    const int64_t cap_blocks = (int64_t)grid_cap() * 8;
+    if (blocks > cap_blocks) blocks = cap_blocks;
+    EDGPU_DISPATCH_W(n_words, {
+      cudaFuncSetAttribute(apply_columns_bucket_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)bucket_smem);
+      apply_columns_bucket_kernel<W><<<(unsigned)blocks, 32 * bwarps, bucket_smem, s>>>(p);
+      note_launch();
+    });
+    return check_launch();
   }
   const size_t smem = (p.stage_terms ? term_bytes : 0) + per_warp * warps;
   const int threads = 32 * warps;
