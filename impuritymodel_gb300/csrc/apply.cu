@@ -309,6 +309,14 @@ __device__ __forceinline__ int term_bucket(uint64_t ops, uint32_t flags) {
   return key;  // orbitals at or beyond NKEY (outside the state) also fall in bucket NKEY
 }
 
+// Per-warp shared memory of the bucketed kernel: emissions (value, state, basis index, term
+// index, group slot), the hash table (slot, smallest term index, size) and the kept-head
+// bitmask over term indices with its prefix counts.
+__host__ __device__ inline size_t bucket_warp_bytes(int cap, int W, int T) {
+  const size_t nwt = (size_t)((T + 31) >> 5);
+  return ((size_t)cap * (16 + 8 * (size_t)W + 8 + 4 + 4 + 12) + nwt * 8 + 15) & ~(size_t)15;
+}
+
 template <int W>
 __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel(ColParams p) {
   constexpr int NB = 64 * W + 2;
@@ -355,27 +363,39 @@ __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel
   __syncthreads();
 
   const int cap = p.cap;
-  const size_t per_warp = ((size_t)cap * (24 + 8 * W) + 15) & ~(size_t)15;
+  const int ht = cap;                // hash slots: a power of two, at least m (open addressing)
+  const int nwt = (T + 31) >> 5;     // words of the kept-head bitmask over term indices
+  const size_t per_warp = bucket_warp_bytes(cap, W, T);
   unsigned char* wbase = smem + index_bytes + per_warp * warp;
   double2* wvals = reinterpret_cast<double2*>(wbase);
   uint64_t* wkeys = reinterpret_cast<uint64_t*>(wbase + 16 * (size_t)cap);
-  int* wtidx = reinterpret_cast<int*>(wbase + (16 + 8 * W) * (size_t)cap);
-  int* wperm = wtidx + cap;
+  int64_t* widx = reinterpret_cast<int64_t*>(wbase + (16 + 8 * W) * (size_t)cap);
+  int* wtidx = reinterpret_cast<int*>(widx + cap);
+  int* wslot = wtidx + cap;
+  int* hslot = wslot + cap;
+  int* hmin = hslot + ht;
+  int* hcnt = hmin + ht;
+  unsigned* kbits = reinterpret_cast<unsigned*>(hcnt + ht);
+  int* kpre = reinterpret_cast<int*>(kbits + nwt);
   const bool fill = p.offsets != nullptr;
   const int wpb = blockDim.x >> 5;
   const int64_t nwarps = (int64_t)gridDim.x * wpb;
   for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += nwarps) {
     uint64_t s0[W];
     load_state<W>(p.states + j * W, s0);
-    // diagonal entry: the valid diagonal terms summed in term order
+    // diagonal entry: the valid diagonal terms summed in term order (not needed when the
+    // basis filter drops the input state itself: its output could not be kept)
     double dre = 0.0, dim = 0.0;
     int dfirst = -1;
-    for (int b = bptr[DIAG]; b < bptr[DIAG + 1]; b += 32) {
+    const int dend = (p.filter == EDGPU_FILTER_NOT_IN_BASIS && find_state<W>(p.basis, p.n_basis, s0) >= 0)
+                         ? bptr[DIAG]
+                         : bptr[DIAG + 1];
+    for (int b = bptr[DIAG]; b < dend; b += 32) {
       const int i = b + lane;
       bool valid = false;
       double cx = 0.0, cy = 0.0;
       int t = 0;
-      if (i < bptr[DIAG + 1]) {
+      if (i < dend) {
         t = blist[i];
         uint64_t s[W];
 #pragma unroll
@@ -467,14 +487,89 @@ __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel
       __syncwarp();
       continue;
     }
-    // term order: rank of each emission by its term index (a term emits once per state)
+    // Merge equal output states.  A per-warp hash table maps each emission to the group of
+    // its output state: the group's head is its member with the smallest term index, its
+    // value the members' sum in term order (upstream's sequential dict sums); kept heads set
+    // their term index in a bitmask whose prefix counts give each output's rank in term order.
+    for (int h = lane; h < ht; h += 32) {
+      hslot[h] = -1;
+      hmin[h] = 0x7fffffff;
+      hcnt[h] = 0;
+    }
+    for (int q = lane; q < nwt; q += 32) kbits[q] = 0u;
+    __syncwarp();
     for (int k = lane; k < m; k += 32) {
-      const int tk = wtidx[k];
-      int r = 0;
-      for (int e = 0; e < m; ++e) r += wtidx[e] < tk;
-      wperm[r] = k;
+      uint64_t key[W];
+#pragma unroll
+      for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)k * W + q];
+      uint64_t hv = 0x9E3779B97F4A7C15ull;
+#pragma unroll
+      for (int q = 0; q < W; ++q) {
+        hv ^= key[q] + 0x9E3779B97F4A7C15ull + (hv << 6) + (hv >> 2);
+        hv *= 0xBF58476D1CE4E5B9ull;
+        hv ^= hv >> 31;
+      }
+      int h = (int)(hv & (uint64_t)(ht - 1));
+      for (int probe = 0; probe < ht; ++probe) {  // m <= ht groups: a free or equal slot is found
+        const int old = atomicCAS(&hslot[h], -1, k);
+        if (old == -1 || state_eq<W>(key, wkeys + (size_t)old * W)) break;
+        h = (h + 1) & (ht - 1);
+      }
+      wslot[k] = h;
+      atomicMin(&hmin[h], wtidx[k]);
+      atomicAdd(&hcnt[h], 1);
     }
     __syncwarp();
+    // heads: value, restriction / weight / basis filters; kept heads mark their term index
+    for (int k = lane; k < m; k += 32) {
+      const int h = wslot[k], tk = wtidx[k];
+      if (tk != hmin[h]) continue;
+      uint64_t key[W];
+#pragma unroll
+      for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)k * W + q];
+      double2 v = wvals[k];
+      if (hcnt[h] > 1) {  // the other members in increasing term index
+        int cur = tk;
+        for (int g = 1; g < hcnt[h]; ++g) {
+          int nxt = 0x7fffffff, ne = -1;
+          for (int e = 0; e < m; ++e)
+            if (wslot[e] == h && wtidx[e] > cur && wtidx[e] < nxt) {
+              nxt = wtidx[e];
+              ne = e;
+            }
+          const double2 u = wvals[ne];
+          v.x = __dadd_rn(v.x, u.x);
+          v.y = __dadd_rn(v.y, u.y);
+          cur = nxt;
+        }
+        wvals[k] = v;  // read back only by this lane
+      }
+      int64_t idx = -1;
+      bool keep = abs2_py(v.x, v.y) >= p.weight_min && restr_ok<W>(p.restr, key);
+      if (keep) keep = filter_pass<W>(p, key, idx);
+      if (keep) {
+        widx[k] = idx;
+        atomicOr(&kbits[tk >> 5], 1u << (tk & 31));
+      }
+    }
+    __syncwarp();
+    // exclusive prefix counts of kept heads per 32 term indices
+    int run = 0;
+    for (int q0 = 0; q0 < nwt; q0 += 32) {
+      const int q = q0 + lane;
+      const int c = q < nwt ? __popc(kbits[q]) : 0;
+      int incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (q < nwt) kpre[q] = run + incl - c;
+      run += __shfl_sync(FULL, incl, 31);
+    }
+    __syncwarp();
+    const int kept = run;
+    auto kept_below = [&](int t) { return kpre[t >> 5] + __popc(kbits[t >> 5] & ((1u << (t & 31)) - 1u)); };
     // Diagonal entry (output == input state).
     bool dkeep = false;
     int64_t didx = -1;
@@ -482,60 +577,26 @@ __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel
       dkeep = abs2_py(dre, dim) >= p.weight_min && restr_ok<W>(p.restr, s0);
       if (dkeep) dkeep = filter_pass<W>(p, s0, didx);
     }
-    int kept = 0;     // kept off-diagonal heads so far (warp uniform)
-    int dbefore = 0;  // kept heads with first term index < dfirst
-    const int64_t obase = fill ? p.offsets[j] : 0;
-    for (int c0 = 0; c0 < m; c0 += 32) {
-      const int k = c0 + lane;
-      bool keep = false;
-      double sre = 0.0, sim = 0.0;
-      int64_t idx = -1;
-      uint64_t key[W];
-      int tk = 0x7fffffff;
-      if (k < m) {
-        const int pk = wperm[k];
-#pragma unroll
-        for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)pk * W + q];
-        bool head = true;
-        for (int e = 0; e < k; ++e) {
-          if (state_eq<W>(key, wkeys + (size_t)wperm[e] * W)) {
-            head = false;
-            break;
-          }
-        }
-        if (head) {
-          double2 v = wvals[pk];
-          sre = v.x;
-          sim = v.y;
-          for (int e = k + 1; e < m; ++e) {
-            const int pe = wperm[e];
-            if (state_eq<W>(key, wkeys + (size_t)pe * W)) {
-              double2 u = wvals[pe];
-              sre = __dadd_rn(sre, u.x);
-              sim = __dadd_rn(sim, u.y);
-            }
-          }
-          keep = abs2_py(sre, sim) >= p.weight_min && restr_ok<W>(p.restr, key);
-          if (keep) keep = filter_pass<W>(p, key, idx);
-          tk = wtidx[pk];
-        }
-      }
-      const unsigned bk = __ballot_sync(FULL, keep);
-      const unsigned bb = __ballot_sync(FULL, keep && dkeep && tk < dfirst);
-      if (fill && keep) {
-        const int rank = kept + __popc(bk & ((1u << lane) - 1u)) + ((dkeep && dfirst < tk) ? 1 : 0);
-        const int64_t o = obase + rank;
-        if (p.out_states) store_state<W>(p.out_states + o * W, key);
-        if (p.out_index) p.out_index[o] = idx;
-        if (p.out_vals) p.out_vals[o] = make_double2(sre, p.conj_vals ? neg_bits(sim) : sim);
-      }
-      kept += __popc(bk);
-      dbefore += __popc(bb);
-    }
     if (!fill) {
       if (lane == 0) p.counts[j] = kept + (dkeep ? 1 : 0);
-    } else if (dkeep && lane == 0) {
-      const int64_t o = obase + dbefore;
+      __syncwarp();
+      continue;
+    }
+    const int64_t obase = p.offsets[j];
+    for (int k = lane; k < m; k += 32) {
+      const int h = wslot[k], tk = wtidx[k];
+      if (tk != hmin[h] || !((kbits[tk >> 5] >> (tk & 31)) & 1u)) continue;
+      const int64_t o = obase + kept_below(tk) + ((dkeep && dfirst < tk) ? 1 : 0);
+      uint64_t key[W];
+#pragma unroll
+      for (int q = 0; q < W; ++q) key[q] = wkeys[(size_t)k * W + q];
+      const double2 v = wvals[k];
+      if (p.out_states) store_state<W>(p.out_states + o * W, key);
+      if (p.out_index) p.out_index[o] = widx[k];
+      if (p.out_vals) p.out_vals[o] = make_double2(v.x, p.conj_vals ? neg_bits(v.y) : v.y);
+    }
+    if (dkeep && lane == 0) {
+      const int64_t o = obase + (dfirst >= 0 ? kept_below(dfirst) : 0);
       if (p.out_states) store_state<W>(p.out_states + o * W, s0);
       if (p.out_index) p.out_index[o] = didx;
       if (p.out_vals) p.out_vals[o] = make_double2(dre, p.conj_vals ? neg_bits(dim) : dim);
@@ -659,11 +720,11 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
   // the bucketed kernel when its term index and four warps' emission buffers fit
   const int nb_keys = 64 * n_words + 2;
   const size_t index_bytes = ((size_t)4 * (2 * nb_keys + 1 + p.n_terms) + 15) & ~(size_t)15;
-  const size_t bucket_warp = (((size_t)p.cap * (24 + 8 * (size_t)n_words)) + 15) & ~(size_t)15;
+  const size_t bucket_warp = bucket_warp_bytes(p.cap, n_words, p.n_terms);
   int bwarps = kBucketWarps;
   while (bwarps > 1 && index_bytes + bucket_warp * bwarps > smem_max) bwarps >>= 1;
   const size_t bucket_smem = index_bytes + bucket_warp * bwarps;
-  if (bucket_smem <= smem_max) {
+  if (bucket_smem <= smem_max && (p.cap & (p.cap - 1)) == 0) {
     int64_t blocks = (n_states + bwarps - 1) / bwarps;
     const int64_t cap_blocks = (int64_t)grid_cap() * 8;
     if (blocks > cap_blocks) blocks = cap_blocks;
