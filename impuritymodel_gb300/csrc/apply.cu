@@ -36,6 +36,7 @@ struct ColParams {
   int conj_vals;
   int cap;
   int stage_terms;
+  int diag_group;  // bucketed kernel: states per warp whose diagonal sums run one per lane
   int32_t* status;
 };
 
@@ -314,7 +315,7 @@ __device__ __forceinline__ int term_bucket(uint64_t ops, uint32_t flags) {
 // bitmask over term indices with its prefix counts.
 __host__ __device__ inline size_t bucket_warp_bytes(int cap, int W, int T) {
   const size_t nwt = (size_t)((T + 31) >> 5);
-  return ((size_t)cap * (16 + 8 * (size_t)W + 8 + 4 + 4 + 12) + nwt * 8 + 15) & ~(size_t)15;
+  return ((size_t)cap * (16 + 8 * (size_t)W + 8 + 4 + 4 + 12) + nwt * 8 + 32 * 20 + 15) & ~(size_t)15;
 }
 
 template <int W>
@@ -377,17 +378,62 @@ __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel
   int* hcnt = hmin + ht;
   unsigned* kbits = reinterpret_cast<unsigned*>(hcnt + ht);
   int* kpre = reinterpret_cast<int*>(kbits + nwt);
+  double* gre = reinterpret_cast<double*>(wbase + (((size_t)cap * (16 + 8 * W + 8 + 4 + 4 + 12) + nwt * 8 + 7) & ~(size_t)7));
+  double* gim = gre + 32;
+  int* gfirst = reinterpret_cast<int*>(gim + 32);
   const bool fill = p.offsets != nullptr;
   const int wpb = blockDim.x >> 5;
   const int64_t nwarps = (int64_t)gridDim.x * wpb;
-  for (int64_t j = (int64_t)blockIdx.x * wpb + warp; j < p.n_states; j += nwarps) {
+  const int G = p.diag_group;  // 1: each state's diagonal terms tested 32 at a time
+  for (int64_t jg = ((int64_t)blockIdx.x * wpb + warp) * G; jg < p.n_states; jg += nwarps * G) {
+  if (G > 1) {
+    // the diagonal sums of the group's states, one state per lane, each in term order
+    const int64_t jl = jg + lane;
+    double re = 0.0, im = 0.0;
+    int first = -1;
+    if (lane < G && jl < p.n_states) {
+      uint64_t s0[W];
+      load_state<W>(p.states + jl * W, s0);
+      // not needed when the basis filter drops the input state itself
+      const bool drop = p.filter == EDGPU_FILTER_NOT_IN_BASIS && find_state<W>(p.basis, p.n_basis, s0) >= 0;
+      const int dend = drop ? bptr[DIAG] : bptr[DIAG + 1];
+      for (int d = bptr[DIAG]; d < dend; ++d) {
+        const int t = blist[d];
+        uint64_t s[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) s[q] = s0[q];
+        int par = 0;
+        if (!apply_term<W>(s, __ldg(p.ops + t), par)) continue;
+        double2 c = __ldg(&p.coeff[t]);
+        if (par & 1) {
+          c.x = neg_bits(c.x);
+          c.y = neg_bits(c.y);
+        }
+        if (first < 0) {
+          re = c.x;
+          im = c.y;
+          first = t;
+        } else {
+          re = __dadd_rn(re, c.x);
+          im = cplx ? __dadd_rn(im, c.y) : __longlong_as_double(__double_as_longlong(im) & __double_as_longlong(c.y));
+        }
+      }
+    }
+    gre[lane] = re;
+    gim[lane] = im;
+    gfirst[lane] = first;
+    __syncwarp();
+  }
+  const int gn = (int)((p.n_states - jg) < G ? (p.n_states - jg) : G);
+  for (int l = 0; l < gn; ++l) {
+    const int64_t j = jg + l;
     uint64_t s0[W];
     load_state<W>(p.states + j * W, s0);
     // diagonal entry: the valid diagonal terms summed in term order (not needed when the
     // basis filter drops the input state itself: its output could not be kept)
-    double dre = 0.0, dim = 0.0;
-    int dfirst = -1;
-    const int dend = (p.filter == EDGPU_FILTER_NOT_IN_BASIS && find_state<W>(p.basis, p.n_basis, s0) >= 0)
+    double dre = G > 1 ? gre[l] : 0.0, dim = G > 1 ? gim[l] : 0.0;
+    int dfirst = G > 1 ? gfirst[l] : -1;
+    const int dend = (G > 1 || (p.filter == EDGPU_FILTER_NOT_IN_BASIS && find_state<W>(p.basis, p.n_basis, s0) >= 0))
                          ? bptr[DIAG]
                          : bptr[DIAG + 1];
     for (int b = bptr[DIAG]; b < dend; b += 32) {
@@ -603,6 +649,8 @@ __global__ void __launch_bounds__(32 * kBucketWarps) apply_columns_bucket_kernel
     }
     __syncwarp();
   }
+  __syncwarp();  // the group's diagonal sums are read before the next group writes them
+  }
 }
 
 struct VecParams {
@@ -725,7 +773,12 @@ extern "C" int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t 
   while (bwarps > 1 && index_bytes + bucket_warp * bwarps > smem_max) bwarps >>= 1;
   const size_t bucket_smem = index_bytes + bucket_warp * bwarps;
   if (bucket_smem <= smem_max && (p.cap & (p.cap - 1)) == 0) {
-    int64_t blocks = (n_states + bwarps - 1) / bwarps;
+    // diagonal sums one state per lane when there are states enough for two groups per warp
+    // of a full grid (8 warps resident per SM); below 8 states a group, 32 lanes per state
+    const int64_t resident = (int64_t)grid_cap() * 8;
+    int64_t g = n_states / (2 * resident);
+    p.diag_group = g >= 8 ? (int)(g < 32 ? g : 32) : 1;
+    int64_t blocks = (n_states + (int64_t)bwarps * p.diag_group - 1) / ((int64_t)bwarps * p.diag_group);
     const int64_t cap_blocks = (int64_t)grid_cap() * 8;
     if (blocks > cap_blocks) blocks = cap_blocks;
     EDGPU_DISPATCH_W(n_words, {
