@@ -704,11 +704,16 @@ def large_config(eng, K=150, n_states=1):
         torch.cuda.synchronize()
         t64 = time.perf_counter() - t0
         sector = info.pop("sector_obj")
-        t0 = time.perf_counter()
-        g64c, _ = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=1, matfree=False,
-                                sector=sector)
-        torch.cuda.synchronize()
-        t64c = time.perf_counter() - t0
+        # the complex64 CSR form twice: the first call also runs the H.v autotuner for this
+        # shape (timed apart), the second is the steady state
+        t64c_first = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            g64c, _ = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=1,
+                                    matfree=False, sector=sector)
+            torch.cuda.synchronize()
+            t64c = time.perf_counter() - t0
+            t64c_first = t64c if t64c_first is None else t64c_first
         t0 = time.perf_counter()
         g128, _ = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=0, sector=sector)
         torch.cuda.synchronize()
@@ -740,6 +745,7 @@ def large_config(eng, K=150, n_states=1):
         out[name] = {"sector": info["sector"], "runs": info["runs"], "hv_width": R, "k_len_min": min(info["k_len"]),
                      "sector_build_s": round(info["sector_s"], 3), "dgks_second_passes": info["second_passes"],
                      "c64_matfree_s": round(t64 - info["sector_s"], 3), "c64_csr_s": round(t64c, 3),
+                     "c64_csr_first_call_s": round(t64c_first, 3),
                      "c128_csr_s": round(t128, 3),
                      "rel_l1_vs_c128": {"max": max(errs), "median": float(np.median(errs))},
                      "csr_rel_l1_vs_c128": {"max": max(errs_c), "median": float(np.median(errs_c))},

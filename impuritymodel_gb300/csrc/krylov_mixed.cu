@@ -90,14 +90,28 @@ __device__ __forceinline__ void tree_rows(A* red, int tid, int rr, int rows, int
   }
 }
 
-// Asynchronous 16- or 8-byte copies global -> shared (the thread's own lane of a stage).
+// Asynchronous 16- or 8-byte copies global -> shared (the thread's own lane of a stage), with
+// an L2 eviction-priority policy: the basis vectors stream through once (evict first), w is
+// read again by every vector group of the pass (evict last).
 template <int BYTES>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, uint64_t pol) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
   if constexpr (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "l"(pol)
+                 : "memory");
   else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
@@ -140,14 +154,16 @@ __global__ void __launch_bounds__(kKmThreads)
   const int64_t step = (int64_t)gridDim.x * rpb;
   const int64_t i0 = (int64_t)blockIdx.x * rpb + rr;
   const int64_t ns = (rr < rpb && i0 < n) ? (n - i0 + step - 1) / step : 0;  // this thread's row steps
+  const uint64_t pol_v = l2_evict_first(), pol_w = l2_evict_last();
   auto issue = [&](int64_t s) {
     if (s < ns) {
       const int64_t e = (i0 + s * step) * tpr + c;
       LT* slot = ring + (size_t)(s % kDotStages) * (KD + 1) * kKmThreads + tid;
-      cp_async<sizeof(LT)>(slot, w + e);
+      cp_async<sizeof(LT)>(slot, w + e, pol_w);
 #pragma unroll
       for (int kk = 0; kk < KD; ++kk)
-        if (kk < kn) cp_async<sizeof(LT)>(slot + (kk + 1) * kKmThreads, V + (int64_t)(k0 + kk) * stride_l + e);
+        if (kk < kn)
+          cp_async<sizeof(LT)>(slot + (kk + 1) * kKmThreads, V + (int64_t)(k0 + kk) * stride_l + e, pol_v);
     }
     cp_async_commit();  // one group per step, empty past the end, so the wait count holds
   };
@@ -314,22 +330,33 @@ __global__ void __launch_bounds__(kKmThreads) krylov_scale_kernel(const double* 
     const double b = beta[c * VW + q];
     inv[q] = b > 0.0 ? (T)(1.0 / b) : T(0);
   }
-  for (int64_t i = (int64_t)blockIdx.x * rpb + rr; i < n; i += (int64_t)gridDim.x * rpb) {
-    T re[VW], im[VW];
-    unpack(__ldcs(w + i * tpr + c), re, im);
+  // four row steps per iteration: their loads are issued before any store
+  constexpr int U = 4;
+  const int64_t step = (int64_t)gridDim.x * rpb;
+  for (int64_t i0 = (int64_t)blockIdx.x * rpb + rr; i0 < n; i0 += U * step) {
+    typename Lane<T, VW>::type a[U];
 #pragma unroll
-    for (int q = 0; q < VW; ++q) {
-      re[q] *= inv[q];
-      im[q] *= inv[q];
+    for (int u = 0; u < U; ++u)
+      if (i0 + u * step < n) a[u] = __ldcs(w + (i0 + u * step) * tpr + c);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u * step >= n) break;
+      T re[VW], im[VW];
+      unpack(a[u], re, im);
+#pragma unroll
+      for (int q = 0; q < VW; ++q) {
+        re[q] *= inv[q];
+        im[q] *= inv[q];
+      }
+      v[(i0 + u * step) * tpr + c] = pack(re, im);
     }
-    v[i * tpr + c] = pack(re, im);
   }
 }
 
 inline int km_blocks(int64_t n, int R) {
   const int rpb = kKmThreads / R;
   int64_t b = (n + rpb - 1) / rpb;
-  const int64_t cap = (int64_t)grid_cap() * 4;
+  const int64_t cap = (int64_t)grid_cap() * 5;  // the projection's register limit: 5 blocks per SM
   if (b > cap) b = cap;
   return (int)(b > 0 ? b : 1);
 }

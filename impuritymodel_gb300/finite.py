@@ -204,13 +204,43 @@ def norm2(psi):
 # ---------------------------------------------------------------------------------------
 
 
+def _combination_masks(idx, k, n_bits):
+    """Occupation masks [C, n_bits] (bool) of itertools.combinations(idx, k), in its order.
+
+    For k above half of the index list the complements (the holes) are enumerated instead:
+    the lexicographic order of k-subsets is the reverse lexicographic order of their
+    complements, so the hole masks are generated and reversed."""
+    idx = np.asarray(idx, dtype=np.int64)
+    m = idx.size
+    if k < 0 or k > m:
+        return np.zeros((0, n_bits), dtype=bool)
+    holes = k > m - k
+    r = m - k if holes else k
+    if r == 0:
+        combos = np.zeros((1, 0), dtype=np.int64)
+    else:
+        combos = np.array(list(itertools.combinations(range(m), r)), dtype=np.int64).reshape(-1, r)
+    out = np.zeros((combos.shape[0], n_bits), dtype=bool)
+    if r:
+        out[np.arange(combos.shape[0])[:, None], idx[combos]] = True
+    if holes:
+        full = np.zeros(n_bits, dtype=bool)
+        full[idx] = True
+        out = (full[None, :] & ~out)[::-1]
+    return out
+
+
 def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
-    """Restricted basis of product states, in upstream's itertools order."""
+    """Restricted basis of product states, in upstream's itertools order (upstream
+    get_basis, impurityModel/ed/finite.py).  The occupations are built as bit masks: per
+    angular momentum the impurity x valence x conduction combinations, then the product over
+    angular momenta, each state the union of its parts packed big-endian into bytes."""
     for l in nBaths.keys():
         assert valBaths[l] <= nBaths[l]
-    basis_l = {}
+    n = sum(2 * (2 * ang + 1) + nb for ang, nb in nBaths.items())
+    parts = []
     for l in nBaths.keys():
-        basis_l[l] = []
+        blocks = []
         for dn_val in range(dnValBaths[l] + 1):
             for dn_con in range(dnConBaths[l] + 1):
                 dn_imp = dn_val - dn_con
@@ -221,27 +251,25 @@ def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
                     assert n_val <= valBaths[l]
                     assert n_con <= nBaths[l] - valBaths[l]
                     assert n_imp <= 2 * (2 * l + 1)
-                    idx = [c2i(nBaths, (l, s, m)) for s in range(2) for m in range(-l, l + 1)]
-                    b_imp = tuple(itertools.combinations(idx, n_imp))
+                    idx = [c2i(nBaths, (l, s_, m_)) for s_ in range(2) for m_ in range(-l, l + 1)]
+                    b_imp = _combination_masks(idx, n_imp, n)
                     if valBaths[l] == 0:
-                        b_val = ((),)
+                        b_val = np.zeros((1, n), dtype=bool)
                     else:
-                        idx = [c2i(nBaths, (l, b)) for b in range(valBaths[l])]
-                        b_val = tuple(itertools.combinations(idx, n_val))
+                        b_val = _combination_masks([c2i(nBaths, (l, b_)) for b_ in range(valBaths[l])], n_val, n)
                     if nBaths[l] - valBaths[l] == 0:
-                        b_con = ((),)
+                        b_con = np.zeros((1, n), dtype=bool)
                     else:
-                        idx = [c2i(nBaths, (l, b)) for b in range(valBaths[l], nBaths[l])]
-                        b_con = tuple(itertools.combinations(idx, n_con))
-                    for bi in b_imp:
-                        for bv in b_val:
-                            for bc in b_con:
-                                basis_l[l].append(bi + bv + bc)
-    n = sum(2 * (2 * ang + 1) + nb for ang, nb in nBaths.items())
-    basis = []
-    for conf in itertools.product(*basis_l.values()):
-        basis.append(codec.tuple_to_bytes(tuple(sorted(itertools.chain.from_iterable(conf))), n))
-    return tuple(basis)
+                        b_con = _combination_masks([c2i(nBaths, (l, b_)) for b_ in range(valBaths[l], nBaths[l])],
+                                                   n_con, n)
+                    blocks.append((b_imp[:, None, None, :] | b_val[None, :, None, :] | b_con[None, None, :, :])
+                                  .reshape(-1, n))
+        parts.append(np.concatenate(blocks, 0) if blocks else np.zeros((0, n), dtype=bool))
+    occ = np.zeros((1, n), dtype=bool)
+    for part in parts:
+        occ = (occ[:, None, :] | part[None, :, :]).reshape(-1, n)
+    packed = np.packbits(occ, axis=1, bitorder="big")
+    return tuple(row.tobytes() for row in packed)
 
 
 # ---------------------------------------------------------------------------------------

@@ -86,3 +86,32 @@ def test_locality_order_blocks_by_non_lead_orbitals():
     assert key == sorted(key)
     # no orbital stands out: the sorted order is kept
     assert locality_order(basis, _Op(np.full(n_orb, 3))) is None
+
+
+def test_combination_masks_follow_itertools_order():
+    import itertools
+
+    from impuritymodel_gb300.finite import _combination_masks
+
+    for m in range(0, 9):
+        idx = list(range(3, 3 + m))
+        for k in range(0, m + 2):
+            cs = list(itertools.combinations(idx, k))
+            ref = np.zeros((len(cs), 16), dtype=bool)
+            for i, c in enumerate(cs):
+                ref[i, list(c)] = True
+            got = _combination_masks(idx, k, 16)
+            assert got.shape == ref.shape and (got == ref).all(), (m, k)
+
+
+def test_get_basis_equals_upstream_order():
+    """The bit-mask basis enumeration gives upstream's basis in upstream's order (the oracle
+    restates upstream's itertools loops), for the 26- and 316-spin-orbital models and random
+    models."""
+    import oracle.ed_oracle as O
+    from impuritymodel_gb300 import finite, models
+
+    for mod in [models.make_model("config1"), models.make_model("config4")] + [
+            models.random_model(s, 1 + s % 5) for s in range(4)]:
+        args = mod.basis_args()
+        assert finite.get_basis(*args) == tuple(O.get_basis(*args))
