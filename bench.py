@@ -684,15 +684,23 @@ def large_config(eng, K=150, n_states=1):
     n = mod.n_spin_orbitals
     out = {"model": "316 spin-orbitals (6 2p + 10 3d + 300 bath), seed 3, <=2 bath holes", "krylov": K,
            "states": n_states}
-    t0 = time.perf_counter()
-    basis = finite.get_basis(*mod.basis_args())
-    dop = DeviceOp(mod.hOp, eng.device)
+    # the ground state twice: the first call also pays the process's first use of these
+    # shapes (the Lanczos CTA autotuner for this size, library module loading), the second is
+    # the steady state; each from the model dict (basis enumeration included)
+    gs_times = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        basis = finite.get_basis(*mod.basis_args())
+        dop = DeviceOp(mod.hOp, eng.device)
+        restr = make_restrictions(mod.restrictions, n)
+        sb = finite._SortedBasis(eng, list(basis), n)
+        es, psi_t = finite.eigensystem_device(eng, dop, sb, n_states, precision=3)
+        torch.cuda.synchronize()
+        gs_times.append(time.perf_counter() - t0)
     mop = MatfreeOp(mod.hOp, n, eng.device)
-    restr = make_restrictions(mod.restrictions, n)
-    sb = finite._SortedBasis(eng, list(basis), n)
-    es, psi_t = finite.eigensystem_device(eng, dop, sb, n_states, precision=3)
-    torch.cuda.synchronize()
-    out["gs"] = {"sector": len(basis), "s": round(time.perf_counter() - t0, 3), "e0": float(es[0])}
+    out["gs"] = {"sector": len(basis), "s": round(gs_times[1], 3), "first_call_s": round(gs_times[0], 3),
+                 "e0": float(es[0])}
     w = np.linspace(-25.0, 25.0, 2000)
     fams = {"PS": ([DeviceOp(t, eng.device) for t in mod.ps_ops()], -w, -0.2),
             "XPS": ([DeviceOp(t, eng.device) for t in mod.ps_ops(l=1)], -w, -0.2),

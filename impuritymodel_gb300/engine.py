@@ -34,37 +34,46 @@ class DeviceOp:
     """
 
     def __init__(self, op, device):
-        keys = list(op.keys())
-        t = len(keys)
+        t = len(op)
         ops = np.zeros(t, dtype=np.uint64)
         flags = np.zeros(t, dtype=np.uint32)
         coeff = np.zeros((t, 2), dtype=np.float64)
+        enc = {}  # (index, 'c'|'a') -> (16-bit code, index, created); each pair validated once
         max_orb = -1
-        moved = []  # orbitals whose occupation an off-diagonal term changes
-        for k, key in enumerate(keys):
+        for k, (key, val) in enumerate(op.items()):
             if len(key) > 4:
                 raise ValueError("terms with more than four operators are not supported")
             packed = 0
-            cre, ann = [], []
-            for j, (i, a) in enumerate(key):
-                if a not in ("c", "a"):
-                    raise ValueError("Operator type unknown: {}".format(a))
-                i = int(i)
-                if not 0 <= i < 1024:
-                    raise ValueError("spin-orbital index out of range: %d" % i)
-                max_orb = max(max_orb, i)
-                packed |= (0x8000 | (0x4000 if a == "c" else 0) | i) << (16 * j)
-                (cre if a == "c" else ann).append(i)
+            cre = []
+            ann = []
+            for j, pair in enumerate(key):
+                e = enc.get(pair)
+                if e is None:
+                    i, a = pair
+                    if a not in ("c", "a"):
+                        raise ValueError("Operator type unknown: {}".format(a))
+                    i = int(i)
+                    if not 0 <= i < 1024:
+                        raise ValueError("spin-orbital index out of range: %d" % i)
+                    e = enc[pair] = (0x8000 | (0x4000 if a == "c" else 0) | i, i, a == "c")
+                packed |= e[0] << (16 * j)
+                (cre if e[2] else ann).append(e[1])
+                if e[1] > max_orb:
+                    max_orb = e[1]
             ops[k] = packed
-            flags[k] = (1 if sorted(cre) == sorted(ann) else 0) | (len(key) << 8)
-            if sorted(cre) != sorted(ann):
-                moved += sorted(set(cre) ^ set(ann))
-            v = complex(op[key])
-            coeff[k] = (v.real, v.imag)
+            if len(cre) == 1 and len(ann) == 1:
+                diag = cre[0] == ann[0]
+            else:
+                diag = sorted(cre) == sorted(ann)
+            flags[k] = (1 if diag else 0) | (len(key) << 8)
+            v = complex(val)
+            coeff[k, 0] = v.real
+            coeff[k, 1] = v.imag
         self.n_terms = t
         self.max_orbital = max_orb
-        # off-diagonal terms moving each orbital (host; orders sector rows for locality)
-        self.moves = np.bincount(np.array(moved, dtype=np.int64), minlength=max_orb + 1)
+        self._ops_host = ops
+        self._flags_host = flags
+        self._moves = None
         self.is_real = bool(np.all(coeff[:, 1] == 0.0))
         self.nbytes = ops.nbytes + coeff.nbytes + flags.nbytes
         self.ops = torch.from_numpy(ops.view(np.int64)).to(device)
@@ -72,6 +81,28 @@ class DeviceOp:
         self.flags = torch.from_numpy(flags.view(np.int32)).to(device)
         self.terms = L.Terms(self.ops.data_ptr() if t else 0, self.coeff.data_ptr() if t else 0,
                              self.flags.data_ptr() if t else 0, t)
+
+    @property
+    def moves(self):
+        """Off-diagonal terms moving each orbital (host array [max_orbital + 1]): orbitals in the
+        symmetric difference of a term's created and annihilated sets (orders sector rows for
+        locality)."""
+        if self._moves is None:
+            t = self.n_terms
+            code = np.stack([(self._ops_host >> np.uint64(16 * j)) & np.uint64(0xFFFF) for j in range(4)], 1)
+            code = code.astype(np.int64).reshape(t, 4)
+            valid = (code & 0x8000) != 0
+            orb = np.where(valid, code & 0x3FF, -1)
+            cre = valid & ((code & 0x4000) != 0)
+            ann = valid & ~cre
+            same = orb[:, :, None] == orb[:, None, :]
+            in_cre = (same & cre[:, None, :]).any(2)
+            in_ann = (same & ann[:, None, :]).any(2)
+            first = ~np.tril(same, -1).any(2)  # first slot holding this orbital
+            off = (self._flags_host & 1) == 0
+            moved = valid & (in_cre != in_ann) & first & off[:, None]
+            self._moves = np.bincount(orb[moved], minlength=self.max_orbital + 1)
+        return self._moves
 
 
 def make_restrictions(restrictions, n_spin_orbitals):
