@@ -386,8 +386,9 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3, orders=("sorted", "loca
     _, n_heavy = eng.spmv_plan(csr, mapping[1], mapping[2])
     return {
         "bound": "hbm",
-        "kernel": ("spmv_pages_kernel<float> (edgpu_spmv_paged_c64)"
-                   if mapping[0] == "pages" else "spmv_sched_kernel<float> (edgpu_spmv_planned_c64)"),
+        "kernel": {"pages": "spmv_pages_kernel<float> (edgpu_spmv_paged_c64)",
+                   "tma": "spmv_pages_tma_kernel (edgpu_spmv_paged_tma_c64)"}.get(
+                       mapping[0], "spmv_sched_kernel<float> (edgpu_spmv_planned_c64)"),
         "achieved": round(achieved, 1),
         "peak": peak,
         "unit": "GB/s",
@@ -396,7 +397,8 @@ def hv_roofline(eng, peaks, R=16, launches=30, warmup=3, orders=("sorted", "loca
         "algorithmic_bytes_per_launch": int(alg),
         "avg_launch_us": round(avg_s * 1e6, 2),
         "launches": launches,
-        "mapping": {"kernel": mapping[0], "window": mapping[1], "heavy_min": mapping[2], "unroll": mapping[3],
+        "mapping": {"kernel": mapping[0], "window": mapping[1], "heavy_min": mapping[2],
+                    ("slots" if mapping[0] == "tma" else "unroll"): mapping[3],
                     ("page_entries" if mapping[0] == "pages" else "block"): mapping[4], "flags": mapping[5],
                     "heavy_rows": int(n_heavy), "tune_s": round(tune_s, 3),
                     "candidates_us": get_tuner_report("spmv", eng.spmv_key(csr, R, 1))},

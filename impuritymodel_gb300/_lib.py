@@ -102,6 +102,7 @@ SIGNATURES = {
     "edgpu_spmv_pages_build": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _I64, C.POINTER(_I64), _P, _SZ, _P]),
     "edgpu_spmv_paged": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _P, _I, _P]),
     "edgpu_spmv_paged_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _I, _P, _P, _I, _P]),
+    "edgpu_spmv_paged_tma_c64": (_I, [C.POINTER(CSR), _P, _I64, _I, _I, _P, _P, _I, _P, _P]),
     "edgpu_hv_diag": (_I, [_I, _P, _I64, C.POINTER(Terms), _P, _P]),
     "edgpu_state_hash_build": (_I, [_I, _P, _I64, _P, _I64, _P]),
     "edgpu_hv_matfree": (_I, [_I, _P, _I64, _P, _I64, _I, _P, C.POINTER(Terms), _I, C.POINTER(Restrictions), _P, _D,

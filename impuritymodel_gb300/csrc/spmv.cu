@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "pages.cuh"
 
 namespace edgpu {
 namespace {
@@ -219,32 +220,6 @@ int spmv_planned(const edgpu_csr* h, const int32_t* sched, int64_t n_heavy, int 
 // xor shuffles) and opens the next.  The only memory latencies on a warp's path are the page
 // copy and the gathers; the rows, columns and values come from shared memory.
 // ---------------------------------------------------------------------------------------
-template <typename T, bool VALC>
-struct Ent;
-template <>
-struct __align__(8) Ent<float, false> {
-  int32_t c;
-  float v;
-  __device__ __forceinline__ int flag() const { return __float_as_int(v); }
-  __device__ __forceinline__ void set_flag(int f) { v = __int_as_float(f); }
-};
-template <>
-struct __align__(16) Ent<double, false> {
-  int32_t c;
-  int32_t aux;
-  double v;
-  __device__ __forceinline__ int flag() const { return aux; }
-  __device__ __forceinline__ void set_flag(int f) { aux = f; }
-};
-template <>
-struct __align__(16) Ent<float, true> {
-  int32_t c;
-  int32_t aux;
-  float vr, vi;
-  __device__ __forceinline__ int flag() const { return aux; }
-  __device__ __forceinline__ void set_flag(int f) { aux = f; }
-};
-
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");

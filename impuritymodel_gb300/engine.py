@@ -794,6 +794,11 @@ class Engine:
     SPMV_UNROLL = (4, 8)
     SPMV_BLOCK = (128, 256)
     SPMV_PAGES = (256, 512, 1024)
+    SPMV_SLOTS = (8, 16, 32)  # columns in flight per warp of the tensor-memory-accelerator form
+    # The tensor-memory-accelerator form is not among the autotuner's candidates: on the
+    # 462 120-state PS sector (R = 16, 128-byte x rows) it took 196-508 us against 51-53 us for
+    # the per-lane gathers (one bulk-tensor operation per four 128-byte rows).
+    SPMV_TMA = False
 
     @staticmethod
     def spmv_planned_ok(R, precision):
@@ -809,7 +814,10 @@ class Engine:
         one warp each, light rows in length-sorted windows;
         ("pages", window, heavy_min, unroll, page_entries, flags): the same schedule packed
         into pages that one warp each copies into shared memory (real values, or complex64);
-        flags bit 0 keeps two batches of gathers in flight, bit 1 adds L2 eviction hints."""
+        flags bit 0 keeps two batches of gathers in flight, bit 1 adds L2 eviction hints;
+        ("tma", window, heavy_min, slots, page_entries, 0): the same pages with the x rows
+        gathered into shared memory by bulk-tensor gathers, `slots` columns in flight per warp
+        (complex64 vectors)."""
         out = [("sched", w, hm, u, b, 0) for w in self.SPMV_WINDOWS for hm in self.SPMV_HEAVY
                for u in self.SPMV_UNROLL for b in self.SPMV_BLOCK]
         lanes = R // (2 if precision else 1)
@@ -824,6 +832,9 @@ class Engine:
                     need = groups * (max(hm, -(-max_len // groups)) + 2)
                     out += [("pages", w, hm, u, ch, f) for u in self.SPMV_UNROLL for ch in self.SPMV_PAGES
                             for f in (0, 1, 2, 3) if need <= ch]
+                    if precision and self.SPMV_TMA:  # complex64: x rows by bulk-tensor gathers
+                        out += [("tma", w, hm, sl, ch, 0) for sl in self.SPMV_SLOTS for ch in self.SPMV_PAGES
+                                if need <= ch]
         return out
 
     @staticmethod
@@ -891,6 +902,12 @@ class Engine:
     def _spmv_planned(self, csr, xr, yr, R, precision, mapping):
         kernel, w, hm, u, last, flags = mapping
         sched, nh = self.spmv_plan(csr, w, hm)
+        if kernel == "tma":
+            buf, npg = self.spmv_pages(csr, w, hm, R // 2, last, self._pages_kind(csr, precision))
+            L.check(self.lib.edgpu_spmv_paged_tma_c64(C.byref(csr.struct()), _ptr(buf), npg, int(last), int(u),
+                                                      _ptr(xr), _ptr(yr), int(R), _ptr(self.status), self.stream),
+                    "spmv_paged_tma")
+            return
         if kernel == "pages":
             lanes = R // (2 if precision else 1)
             buf, npg = self.spmv_pages(csr, w, hm, lanes, last, self._pages_kind(csr, precision))

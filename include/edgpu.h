@@ -242,6 +242,20 @@ int edgpu_spmv_paged_c64(const edgpu_csr* h, const void* pages, int64_t n_pages,
                          int flags, const float* x, float* y, int R, void* stream);
 
 /*
+ * The same product from the same pages with the x rows brought into shared memory by the
+ * tensor memory accelerator: each page column's x rows (one per row group) are fetched by
+ * cp.async.bulk.tensor tile::gather4 copies (four rows each, from a 2-D tensor map of x) into a
+ * ring of `slots` (2..32) column buffers per warp with one mbarrier each; lane 0 keeps `slots`
+ * columns in flight and the lanes add the products from shared memory.  complex64 vectors, R in
+ * {4, 8, 16, 32} (pages built for R / 2 lanes), page_entries in {256, 512, 1024}, x and y
+ * 16-byte aligned, n < 2^31; y equals edgpu_spmv_paged_c64's bit for bit.  Waits are bounded: a
+ * barrier that does not complete sets *status_dev = EDGPU_ERR_NOCONV (y then incomplete).
+ * Replaces upstream's h.dot (finite.py:1946-1989).
+ */
+int edgpu_spmv_paged_tma_c64(const edgpu_csr* h, const void* pages, int64_t n_pages, int page_entries, int slots,
+                             const float* x, float* y, int R, int32_t* status_dev, void* stream);
+
+/*
  * Batched Lanczos tridiagonalisation without reorthogonalisation, R independent runs on one
  * CSR matrix.  Replaces upstream ``get_tridiagonal_krylov_vectors`` (finite.py:1897-1995):
  * same recurrence (alpha_j = Re<H v_j, v_j>, w = H v_j - alpha_j v_j - beta_{j-1} v_{j-1},

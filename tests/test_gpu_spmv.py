@@ -113,3 +113,29 @@ def test_autotuner_picks_and_caches_a_mapping(eng, tmp_path):
     assert t2.lookup("spmv", key) == best
     times = t2.report("spmv")["spmv|" + ",".join(str(k) for k in key)]["times_us"]
     assert len(times) == len(cands) and all(v > 0 for v in times.values())
+
+
+@pytest.mark.parametrize("complex_vals", [False, True])
+def test_tma_gather_form_equals_paged_form(eng, complex_vals):
+    """The tensor-memory-accelerator form (x rows by bulk-tensor gathers into shared memory)
+    gives the paged form's product bit for bit, for every ring size and page size, on a matrix
+    with heavy and empty rows; no wait runs out."""
+    from impuritymodel_gb300 import finite
+
+    n = 6000
+    h = _matrix(n, 5 + complex_vals, complex_vals)
+    csr = finite._scipy_to_device_csr(eng, h)
+    csr.mixed()
+    rng = np.random.default_rng(11)
+    eng.reset_status()
+    for R in (4, 8, 16, 32):
+        x = torch.from_numpy(rng.standard_normal((n, R)) + 1j * rng.standard_normal((n, R))).to(eng.device)
+        pages = [m for m in eng.spmv_candidates(csr, R, 1) if m[0] == "pages" and m[3] == 4 and m[5] == 0]
+        tma = [("tma", m[1], m[2], sl, m[4], 0) for m in pages[::3] for sl in eng.SPMV_SLOTS]
+        assert tma
+        for m in tma:
+            paged = ("pages", m[1], m[2], 4, m[4], 0)
+            y_t = eng.spmv(csr, x, precision=1, mapping=m)
+            y_p = eng.spmv(csr, x, precision=1, mapping=paged)
+            assert torch.equal(y_t, y_p), (R, m)
+    assert int(eng.status.item()) == 0
