@@ -710,7 +710,7 @@ def large_config(eng, K=150, n_states=1):
     for name, (tops, mesh, delta) in fams.items():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        g64, info = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=1)
+        g64, info = spectra_large(eng, dop, mop, restr, tops, psi_t, es, mesh, delta, K=K, precision=1, matfree=True)
         torch.cuda.synchronize()
         t64 = time.perf_counter() - t0
         sector = info.pop("sector_obj")

@@ -281,13 +281,14 @@ def _sector_operator(eng, sector, dop, mop, order, precision, matfree):
     return apply_h, 0.0
 
 
-def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K=150, precision=1, matfree=True,
-                order=True):
+def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K=150, precision=1, matfree=False,
+                order=False):
     """Continued-fraction Green's functions of R normalised start vectors ``v0`` [n, R] on a
     large ``sector`` (its sorted basis and, for the CSR path, its Hamiltonian).
 
-    ``precision=1``: complex64 vectors, H matrix-free (or the complex64 CSR copy), FP64
-    reductions; ``precision=0``: complex128 vectors on the FP64 CSR (the reference).
+    ``precision=1``: complex64 vectors, H from the complex64 CSR copy (or matrix-free with
+    ``matfree``, for sectors whose matrix is not to be stored), FP64 reductions;
+    ``precision=0``: complex128 vectors on the FP64 CSR (the reference).
     ``order``: the recurrence runs on the rows in :func:`locality_order` (v0 is permuted in,
     the coefficients do not depend on the row order).  Returns (g [R, n_omega] complex128
     host, alpha, beta, k_len)."""
@@ -327,8 +328,8 @@ def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, prec
     return eng.to_host(g), a, b, k_len
 
 
-def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, precision=1, matfree=True,
-                  slaterWeightMin=1e-7, sector=None, order=True):
+def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, precision=1, matfree=False,
+                  slaterWeightMin=1e-7, sector=None, order=False):
     """Spectra ``g[n_states, n_ops, n_w]`` of transition operators on large sectors (upstream
     getSpectra, impurityModel/ed/spectra.py:684-806: T psi, normalised, Green's function
     scaled by the squared norm), every (operator, state) run in one batched recurrence on the

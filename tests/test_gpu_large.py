@@ -91,7 +91,8 @@ def test_reorth_lanczos_and_spectra_316_orbitals(eng, small316):
     es, psi_t = finite.eigensystem_device(eng, s["dop"], s["sb"], 1)
     w = np.linspace(-15, 15, 600)
     ps = [DeviceOp(t, eng.device) for t in mod.ps_ops()[:4]]
-    g64, info = spectra_large(eng, s["dop"], s["mop"], s["restr"], ps, psi_t, es, -w, -0.2, K=120, precision=1)
+    g64, info = spectra_large(eng, s["dop"], s["mop"], s["restr"], ps, psi_t, es, -w, -0.2, K=120, precision=1,
+                              matfree=True)
     sector = info["sector_obj"]
     assert info["runs"] == 4 and info["sector"] > 1000
     g128, _ = spectra_large(eng, s["dop"], s["mop"], s["restr"], ps, psi_t, es, -w, -0.2, K=120, precision=0,
