@@ -26,6 +26,11 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else C.c_void_p(0)
 
 
+# packed operators and flags by key sequence: operators of the same structure (an ensemble's
+# models of one bath size differ only in their coefficients) are encoded once
+_TERM_ENCODING = {}
+
+
 class DeviceOp:
     """Operator dict compiled to the device term table of ``edgpu_terms``.
 
@@ -35,12 +40,27 @@ class DeviceOp:
 
     def __init__(self, op, device):
         t = len(op)
+        keys = tuple(op.keys())
+        coeff = np.array(list(op.values()), dtype=np.complex128).reshape(t).view(np.float64).reshape(t, 2).copy()
+        hit = _TERM_ENCODING.get(keys)
+        if hit is None:
+            ops, flags, max_orb = self._encode(keys)
+            if len(_TERM_ENCODING) >= 64:
+                _TERM_ENCODING.clear()
+            _TERM_ENCODING[keys] = (ops, flags, max_orb)
+        else:
+            ops, flags, max_orb = hit
+        self._finish(t, ops, flags, coeff, max_orb, device)
+
+    @staticmethod
+    def _encode(keys):
+        """Packed operators and flags of a key sequence (validated)."""
+        t = len(keys)
         ops = np.zeros(t, dtype=np.uint64)
         flags = np.zeros(t, dtype=np.uint32)
-        coeff = np.zeros((t, 2), dtype=np.float64)
         enc = {}  # (index, 'c'|'a') -> (16-bit code, index, created); each pair validated once
         max_orb = -1
-        for k, (key, val) in enumerate(op.items()):
+        for k, key in enumerate(keys):
             if len(key) > 4:
                 raise ValueError("terms with more than four operators are not supported")
             packed = 0
@@ -66,9 +86,9 @@ class DeviceOp:
             else:
                 diag = sorted(cre) == sorted(ann)
             flags[k] = (1 if diag else 0) | (len(key) << 8)
-            v = complex(val)
-            coeff[k, 0] = v.real
-            coeff[k, 1] = v.imag
+        return ops, flags, max_orb
+
+    def _finish(self, t, ops, flags, coeff, max_orb, device):
         self.n_terms = t
         self.max_orbital = max_orb
         self._ops_host = ops

@@ -223,8 +223,8 @@ def ensemble_xas_setup(eng, sectors, energies, psis, omega, delta, krylovSize=15
         t_dops = [_device_op(t, eng) for t in sec.model.xas_ops()]
         ps = psis[m]
         run_states, run_amps, e_runs = [], [], []
-        per_t = [eng.apply_vectors([p[0] for p in ps], [p[1] for p in ps], tdop, sec.restr, slaterWeightMin)
-                 for tdop in t_dops]
+        # every polarisation on every eigenstate in one pass (one scan, one sort, one unique)
+        per_t = eng.apply_vectors_multi([p[0] for p in ps], [p[1] for p in ps], t_dops, sec.restr, slaterWeightMin)
         for q in range(len(ps)):
             for t in range(len(t_dops)):
                 o_s, o_a = per_t[t][q]

@@ -223,7 +223,9 @@ def green_setup(eng, dop, restr, run_states, run_amps, krylovSize=150, precision
     else:
         scale_h = np.ones(runs) if scales is None else np.asarray(scales, dtype=np.float64)
     v0 = torch.zeros((sector.n, live.size), dtype=torch.complex128, device=eng.device)
-    v0.index_put_((rows[sel].clamp_min(0), lr[sel]), vals[sel], accumulate=True)
+    # a run's start states are distinct (dict keys, or unique outputs of an operator
+    # application), so every (row, run) pair is written once: a plain scatter
+    v0[rows[sel].clamp_min(0), lr[sel]] = vals[sel]
     if perturb is not None:
         # verification only: relative start-vector perturbation (eps, seed) to measure how
         # much the unreorthogonalised recurrence amplifies rounding-level differences
