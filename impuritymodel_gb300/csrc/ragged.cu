@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(kRaggedThreads)
   }
 }
 
-// Lanczos with full reorthogonalisation (two classical Gram-Schmidt passes), one CTA per run;
+// Lanczos with full reorthogonalisation (classical Gram-Schmidt, a second pass where the DGKS
+// test asks), one CTA per run;
 // the Krylov basis of run r at V + run_V0[r] ([k_max[r]][n] complex128), the work vector and
 // projections in shared memory.  beta[r][k_max-1] is the residual coupling of the last step
 // (for Ritz residual estimates); no vector is formed from it.
@@ -183,8 +184,12 @@ __global__ void __launch_bounds__(kRaggedThreads)
       }
       if (tid == 0) alpha[(int64_t)r * K + j] = a;
       const int m = j + 1;
-      double nrm = 0.0;
+      // classical Gram-Schmidt against the whole basis, a second pass only when the first
+      // removed more than half of |w|^2 (the test of Daniel, Gragg, Kaufman and Stewart with
+      // eta = 1/sqrt(2): |w_before|^2 = |w_after|^2 + |h|^2, so the test is |h|^2 > |w_after|^2)
+      double wn = 0.0;  // |w|^2 after the last pass (block sum)
       for (int pass = 0; pass < 2; ++pass) {
+        double nrm = 0.0;
         __syncthreads();
         for (int k = warp; k < m; k += nwarps) {
           const double2* vk = Vr + (int64_t)k * n;
@@ -215,10 +220,16 @@ __global__ void __launch_bounds__(kRaggedThreads)
           x.x -= acc.x;
           x.y -= acc.y;
           w[i] = x;
-          if (pass == 1) nrm += x.x * x.x + x.y * x.y;
+          nrm += x.x * x.x + x.y * x.y;
+        }
+        wn = rg_block_sum(nrm, red);
+        if (pass == 0) {
+          double hh = 0.0;
+          for (int k = tid; k < m; k += bs) hh += h[k].x * h[k].x + h[k].y * h[k].y;
+          if (!(rg_block_sum(hh, red) > wn)) break;  // the same decision in every thread
         }
       }
-      const double b = sqrt(rg_block_sum(nrm, red));
+      const double b = sqrt(wn);
       if (tid == 0) beta[(int64_t)r * K + j] = b;
       if (j + 1 == km) break;
       if (!(b > 0.0)) {

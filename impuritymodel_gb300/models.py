@@ -23,6 +23,7 @@ cubic orbital minor), then all hoppings in the same order; both spins share a dr
 
 from __future__ import annotations
 
+import functools
 import math
 from collections import OrderedDict
 from fractions import Fraction
@@ -36,6 +37,7 @@ K_B = 8.617333262e-05  # Boltzmann constant in eV/K (CODATA 2018, as scipy.const
 # ----------------------------------------------------------------------------------------
 
 
+@functools.lru_cache(maxsize=None)
 def _racah_3j_parts(j1, j2, j3, m1, m2, m3):
     """Return (sign, A, S) with 3j = sign * sqrt(A) * S, A and S rational (integer j)."""
     if m1 + m2 + m3 != 0:
@@ -64,6 +66,7 @@ def wigner3j(j1, j2, j3, m1, m2, m3):
     return sign * math.sqrt(float(a)) * float(s)
 
 
+@functools.lru_cache(maxsize=None)
 def gaunt_c(k, l, m, lp, mp):
     r"""Coulomb-expansion Gaunt coefficient :math:`c^k(l m; l' m')`.
 

@@ -483,7 +483,8 @@ size_t edgpu_lanczos_ragged_smem(int64_t max_rows);
 int edgpu_lanczos_ragged(const edgpu_csr* h, const edgpu_ragged* rg, const double* v0, const int32_t* k_max, int K,
                          double* alpha, double* beta, int32_t* status_dev, void* stream);
 
-/* Lanczos with full reorthogonalisation (two classical Gram-Schmidt passes) for every run of
+/* Lanczos with full reorthogonalisation (classical Gram-Schmidt against the whole basis, a
+ * second pass only when the first removed more than half of |w|^2) for every run of
  * a ragged batch in one launch, one CTA per run.  Run r keeps its Krylov basis at
  * V + 2 * run_V0[r] doubles ([k_max[r]][n] complex128, caller-allocated); beta[r][k_max-1] is
  * the last step's residual norm (Ritz residual estimates); breakdown before k_max sets
