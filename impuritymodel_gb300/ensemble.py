@@ -145,22 +145,70 @@ def ensemble_ground_states(eng, sectors, n_states=3, k_start=120, tol_rel=1e-12,
                 retry.append(i)
         if done:
             X = eng.combine_ragged(batch, V, run_V0, k, S)
-            for r, i, q in done:
-                n = sectors[i].csr.n
-                base = Q * int(batch.run_vec0_h[r])
-                out = []
-                for qq in range(q):
-                    v = X[base + qq * n: base + (qq + 1) * n]
-                    v = v / torch.linalg.vector_norm(v)
-                    keep = (v.real ** 2 + v.imag ** 2) >= slaterWeightMin
-                    idx = torch.nonzero(keep).flatten()
-                    out.append((sectors[i].sb.sorted[idx].contiguous(), torch.view_as_real(v[idx]).contiguous()))
-                psis[i] = out
+            _ritz_states(eng, sectors, batch, X, Q, done, slaterWeightMin, psis)
         if retry and k_cap >= max(sectors[i].csr.n for i in retry):
             raise RuntimeError("ensemble ground states: no convergence at the full basis size")
         todo = retry
         k_cap *= 2
     return energies, psis
+
+
+def _ritz_states(eng, sectors, batch, X, Q, done, slaterWeightMin, psis):
+    """psis[i] = [(states, amps)] of the converged models' Ritz vectors, all at once: the
+    vectors (segments of X) padded into one [segments, max rows] array, normalised, pruned at
+    |amp|^2 < slaterWeightMin with one nonzero, then split per (model, state) with one host
+    read of the segment counts."""
+    dev = eng.device
+    # models grouped by state width (words per state), each group's bases concatenated: the
+    # segments of a group are then contiguous in the nonzero output and gather from one array
+    done = sorted(done, key=lambda d: int(sectors[d[1]].sb.sorted.shape[1]))
+    seg_model, seg_base, seg_n, seg_q, row0, seg_group = [], [], [], [], [], []
+    groups = []  # (width, [bases])
+    off = 0
+    for r, i, q in done:
+        b = sectors[i].sb.sorted
+        if not groups or groups[-1][0] != int(b.shape[1]):
+            groups.append((int(b.shape[1]), []))
+            off = 0
+        n = sectors[i].csr.n
+        base = Q * int(batch.run_vec0_h[r])
+        for qq in range(q):
+            seg_model.append(i)
+            seg_base.append(base + qq * n)
+            seg_n.append(n)
+            seg_q.append(qq)
+            row0.append(off)
+            seg_group.append(len(groups) - 1)
+        groups[-1][1].append(b)
+        off += n
+    ns = len(seg_n)
+    width = max(seg_n)
+    n_h = np.asarray(seg_n, dtype=np.int64)
+    cols = torch.arange(width, device=dev).view(1, -1)
+    nt = torch.from_numpy(n_h).to(dev).view(-1, 1)
+    valid = cols < nt
+    src = torch.from_numpy(np.asarray(seg_base, dtype=np.int64)).to(dev).view(-1, 1) + cols
+    P = torch.where(valid, X[src.clamp(max=X.numel() - 1)], torch.zeros((), dtype=X.dtype, device=dev))
+    P = P / torch.linalg.vector_norm(P, dim=1, keepdim=True)
+    keep = valid & ((P.real ** 2 + P.imag ** 2) >= slaterWeightMin)
+    seg, col = torch.nonzero(keep, as_tuple=True)  # grouped by segment, rows in order
+    counts = torch.bincount(seg, minlength=ns).cpu().numpy()
+    rows = torch.from_numpy(np.asarray(row0, dtype=np.int64)).to(dev)[seg] + col
+    am = torch.view_as_real(P[seg, col]).contiguous()
+    am_parts = torch.split(am, counts.tolist())
+    ends = np.cumsum(counts)
+    gseg = np.asarray(seg_group)
+    st_parts = []
+    for g, (_, bs) in enumerate(groups):
+        segs = np.nonzero(gseg == g)[0]
+        lo = int(ends[segs[0]] - counts[segs[0]])
+        hi = int(ends[segs[-1]])
+        st_g = torch.cat(bs, 0)[rows[lo:hi]]
+        st_parts += list(torch.split(st_g, counts[segs].tolist()))
+    for t, i in enumerate(seg_model):
+        if seg_q[t] == 0:
+            psis[i] = []
+        psis[i].append((st_parts[t].contiguous(), am_parts[t].contiguous()))
 
 
 class RaggedSpectra:

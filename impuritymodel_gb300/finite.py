@@ -241,6 +241,9 @@ def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
     parts = []
     for l in nBaths.keys():
         blocks = []
+        idx_imp = [c2i(nBaths, (l, s_, m_)) for s_ in range(2) for m_ in range(-l, l + 1)]
+        idx_val = [c2i(nBaths, (l, b_)) for b_ in range(valBaths[l])]
+        idx_con = [c2i(nBaths, (l, b_)) for b_ in range(valBaths[l], nBaths[l])]
         for dn_val in range(dnValBaths[l] + 1):
             for dn_con in range(dnConBaths[l] + 1):
                 dn_imp = dn_val - dn_con
@@ -251,17 +254,15 @@ def get_basis(nBaths, valBaths, dnValBaths, dnConBaths, dnTol, n0imp):
                     assert n_val <= valBaths[l]
                     assert n_con <= nBaths[l] - valBaths[l]
                     assert n_imp <= 2 * (2 * l + 1)
-                    idx = [c2i(nBaths, (l, s_, m_)) for s_ in range(2) for m_ in range(-l, l + 1)]
-                    b_imp = _combination_masks(idx, n_imp, n)
+                    b_imp = _combination_masks(idx_imp, n_imp, n)
                     if valBaths[l] == 0:
                         b_val = np.zeros((1, n), dtype=bool)
                     else:
-                        b_val = _combination_masks([c2i(nBaths, (l, b_)) for b_ in range(valBaths[l])], n_val, n)
+                        b_val = _combination_masks(idx_val, n_val, n)
                     if nBaths[l] - valBaths[l] == 0:
                         b_con = np.zeros((1, n), dtype=bool)
                     else:
-                        b_con = _combination_masks([c2i(nBaths, (l, b_)) for b_ in range(valBaths[l], nBaths[l])],
-                                                   n_con, n)
+                        b_con = _combination_masks(idx_con, n_con, n)
                     blocks.append((b_imp[:, None, None, :] | b_val[None, :, None, :] | b_con[None, None, :, :])
                                   .reshape(-1, n))
         parts.append(np.concatenate(blocks, 0) if blocks else np.zeros((0, n), dtype=bool))

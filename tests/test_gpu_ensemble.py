@@ -12,7 +12,9 @@ from impuritymodel_gb300 import models as M
 
 pytestmark = pytest.mark.gpu
 
-MODELS = [(11, 1), (12, 2), (13, 1)]  # (seed, bath levels per 3d spin-orbital)
+# (seed, bath levels per 3d spin-orbital); the last model has two words per state, the
+# others one (ragged batches mix state widths)
+MODELS = [(11, 1), (12, 2), (13, 1), (14, 5)]
 
 
 @pytest.fixture(scope="module")
