@@ -105,6 +105,10 @@ const char* edgpu_status_string(int status);
  *             (complex128; conjugated when conj_vals != 0).
  * scratch_entries: per-warp capacity for off-diagonal emissions (0 = default 256); on
  * overflow *status_dev receives EDGPU_ERR_OVERFLOW and the caller retries larger.
+ * Work per state: with a power-of-two capacity and a term index that fits in shared memory,
+ * only the terms whose created orbitals are empty in the state are tried (terms bucketed by
+ * created orbital per block) and equal outputs are merged through a hash table; otherwise
+ * every term is tried on every state.  Both give the same outputs bit for bit.
  */
 int edgpu_apply_columns(int n_words, const uint64_t* states, int64_t n_states, const edgpu_terms* terms,
                         const edgpu_restrictions* restr, double weight_min, const uint64_t* basis,
