@@ -142,7 +142,7 @@ def hv_matfree_into(eng, basis_sorted, mop, restr, diag, x, y, shift=0.0, table=
     return y
 
 
-def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0, reorth="dgks"):
+def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0, reorth="dgks", stats=None):
     """Batched Lanczos with full reorthogonalisation against the whole basis, for R runs at
     once.
 
@@ -156,8 +156,9 @@ def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0, reorth="
 
     ``v0`` [n, R] complex128, each column normalised; ``apply_h(x, y)`` writes y = (H - shift)
     x for [n, R] vectors of the run dtype (complex64 for ``precision=1``, complex128 for 0).
-    Returns (alpha [R, K], beta [R, K] host float64 with ``shift`` added back to alpha,
-    k_len [R]: the Krylov size of each run, cut at its first zero beta)."""
+    ``stats`` (a dict, optional) accumulates ``second_passes``: the steps that took a second
+    Gram-Schmidt pass.  Returns (alpha [R, K], beta [R, K] host float64 with ``shift`` added
+    back to alpha, k_len [R]: the Krylov size of each run, cut at its first zero beta)."""
     if reorth not in ("dgks", "cgs2"):
         raise ValueError("reorth must be 'dgks' or 'cgs2'")
     n, R = v0.shape
@@ -228,7 +229,8 @@ def lanczos_reorth_batched(eng, apply_h, v0, K, precision=1, shift=0.0, reorth="
         z = np.nonzero(b[r] == 0.0)[0]
         if z.size:
             k_len[r] = int(z[0]) + 1
-    lanczos_reorth_batched.second_passes = second
+    if stats is not None:
+        stats["second_passes"] = stats.get("second_passes", 0) + second
     return a, b, k_len
 
 
@@ -282,7 +284,7 @@ def _sector_operator(eng, sector, dop, mop, order, precision, matfree):
 
 
 def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K=150, precision=1, matfree=False,
-                order=False):
+                order=False, stats=None):
     """Continued-fraction Green's functions of R normalised start vectors ``v0`` [n, R] on a
     large ``sector`` (its sorted basis and, for the CSR path, its Hamiltonian).
 
@@ -297,10 +299,10 @@ def green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, omega, delta, K
     _, perm = ordered_sector(eng, sector, dop, order)
     if perm is not None:
         v0 = v0[perm]
-    return _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision)
+    return _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision, stats)
 
 
-def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision):
+def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, precision, stats=None):
     """green_large after the row order and the operator are fixed."""
     # the H.v kernels serve R / (complex numbers per 16 bytes) lanes per row, a divisor of
     # 32: the run count is padded with empty runs (they stop at their first step)
@@ -308,7 +310,7 @@ def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, prec
     runs16 = 2 if precision else 1
     if R > 32 * runs16:  # more runs than one H.v launch serves: in chunks
         parts = [_green_ordered(eng, apply_h, shift, v0[:, c:c + 32 * runs16], scale[c:c + 32 * runs16],
-                                e_runs[c:c + 32 * runs16], omega, delta, K, precision)
+                                e_runs[c:c + 32 * runs16], omega, delta, K, precision, stats)
                  for c in range(0, R, 32 * runs16)]
         Kc = max(p[1].shape[1] for p in parts)
         pad = lambda x: np.pad(x, ((0, 0), (0, Kc - x.shape[1])))  # noqa: E731
@@ -319,7 +321,7 @@ def _green_ordered(eng, apply_h, shift, v0, scale, e_runs, omega, delta, K, prec
         Rp *= 2
     if Rp != R:
         v0 = torch.cat([v0, torch.zeros((v0.shape[0], Rp - R), dtype=v0.dtype, device=v0.device)], 1)
-    a, b, k_len = lanczos_reorth_batched(eng, apply_h, v0, K, precision, shift)
+    a, b, k_len = lanczos_reorth_batched(eng, apply_h, v0, K, precision, shift, stats=stats)
     a, b, k_len = a[:R], b[:R], k_len[:R]
     at = torch.from_numpy(np.ascontiguousarray(a)).to(eng.device)
     bt = torch.from_numpy(np.ascontiguousarray(b)).to(eng.device)
@@ -366,9 +368,10 @@ def spectra_large(eng, dop, mop, restr, t_dops, psi_t, es, w, delta, K=150, prec
         scale[r] = nrm * nrm
         v0[rows, r] = vals / nrm
     e_runs = [es[i] for i, _ in runs]
+    stats = {}
     gr, a, b, k_len = green_large(eng, dop, mop, restr, sector, v0, scale, e_runs, w, delta, K, precision, matfree,
-                                  order)
+                                  order, stats)
     for r, (i, o) in enumerate(runs):
         g[i, o] = gr[r]
     return g, {"runs": R, "sector": int(n), "k_len": [int(x) for x in k_len], "sector_obj": sector,
-               "sector_s": sector_s, "second_passes": getattr(lanczos_reorth_batched, "second_passes", None)}
+               "sector_s": sector_s, "second_passes": stats.get("second_passes", 0)}
