@@ -826,6 +826,51 @@ def krylov_roofline(eng, peaks, n=462120, R=16, K=150, ms=(1, 16, 75, 150), prec
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
 
 
+def sector_build_timing(eng, reps=2):
+    """Expansion and CSR of the 316-spin-orbital model's photoemission sector (462 120 states
+    from the c_i images of its 47 895-state ground basis): wall time of each, device
+    synchronised, the second of ``reps`` builds reported (the first also loads modules)."""
+    import torch
+
+    from impuritymodel_gb300 import finite, models
+    from impuritymodel_gb300.engine import DeviceOp, make_restrictions
+
+    mod = models.make_model("config4")
+    n = mod.n_spin_orbitals
+    dop = DeviceOp(mod.hOp, eng.device)
+    restr = make_restrictions(mod.restrictions, n)
+    sb = finite._SortedBasis(eng, list(finite.get_basis(*mod.basis_args())), n)
+    ps = DeviceOp(mod.ps_ops()[0], eng.device)
+    amps = torch.zeros((sb.sorted.shape[0], 2), dtype=torch.float64, device=eng.device)
+    amps[:, 0] = 1.0
+    (st, _), = eng.apply_vectors([sb.sorted], [amps], ps, restr, 0.0)
+    out = {}
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        basis, _ = eng.expand(eng.sort_unique(st), dop, restr)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        csr = eng.build_csr(basis, dop, restr)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out = {"states": int(basis.shape[0]), "nnz": int(csr.nnz), "expand_s": round(t1 - t0, 4),
+               "csr_s": round(t2 - t1, 4), "terms": int(dop.n_terms)}
+    return out
+
+
+def run_sector_only(args):
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from impuritymodel_gb300.engine import get_engine
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps({"sector_build": sector_build_timing(get_engine())}))
+
+
 def run_krylov_only(args):
     import torch
 
@@ -1274,6 +1319,8 @@ def main():
     ap.add_argument("--large-only", action="store_true", help="only the 316-spin-orbital large-sector line")
     ap.add_argument("--hv-only", action="store_true",
                     help="only the H.v roofline measurement (the case profiled under ncu)")
+    ap.add_argument("--sector-only", action="store_true",
+                    help="only the 316-orbital PS sector construction (the case profiled under ncu)")
     ap.add_argument("--krylov-only", action="store_true",
                     help="only the large-sector Krylov kernel timings (the case profiled under ncu)")
     ap.add_argument("--krylov-k", type=int, default=150, help="basis vectors held by --krylov-only")
@@ -1293,6 +1340,8 @@ def main():
         run_hv_only(args)
     elif args.krylov_only:
         run_krylov_only(args)
+    elif args.sector_only:
+        run_sector_only(args)
     elif args.large_only:
         run_large_only()
     elif args.profile_step:
