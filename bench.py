@@ -859,6 +859,90 @@ def sector_build_timing(eng, reps=2):
     return out
 
 
+def gemm_timing(eng, peaks, batch=4096, wide=65536, reps=20):
+    """The tcgen05 GEMMs of the basis-pruning network: the five of one training step at batch
+    ``batch`` (forward layers 1 and 2 with the bias + ReLU epilogue, the weight gradients dW2
+    and dW1 with K = batch, the ReLU-mask backward dH1) and the first forward layer on
+    ``wide`` rows (ranking a large candidate set); per GEMM the mean CUDA-event time of
+    back-to-back calls and 2 M N K flops over it, against the measured bf16 burst peak (the
+    operands, a few MB, stay in L2); and one whole training step (gradients + Adam)."""
+    import numpy as np
+    import torch
+
+    from impuritymodel_gb300 import pruning
+    from impuritymodel_gb300.engine import _ptr
+
+    dev = eng.device
+    g = torch.Generator(device=dev).manual_seed(0)
+    net = pruning.BasisNet(eng, seed=0)
+    B = batch
+    bf = torch.bfloat16
+    X = (torch.rand((B, pruning.N_IN), device=dev, generator=g) < 0.2).to(bf)
+    Xt = X.t().contiguous()
+    H1, H2, dH2, dH1 = (torch.rand((B, pruning.N_H), device=dev, generator=g).to(bf) for _ in range(4))
+    H1t, dH2t, dH1t = (torch.rand((pruning.N_H, B), device=dev, generator=g).to(bf) for _ in range(3))
+    Yt = torch.empty((pruning.N_H, B), dtype=bf, device=dev)
+    Xw = (torch.rand((wide, pruning.N_IN), device=dev, generator=g) < 0.2).to(bf)
+    Yw = torch.empty((wide, pruning.N_H), dtype=bf, device=dev)
+    Y = torch.empty((B, pruning.N_H), dtype=bf, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps * 1e3
+
+    nh, ni = pruning.N_H, pruning.N_IN
+    cases = [
+        ("forward1", (B, nh, ni), lambda: net._gemm(1, X, net.W1b, B, nh, ni, bias=net.p["b1"], Y=Y, Yt=Yt)),
+        ("forward2", (B, nh, nh), lambda: net._gemm(1, H1, net.W2b, B, nh, nh, bias=net.p["b2"], Y=Y, Yt=Yt)),
+        ("dW2", (nh, nh, B), lambda: net._gemm(0, dH2t, H1t, nh, nh, B, C=net.g["W2"])),
+        ("dH1", (B, nh, nh), lambda: net._gemm(2, dH2, net.W2t, B, nh, nh, mask=H1, Y=dH1, Yt=Yt)),
+        ("dW1", (nh, ni, B), lambda: net._gemm(0, dH1t, Xt, nh, ni, B, C=net.g["W1"])),
+        ("forward1_wide", (wide, nh, ni), lambda: net._gemm(1, Xw, net.W1b, wide, nh, ni, bias=net.p["b1"], Y=Yw)),
+    ]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = peaks.get("bf16_tflops")
+    out = {}
+    for name, (M, N, K), fn in cases:
+        us = timed(fn)
+        tf = 2.0 * M * N * K / us / 1e6
+        # the library's tile-width rule: widest of 256 / 64 / 16 dividing N with >= 4/5 of the SMs busy
+        bn = next((w for w in (256, 64, 16) if N % w == 0 and (M // 128) * (N // w) >= sms * 4 // 5), 16)
+        out[name] = {"M": M, "N": N, "K": K, "tile": [128, bn], "ctas": (M // 128) * (N // bn), "us": round(us, 2),
+                     "tflops": round(tf, 2), "frac": round(tf / peak, 4) if peak else None}
+    target = torch.randn(B, device=dev, generator=g)
+
+    def train_step():
+        net.gradients(X, Xt, target)
+        net.adam_step()
+
+    step_us = timed(train_step)
+    eng.read_status("gemm timing")
+    flops = 2.0 * B * (nh * ni + nh * nh) * 3
+    return {"gemms": out, "train_step_us": round(step_us, 1),
+            "train_tflops": round(flops / step_us / 1e6, 2), "batch": B,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst, of measured)", "inputs": "L2-resident"}
+
+
+def run_gemm_only(args):
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from impuritymodel_gb300.engine import get_engine
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps({"gemm": gemm_timing(get_engine(), read_peaks())}))
+
+
 def run_sector_only(args):
     import torch
 
@@ -1323,6 +1407,8 @@ def main():
                     help="only the 316-orbital PS sector construction (the case profiled under ncu)")
     ap.add_argument("--krylov-only", action="store_true",
                     help="only the large-sector Krylov kernel timings (the case profiled under ncu)")
+    ap.add_argument("--gemm-only", action="store_true",
+                    help="only the tensor-core GEMM timings of the pruning network (the case profiled under ncu)")
     ap.add_argument("--krylov-k", type=int, default=150, help="basis vectors held by --krylov-only")
     ap.add_argument("--krylov-m", default="1,16,75,150", help="vectors per pass timed by --krylov-only")
     ap.add_argument("--hv-order", choices=["both", "sorted", "locality"], default="both",
@@ -1342,6 +1428,8 @@ def main():
         run_krylov_only(args)
     elif args.sector_only:
         run_sector_only(args)
+    elif args.gemm_only:
+        run_gemm_only(args)
     elif args.large_only:
         run_large_only()
     elif args.profile_step:

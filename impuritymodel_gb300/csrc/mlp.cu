@@ -2,39 +2,47 @@
 //
 // The network ranks candidate product states during basis pruning (no counterpart in
 // upstream impurityModel, whose expand_basis keeps every state of the closure,
-// impurityModel/ed/finite.py:1696-1803).  Its GEMMs run on tcgen05: one thread issues
-// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor memory) on operand tiles
-// staged in shared memory; the accumulator is read back with tcgen05.ld for a fused
-// epilogue (bias, ReLU, ReLU mask, transposed copies for the backward pass).
+// impurityModel/ed/finite.py:1696-1803).  Its GEMMs run on tcgen05 fed by the tensor memory
+// accelerator: one thread keeps a ring of K tiles in flight (2-D bulk-tensor copies into
+// shared memory, completion on one mbarrier per stage) and issues tcgen05.mma (kind::f16,
+// BF16 operands, FP32 accumulator in tensor memory) on each tile as it lands; every tile's
+// MMAs commit to the stage's second mbarrier, which frees the stage for the tile S ahead.
+// The accumulator is read back with tcgen05.ld for a fused epilogue (bias, ReLU, ReLU mask,
+// transposed copies for the backward pass) with 16-byte stores.
 //
 // One primitive covers forward and backward: C[M][N] = A[M][K] * B[N][K]^T with A and B
-// row-major ("K-major") BF16, K a multiple of 64, M a multiple of 128, N a multiple of 16
-// and at most 256.  Every wait on the MMA completion barrier has an iteration limit after
-// which the kernel records EDGPU_ERR_NOCONV, waits (bounded) once more, frees its tensor
+// row-major ("K-major") BF16, K a multiple of 64, M a multiple of 128, N a multiple of 16.
+// The tile width (256, 64 or 16 columns) is the widest that still gives most SMs a tile.
+// Every mbarrier wait has an iteration limit after which the kernel records
+// EDGPU_ERR_NOCONV, waits (bounded) for its copies and MMAs still in flight, frees its tensor
 // memory and returns.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace edgpu {
 
 constexpr int kGemmThreads = 128;  // 4 warps: tensor-memory lanes 0-127 = tile rows
 constexpr int kBM = 128, kBK = 64;
-constexpr uint32_t kLBO = 128;   // bytes between core matrices adjacent along K
-constexpr uint32_t kSBO = 1024;  // bytes between core matrices adjacent along M/N (8 K-chunks)
+constexpr uint32_t kSwizzleAtom = 1024;  // 8 rows x 128 bytes: one repeat of the 128-byte swizzle
 constexpr long long kWaitLimit = 1LL << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Shared-memory matrix descriptor, no swizzle, K-major canonical layout: core matrices of
-// 8 rows x 16 bytes stored contiguously, LBO apart along K and SBO apart along M/N.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte swizzled layout: rows
+// of 64 BF16 (128 bytes) one after another, the 16-byte chunks of row r permuted by XOR with
+// r % 8, groups of 8 rows 1024 bytes apart (SBO); the leading-dimension offset is unused in
+// this layout (encoded as 1).  `saddr` is the tile base (1024-byte aligned) plus 32 bytes per
+// 16-column K step.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((kLBO >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((kSBO >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of the tcgen05 family
-  return d;                // base offset 0, absolute LBO mode, no swizzle
+  d |= (uint64_t)1 << 16;                     // LBO (unused)
+  d |= (uint64_t)(kSwizzleAtom >> 4) << 32;   // SBO
+  d |= (uint64_t)1 << 46;                     // descriptor version of the tcgen05 family
+  d |= (uint64_t)2 << 61;                     // 128-byte swizzle; base offset 0
+  return d;
 }
 
 // Instruction descriptor of kind::f16: D F32, A and B BF16, both K-major, M x N.
@@ -44,6 +52,10 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 
 __device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_test(uint64_t* m, uint32_t phase) {
@@ -63,6 +75,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t phase) {
   return false;
 }
 
+// Box {64 columns, box rows} of the 2-D BF16 tensor `map` at (column x, row y) into dst,
+// 128-byte swizzled.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -75,6 +97,8 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
       : "memory");
 }
 
+// The barrier's next phase completes once every tcgen05 operation this thread issued so far
+// has completed.
 __device__ __forceinline__ void mma_commit(uint64_t* m) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(m))
                : "memory");
@@ -93,18 +117,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-// Copy a [rows x 64] BF16 tile (row-major source, leading dimension ld elements) into the
-// canonical no-swizzle K-major layout; rows past `valid` are zero.
-__device__ __forceinline__ void stage_tile(unsigned char* dst, const __nv_bfloat16* src, int64_t ld, int rows,
-                                           int valid) {
-  for (int c = threadIdx.x; c < rows * 8; c += blockDim.x) {
-    const int row = c >> 3, kc = c & 7;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (row < valid) v = *reinterpret_cast<const uint4*>(src + (int64_t)row * ld + kc * 8);
-    *reinterpret_cast<uint4*>(dst + (row >> 3) * kSBO + kc * kLBO + (row & 7) * 16) = v;
-  }
-}
-
 enum GemmEpilogue : int {
   kEpiStoreF32 = 0,   // C (float) = acc
   kEpiBiasRelu = 1,   // Y = relu(acc + bias[col]) -> BF16 Y[row][col] and Yt[col][row]
@@ -121,27 +133,48 @@ struct GemmArgs {
   __nv_bfloat16* Y;          // [M][N]
   __nv_bfloat16* Yt;         // [N][M] (may be null)
   int32_t* status;
+  int vec;                   // C, Y and mask 16-byte aligned: 16-byte row stores and loads
+};
+
+// Shared-memory ring of a 128 x BN tile.  One stage holds the K tile (64 columns) of A and of
+// B, each one 2-D bulk-tensor box {64, rows} in the 128-byte swizzled layout (one 128-byte
+// request per row), each 1024-byte aligned.  The narrow 16-column tiles run only where the
+// grid is small (a few row tiles, long K: the weight gradients), so they keep 8 stages in
+// flight; the wider ones 4 or 3 (two or one CTAs per SM).
+template <int BN>
+struct GemmTile {
+  static constexpr int kStages = BN <= 16 ? 8 : (BN >= 256 ? 3 : 4);
+  static constexpr uint32_t kABytes = kBM * kBK * 2;          // 16 KiB
+  static constexpr uint32_t kBBytes = BN * kBK * 2;
+  static constexpr uint32_t kStageBytes = kABytes + kBBytes;  // a multiple of 1 KiB
+  static constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024;  // + alignment of the ring
 };
 
 template <int EPI, int BN>
-__global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs g) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* sA = sm;                   // kBM x kBK bf16 = 16 KiB
-  unsigned char* sB = sm + kBM * kBK * 2;   // BN x kBK bf16
-  __shared__ uint64_t mbar;
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
+                        GemmArgs g) {
+  using T = GemmTile<BN>;
+  constexpr int S = T::kStages;
+  extern __shared__ unsigned char sm[];
+  __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
-  constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  const uint32_t ring = (smem_u32(sm) + 1023u) & ~1023u;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(kCols)
+                 "r"(T::kCols)
                  : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(&mbar, 1);
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -149,98 +182,201 @@ __global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs 
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  const uint32_t idesc = idesc_bf16(kBM, BN);
   const int ktiles = g.K / kBK;
-  const int valid_a = min(kBM, g.M - m0), valid_b = min(BN, g.N - n0);
-  uint32_t phase = 0;
-  for (int kt = 0; kt < ktiles; ++kt) {
-    stage_tile(sA, g.A + (int64_t)m0 * g.K + kt * kBK, g.K, kBM, valid_a);
-    stage_tile(sB, g.B + (int64_t)n0 * g.K + kt * kBK, g.K, BN, valid_b);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic smem writes -> async proxy
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      auto load = [&](int t) {  // K tile t into stage t % S
+        const int s = t % S;
+        const uint32_t a = ring + (uint32_t)s * T::kStageBytes, b = a + T::kABytes;
+        mbar_expect_tx(&full[s], T::kStageBytes);
+        tma_load_2d(a, &amap, t * kBK, m0, &full[s]);
+        tma_load_2d(b, &bmap, t * kBK, n0, &full[s]);
+      };
+      int issued = 0, consumed = 0;
+      bool ok = true;
+      for (; issued < S && issued < ktiles; ++issued) load(issued);
+      for (int kt = 0; kt < ktiles; ++kt) {
+        const int s = kt % S;
+        if (!mbar_wait(&full[s], (uint32_t)(kt / S) & 1u)) {
+          ok = false;
+          break;
+        }
+        ++consumed;
+        tc_fence_after();
+        const uint32_t a = ring + (uint32_t)s * T::kStageBytes, b = a + T::kABytes;
 #pragma unroll
-      for (int k16 = 0; k16 < kBK / 16; ++k16)
-        mma_bf16(tmem, smem_desc(a0 + k16 * 2 * kLBO), smem_desc(b0 + k16 * 2 * kLBO), idesc,
-                 (kt > 0 || k16 > 0) ? 1u : 0u);
-      mma_commit(&mbar);
+        for (int k16 = 0; k16 < kBK / 16; ++k16)
+          mma_bf16(tmem, smem_desc_sw128(a + (uint32_t)k16 * 32u), smem_desc_sw128(b + (uint32_t)k16 * 32u), idesc,
+                   (kt > 0 || k16 > 0) ? 1u : 0u);
+        mma_commit(&empty[s]);
+        // refill the previous tile's stage once its MMAs are done (this tile's are queued
+        // behind them, so the tensor pipe stays busy meanwhile)
+        const int p = kt - 1;
+        if (p >= 0 && p + S < ktiles) {
+          if (!mbar_wait(&empty[p % S], (uint32_t)(p / S) & 1u)) {
+            ok = false;
+            break;
+          }
+          load(p + S);
+          ++issued;
+        }
+      }
+      mma_commit(&done);
+      if (!ok) {
+        atomicExch(&failed, 1);
+        for (int t = consumed; t < issued; ++t) mbar_wait(&full[t % S], (uint32_t)(t / S) & 1u);  // copies in flight
+      }
     }
-    // every thread waits: the tiles are overwritten next iteration, and the epilogue reads
-    // the accumulator after the last one
-    if (!mbar_wait(&mbar, phase)) failed = 1;
-    phase ^= 1u;
-    __syncthreads();
-    if (failed) break;
+    __syncwarp();
   }
+  if (!mbar_wait(&done, 0u)) atomicExch(&failed, 1);
+  __syncthreads();
   tc_fence_after();
   if (failed) {
-    if (tid == 0) {
-      atomicExch(g.status, (int32_t)EDGPU_ERR_NOCONV);
-      mbar_wait(&mbar, phase ^ 1u);  // bounded second chance for the MMAs in flight
-    }
+    if (tid == 0) atomicExch(g.status, (int32_t)EDGPU_ERR_NOCONV);
   } else {
-    // epilogue: warp w owns tensor-memory lanes (= tile rows) 32w .. 32w+31
+    // epilogue: warp w owns tensor-memory lanes (= tile rows) 32w .. 32w+31; M % 128 == 0
+    // and N % BN == 0, so every row and column of the tile exists
     const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     for (int c0 = 0; c0 < BN; c0 += 16) {
       float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row >= g.M) continue;
+      tmem_ld16(trow + (uint32_t)c0, v);
+      const int col0 = n0 + c0;
+      const int64_t off = (int64_t)row * g.N + col0;
+      if (EPI == kEpiStoreF32) {
+        if (g.vec) {
+          float4* dst = reinterpret_cast<float4*>(g.C + off);
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int col = n0 + c0 + q;
-        if (col >= g.N) break;
-        float y = v[q];
-        if (EPI == kEpiStoreF32) {
-          g.C[(int64_t)row * g.N + col] = y;
-          continue;
+          for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) g.C[off + q] = v[q];
         }
-        if (EPI == kEpiBiasRelu) y = fmaxf(y + g.bias[col], 0.0f);
-        if (EPI == kEpiReluMask) y = (__bfloat162float(g.mask[(int64_t)row * g.N + col]) > 0.0f) ? y : 0.0f;
-        const __nv_bfloat16 yb = __float2bfloat16_rn(y);
-        g.Y[(int64_t)row * g.N + col] = yb;
-        if (g.Yt) g.Yt[(int64_t)col * g.M + row] = yb;
+        continue;
+      }
+      if (EPI == kEpiBiasRelu) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = fmaxf(v[q] + g.bias[col0 + q], 0.0f);
+      }
+      if (EPI == kEpiReluMask) {
+        uint32_t mw[8];
+        if (g.vec) {
+          const uint4* src = reinterpret_cast<const uint4*>(g.mask + off);
+          const uint4 m_lo = src[0], m_hi = src[1];
+          mw[0] = m_lo.x, mw[1] = m_lo.y, mw[2] = m_lo.z, mw[3] = m_lo.w;
+          mw[4] = m_hi.x, mw[5] = m_hi.y, mw[6] = m_hi.z, mw[7] = m_hi.w;
+        } else {
+          const unsigned short* src = reinterpret_cast<const unsigned short*>(g.mask + off);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) mw[q] = (uint32_t)src[2 * q] | ((uint32_t)src[2 * q + 1] << 16);
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const float m = __uint_as_float(((mw[q >> 1] >> (16 * (q & 1))) & 0xFFFFu) << 16);  // BF16 -> FP32
+          v[q] = m > 0.0f ? v[q] : 0.0f;
+        }
+      }
+      uint32_t pk[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+        pk[q] = *reinterpret_cast<const uint32_t*>(&h);
+      }
+      if (g.vec) {
+        uint4* dst = reinterpret_cast<uint4*>(g.Y + off);
+        dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+      } else {
+        unsigned short* dst = reinterpret_cast<unsigned short*>(g.Y + off);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) dst[q] = (unsigned short)(pk[q >> 1] >> (16 * (q & 1)));
+      }
+      if (g.Yt) {
+        unsigned short* dst = reinterpret_cast<unsigned short*>(g.Yt);
+#pragma unroll
+        for (int q = 0; q < 16; ++q)  // lanes write consecutive rows: 64-byte runs per warp
+          dst[(int64_t)(col0 + q) * g.M + row] = (unsigned short)(pk[q >> 1] >> (16 * (q & 1)));
       }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::kCols) : "memory");
+}
+
+// [rows][K] row-major BF16 as a 2-D tensor map with box {64 columns, box_rows rows}, 128-byte
+// swizzled in shared memory.
+bool gemm_operand_map(CUtensorMap* map, const __nv_bfloat16* ptr, int K, int rows, int box_rows) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1u, 1u};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(ptr), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <int EPI, int BN>
 int launch_gemm(const GemmArgs& g, cudaStream_t s) {
-  const size_t smem = (size_t)(kBM + BN) * kBK * 2 + 1024;
-  // at least ~100 KiB per CTA keeps two CTAs per SM at most: 2 x 256 tensor-memory columns
-  const size_t req = smem < 100 * 1024 ? 100 * 1024 : smem;
-  auto* kern = gemm_bf16_tc_kernel<EPI, BN>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req) != cudaSuccess)
+  using T = GemmTile<BN>;
+  alignas(64) CUtensorMap amap, bmap;
+  if (!gemm_operand_map(&amap, g.A, g.K, g.M, kBM) || !gemm_operand_map(&bmap, g.B, g.K, g.N, BN))
     return EDGPU_ERR_CUDA;
-  dim3 grid((g.M + kBM - 1) / kBM, (g.N + BN - 1) / BN);
-  kern<<<grid, kGemmThreads, req, s>>>(g);
+  auto* kern = gemm_bf16_tc_kernel<EPI, BN>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem) != cudaSuccess)
+    return EDGPU_ERR_CUDA;
+  dim3 grid(g.M / kBM, g.N / BN);
+  kern<<<grid, kGemmThreads, T::kSmem, s>>>(amap, bmap, g);
   note_launch();
   return check_launch();
 }
 
-int gemm_bf16(int epi, const GemmArgs& g, cudaStream_t s) {
+// Widest tile (256, 64 or 16 columns dividing N) that still gives about four fifths of the SMs
+// a tile; the narrowest that divides N otherwise.
+int gemm_tile_width(int M, int N) {
+  const int64_t want = (int64_t)grid_cap() * 4 / 5;
+  for (int bn : {256, 64, 16})
+    if (N % bn == 0 && (int64_t)(M / kBM) * (N / bn) >= want) return bn;
+  return 16;
+}
+
+template <int EPI>
+int launch_gemm_bn(const GemmArgs& g, cudaStream_t s) {
+  switch (gemm_tile_width(g.M, g.N)) {
+    case 256:
+      return launch_gemm<EPI, 256>(g, s);
+    case 64:
+      return launch_gemm<EPI, 64>(g, s);
+    default:
+      return launch_gemm<EPI, 16>(g, s);
+  }
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+int gemm_bf16(int epi, GemmArgs g, cudaStream_t s) {
   if (!g.A || !g.B || !g.status || g.M < 1 || g.N < 16 || g.K < kBK || g.K % kBK || g.N % 16 || g.M % kBM)
     return EDGPU_ERR_ARG;
-  if (reinterpret_cast<uintptr_t>(g.A) % 16 || reinterpret_cast<uintptr_t>(g.B) % 16) return EDGPU_ERR_ARG;
-  const int bn = g.N % 256 == 0 ? 256 : (g.N % 64 == 0 ? 64 : 16);
+  if (g.N / 16 > 65535) return EDGPU_ERR_ARG;  // grid.y = N / tile width
+  if (!aligned16(g.A) || !aligned16(g.B)) return EDGPU_ERR_ARG;
   switch (epi) {
     case kEpiStoreF32:
       if (!g.C) return EDGPU_ERR_ARG;
-      return bn == 256 ? launch_gemm<kEpiStoreF32, 256>(g, s)
-                       : (bn == 64 ? launch_gemm<kEpiStoreF32, 64>(g, s) : launch_gemm<kEpiStoreF32, 16>(g, s));
+      g.vec = aligned16(g.C);
+      return launch_gemm_bn<kEpiStoreF32>(g, s);
     case kEpiBiasRelu:
       if (!g.Y || !g.bias) return EDGPU_ERR_ARG;
-      return bn == 256 ? launch_gemm<kEpiBiasRelu, 256>(g, s)
-                       : (bn == 64 ? launch_gemm<kEpiBiasRelu, 64>(g, s) : launch_gemm<kEpiBiasRelu, 16>(g, s));
+      g.vec = aligned16(g.Y);
+      return launch_gemm_bn<kEpiBiasRelu>(g, s);
     case kEpiReluMask:
       if (!g.Y || !g.mask) return EDGPU_ERR_ARG;
-      return bn == 256 ? launch_gemm<kEpiReluMask, 256>(g, s)
-                       : (bn == 64 ? launch_gemm<kEpiReluMask, 64>(g, s) : launch_gemm<kEpiReluMask, 16>(g, s));
+      g.vec = aligned16(g.Y) && aligned16(g.mask);
+      return launch_gemm_bn<kEpiReluMask>(g, s);
     default:
       return EDGPU_ERR_ARG;
   }

@@ -15,10 +15,9 @@
 // Waits are bounded: a barrier that does not complete within kWaitLimit polls sets the status
 // word to EDGPU_ERR_NOCONV; the warp then waits (bounded again) for its own copies still in
 // flight and stops.
-#include <cuda.h>
-
 #include "common.cuh"
 #include "pages.cuh"
+#include "tma.cuh"
 
 namespace edgpu {
 namespace {
@@ -203,22 +202,6 @@ __global__ void __launch_bounds__(32 * kTmaWarps)
     }
     flush();
   }
-}
-
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_tiled() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
 }
 
 template <bool VALC, int R>

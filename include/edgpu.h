@@ -500,10 +500,12 @@ int edgpu_lanczos_reorth_ragged(const edgpu_csr* h, const edgpu_ragged* rg, cons
 
 /*
  * C[M][N] (float32) = A[M][K] * B[N][K]^T with A and B row-major BF16 (K-major), on the
- * tcgen05 tensor cores: operand tiles in shared memory, FP32 accumulator in tensor memory.
- * M % 128 == 0, K % 64 == 0, N % 16 == 0, A and B 16-byte aligned.  A completion wait that
- * runs out of its iteration limit sets *status_dev = EDGPU_ERR_NOCONV.  No counterpart in
- * upstream impurityModel (the GEMM of the basis-pruning network).
+ * tcgen05 tensor cores: K tiles of A and B brought into a shared-memory ring by bulk-tensor
+ * copies (3-4 stages in flight), FP32 accumulator in tensor memory, 128-row tiles 256, 64 or
+ * 16 columns wide (the widest that gives most SMs a tile).  M % 128 == 0, K % 64 == 0,
+ * N % 16 == 0, N <= 1048560, A and B 16-byte aligned (C of any alignment).  A wait that runs
+ * out of its iteration limit sets *status_dev = EDGPU_ERR_NOCONV.  No counterpart in upstream
+ * impurityModel (the GEMM of the basis-pruning network).
  */
 int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev, void* stream);
 
