@@ -3,10 +3,11 @@
 // The network ranks candidate product states during basis pruning (no counterpart in
 // upstream impurityModel, whose expand_basis keeps every state of the closure,
 // impurityModel/ed/finite.py:1696-1803).  Its GEMMs run on tcgen05 fed by the tensor memory
-// accelerator: one thread keeps a ring of K tiles in flight (2-D bulk-tensor copies into
-// shared memory, completion on one mbarrier per stage) and issues tcgen05.mma (kind::f16,
-// BF16 operands, FP32 accumulator in tensor memory) on each tile as it lands; every tile's
-// MMAs commit to the stage's second mbarrier, which frees the stage for the tile S ahead.
+// accelerator: a producer thread keeps a ring of K tiles in flight (2-D bulk-tensor copies
+// into shared memory, completion on one mbarrier per stage), and a second thread issues
+// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor memory) on each tile as
+// it lands, never waiting for the MMAs themselves; every tile's MMAs commit to the stage's
+// second mbarrier, which hands the stage back to the producer for the tile S ahead.
 // The accumulator is read back with tcgen05.ld for a fused epilogue (bias, ReLU, ReLU mask,
 // transposed copies for the backward pass) with 16-byte stores.
 //
@@ -183,50 +184,51 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_base;
   const int ktiles = g.K / kBK;
-  if (warp == 0) {
+  if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(kBM, BN);
-      auto load = [&](int t) {  // K tile t into stage t % S
+      // producer: K tile t into stage t % S once the MMAs of tile t - S have released it
+      int issued = 0;
+      bool ok = true;
+      for (int t = 0; t < ktiles; ++t) {
         const int s = t % S;
+        if (t >= S && !mbar_wait(&empty[s], (uint32_t)(t / S - 1) & 1u)) {
+          ok = false;
+          break;
+        }
+        if (*reinterpret_cast<volatile int*>(&failed)) break;  // the MMA side gave up
         const uint32_t a = ring + (uint32_t)s * T::kStageBytes, b = a + T::kABytes;
         mbar_expect_tx(&full[s], T::kStageBytes);
         tma_load_2d(a, &amap, t * kBK, m0, &full[s]);
         tma_load_2d(b, &bmap, t * kBK, n0, &full[s]);
-      };
-      int issued = 0, consumed = 0;
+        ++issued;
+      }
+      if (!ok) atomicExch(&failed, 1);
+      // every copy issued has landed before the CTA may exit (earlier tiles of a stage were
+      // consumed before its last one was issued)
+      for (int t = issued > S ? issued - S : 0; t < issued; ++t) mbar_wait(&full[t % S], (uint32_t)(t / S) & 1u);
+    }
+    __syncwarp();
+  } else if (warp == 0) {
+    if (lane == 0) {
+      // MMA issuer: never waits for MMAs, so they queue back to back in the tensor pipe
+      const uint32_t idesc = idesc_bf16(kBM, BN);
       bool ok = true;
-      for (; issued < S && issued < ktiles; ++issued) load(issued);
       for (int kt = 0; kt < ktiles; ++kt) {
         const int s = kt % S;
         if (!mbar_wait(&full[s], (uint32_t)(kt / S) & 1u)) {
           ok = false;
           break;
         }
-        ++consumed;
         tc_fence_after();
         const uint32_t a = ring + (uint32_t)s * T::kStageBytes, b = a + T::kABytes;
 #pragma unroll
         for (int k16 = 0; k16 < kBK / 16; ++k16)
           mma_bf16(tmem, smem_desc_sw128(a + (uint32_t)k16 * 32u), smem_desc_sw128(b + (uint32_t)k16 * 32u), idesc,
                    (kt > 0 || k16 > 0) ? 1u : 0u);
-        mma_commit(&empty[s]);
-        // refill the previous tile's stage once its MMAs are done (this tile's are queued
-        // behind them, so the tensor pipe stays busy meanwhile)
-        const int p = kt - 1;
-        if (p >= 0 && p + S < ktiles) {
-          if (!mbar_wait(&empty[p % S], (uint32_t)(p / S) & 1u)) {
-            ok = false;
-            break;
-          }
-          load(p + S);
-          ++issued;
-        }
+        mma_commit(&empty[s]);  // releases the stage to the producer once these MMAs are done
       }
       mma_commit(&done);
-      if (!ok) {
-        atomicExch(&failed, 1);
-        for (int t = consumed; t < issued; ++t) mbar_wait(&full[t % S], (uint32_t)(t / S) & 1u);  // copies in flight
-      }
+      if (!ok) atomicExch(&failed, 1);
     }
     __syncwarp();
   }
