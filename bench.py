@@ -1084,6 +1084,8 @@ def run_gpu(args):
         roof["traffic_source"] = "ncu DRAM bytes of this kernel on this sector, as a ratio, scaled to this launch"
     batched = batched_configs(eng) if (rank == 0 and not args.skip_batched) else None
     prune_info = pruning_setup(eng)[1] if (rank == 0 and not args.skip_batched) else None
+    if prune_info is not None:
+        prune_info["gemm_kernels"] = gemm_timing(eng, peaks)
     large = large_config(eng) if (rank == 0 and not args.skip_batched) else None
     if large is not None:
         large["krylov_kernels"] = krylov_roofline(eng, peaks)
