@@ -907,14 +907,12 @@ def gemm_timing(eng, peaks, batch=4096, wide=65536, reps=20):
         ("dW1", (nh, ni, B), lambda: net._gemm(0, dH1t, Xt, nh, ni, B, C=net.g["W1"])),
         ("forward1_wide", (wide, nh, ni), lambda: net._gemm(1, Xw, net.W1b, wide, nh, ni, bias=net.p["b1"], Y=Yw)),
     ]
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     peak = peaks.get("bf16_tflops")
     out = {}
     for name, (M, N, K), fn in cases:
         us = timed(fn)
         tf = 2.0 * M * N * K / us / 1e6
-        # the library's tile-width rule: widest of 256 / 64 / 16 dividing N with >= 4/5 of the SMs busy
-        bn = next((w for w in (256, 64, 16) if N % w == 0 and (M // 128) * (N // w) >= sms * 4 // 5), 16)
+        bn = int(eng.lib.edgpu_gemm_tile_width(M, N))
         out[name] = {"M": M, "N": N, "K": K, "tile": [128, bn], "ctas": (M // 128) * (N // bn), "us": round(us, 2),
                      "tflops": round(tf, 2), "frac": round(tf / peak, 4) if peak else None}
     target = torch.randn(B, device=dev, generator=g)

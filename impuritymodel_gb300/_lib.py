@@ -148,6 +148,7 @@ SIGNATURES = {
     "edgpu_density_matrix": (_I, [_I, _P, _P, _P, _I, _P, _I, _P, _P]),
     "edgpu_components": (_I, [C.POINTER(CSR), _P, _P, _P]),
     "edgpu_gemm_bf16_epi": (_I, [_I, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "edgpu_gemm_tile_width": (_I, [_I, _I]),
     "edgpu_mlp_bits": (_I, [_P, _I, _I64, _I, _P, _P, _P]),
     "edgpu_mlp_head": (_I, [_P, _P, _P, _I64, _I, _P, _P]),
     "edgpu_mlp_head_backward": (_I, [_P, _P, _P, _P, _I64, _I, _P, _P, _P, _P]),

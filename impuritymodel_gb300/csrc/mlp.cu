@@ -566,6 +566,11 @@ extern "C" int edgpu_mlp_to_bf16(const float* Wf, int rows, int cols, void* Wb, 
   return check_launch();
 }
 
+extern "C" int edgpu_gemm_tile_width(int M, int N) {
+  if (M < kBM || M % kBM || N < 16 || N % 16 || N / 16 > 65535) return 0;
+  return gemm_tile_width(M, N);
+}
+
 extern "C" int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev,
                                void* stream) {
   GemmArgs g{};

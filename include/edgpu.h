@@ -508,6 +508,9 @@ int edgpu_lanczos_reorth_ragged(const edgpu_csr* h, const edgpu_ragged* rg, cons
  * impurityModel (the GEMM of the basis-pruning network).
  */
 int edgpu_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int32_t* status_dev, void* stream);
+/* Columns of the output tiles (256, 64 or 16) edgpu_gemm_bf16 and edgpu_gemm_bf16_epi use for
+ * an M x N product on the current device; 0 when they reject the shape.  Host only. */
+int edgpu_gemm_tile_width(int M, int N);
 
 /*
  * Basis-pruning network (input bits -> 256 -> 256 -> 1, BF16 operands, FP32 accumulation);

@@ -56,6 +56,25 @@ def test_entry_points_reject_bad_arguments_without_a_gpu(lib):
     assert lib.edgpu_cfrac(None, None, None, 1, 1, None, 1, 0.1, None, None, None, None) == L.EDGPU_ERR_ARG
 
 
+def test_gemm_tile_width_rule_without_a_gpu(lib):
+    """The GEMM's tile width: the widest of 256, 64 and 16 columns dividing N whose grid gives
+    four fifths of the SMs a tile, else 16; 0 for shapes the GEMM rejects.  Host-only: without
+    a device the library assumes 148 SMs (118 tiles wanted)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 148
+    want = sms * 4 // 5
+
+    def rule(M, N):
+        return next((w for w in (256, 64, 16) if N % w == 0 and (M // 128) * (N // w) >= want), 16)
+
+    for M, N in [(128, 256), (4096, 256), (4096, 320), (256, 256), (19456, 256), (65536, 256), (384, 48),
+                 (16384, 64), (128, 16)]:
+        assert lib.edgpu_gemm_tile_width(M, N) == rule(M, N), (M, N)
+    for M, N in [(0, 256), (100, 256), (128, 8), (128, 24), (-128, 64)]:
+        assert lib.edgpu_gemm_tile_width(M, N) == 0, (M, N)
+
+
 def test_noalloc_rejects_bad_arguments_without_a_gpu(lib):
     """edgpu_lanczos_noalloc validates its arguments before any CUDA call: bad precision,
     missing outputs and problems larger than the static scratch array return their codes.
